@@ -1,0 +1,402 @@
+"""Benchmark of the pirgpu propagation engine (one JSON line on stdout).
+
+Default workload (one step = one full fixpoint from the initial store):
+1,000,000 int32 variables with lb ~ U[-1e6, 0], ub = lb + U[0, 2e6];
+4,000,000 PIR propagators (45% x=y+z, 15% x=y*z, 5% min, 5% max, 10% x=y-z,
+20% reified x=(y<=z)) with a planted solution, plus a 20,000-link chain
+x_{i+1} = x_i + c_i (c_i ~ U[1, 5]) that keeps changing one bound per round
+for ~20,000 rounds.  Metric: propagator executions per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload single_large|single_small|nodes|uneven|learned]
+
+--impl reference times the reference algorithm's CPU path (the C++
+restatement of lala-pc's PIR::deduce driven by the Gauss-Seidel loop) on
+bounded samples of the same workload on the host cores.
+Under torchrun (N > 1) the single instance does not shard: each rank runs an
+independent replica on its own GPU; value = executions of all ranks / max time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "lala-pc_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+ALG_BYTES_PER_EXEC = 40   # 16 B bytecode + 3 x 8 B intervals read
+ALG_BYTES_PER_JOIN = 4    # one int32 bound written per narrowing join
+L2_FLUSH_BYTES = 256 << 20
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------ CUDA runtime --
+class Cudart:
+    """Minimal libcudart access (pinned host buffers, L2 flush, device sync)."""
+
+    def __init__(self):
+        for name in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+            try:
+                self.L = ctypes.CDLL(name)
+                break
+            except OSError:
+                continue
+        else:
+            raise RuntimeError("libcudart not found")
+        self.flush_ptr = None
+
+    def check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError("%s failed with CUDA error %d" % (what, rc))
+
+    def set_device(self, d):
+        self.check(self.L.cudaSetDevice(d), "cudaSetDevice")
+
+    def sync(self):
+        self.check(self.L.cudaDeviceSynchronize(), "cudaDeviceSynchronize")
+
+    def pinned(self, n, dtype=np.int32):
+        p = ctypes.c_void_p()
+        nbytes = int(n) * np.dtype(dtype).itemsize
+        self.check(self.L.cudaHostAlloc(ctypes.byref(p), ctypes.c_size_t(max(nbytes, 16)), 0),
+                   "cudaHostAlloc")
+        buf = (ctypes.c_byte * max(nbytes, 16)).from_address(p.value)
+        return np.frombuffer(buf, dtype=dtype, count=int(n))
+
+    def flush_l2(self):
+        """Overwrite a 256 MiB buffer (twice the L2) so the next step starts cold."""
+        if self.flush_ptr is None:
+            p = ctypes.c_void_p()
+            self.check(self.L.cudaMalloc(ctypes.byref(p), ctypes.c_size_t(L2_FLUSH_BYTES)), "cudaMalloc")
+            self.flush_ptr = p
+        self.check(self.L.cudaMemset(self.flush_ptr, 1, ctypes.c_size_t(L2_FLUSH_BYTES)), "cudaMemset")
+        self.sync()
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names[1:], f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(name):
+    """DRAM bytes per launch recorded by the ncu summary profiles/<name>.md
+    (line 'traffic_bytes_per_launch: N'), or None."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# --------------------------------------------------------------- workloads --
+def make_workload(name):
+    import workloads as W
+    if name == "single_large":
+        inst = W.single_large(0)
+        desc = ("1,000,000 vars / 4,000,000 propagators (planted solution, bounds scale 1e6) "
+                "+ 20,000-link chain")
+    elif name == "single_small":
+        inst = W.single_small(0)
+        desc = "1,000 vars / 3,000 propagators (planted solution, bounds scale 1e3)"
+    else:
+        raise ValueError(name)
+    return inst, desc
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def dist_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------------- CPU baseline --
+def cpu_sample(inst, target_s=12.0, min_sweeps=1):
+    """Gauss-Seidel sweeps of the oracle from the initial store (reference
+    order), as many as fit in ~target_s; returns (execs/s, sweeps, seconds)."""
+    from oracle import oracle as O
+    s = inst.store()
+    st, perm = O.install(inst.op, inst.x, inst.y, inst.z, s)
+    op, x, y, z = (np.ascontiguousarray(a[perm]) for a in (inst.op, inst.x, inst.y, inst.z))
+    t0 = time.perf_counter()
+    O.sweeps(op, x, y, z, s, 1)
+    one = time.perf_counter() - t0
+    n = max(min_sweeps, int(target_s / max(one, 1e-9)) - 1)
+    t0 = time.perf_counter()
+    O.sweeps(op, x, y, z, s, n)
+    dt = time.perf_counter() - t0
+    return (n * inst.nprops) / dt, n + 1, dt + one, (n + 1) * inst.nprops / (dt + one)
+
+
+# ------------------------------------------------------------------- ours ---
+def run_ours(args):
+    import pirgpu
+    ws, rank, local = dist_env()
+    dist = dist_init(ws)
+    cr = Cudart()
+    cr.set_device(local)
+    inst, desc = make_workload(args.workload)
+    ctx = pirgpu.Context(local)
+    ctx.load_store(inst.lb, inst.ub)
+    ctx.tell(inst.op, inst.x, inst.y, inst.z)
+    snap = ctx.snapshot()
+    nprops = ctx.num_deductions()
+    kw = dict(mode=args.mode)
+
+    def step():
+        ctx.restore(snap)
+        rc, st = ctx.fixpoint(**kw)
+        if rc != pirgpu.OK:
+            raise RuntimeError("fixpoint status %s" % pirgpu.STATUS[rc])
+        return st
+
+    for _ in range(args.warmup):
+        step()
+        cr.flush_l2()
+    if dist:
+        dist.barrier()
+    cr.sync()
+    clk = ClockSampler(local)
+    clk.start()
+    stats = []
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        stats.append(step())
+        cr.flush_l2()
+    cr.sync()
+    wall = time.perf_counter() - wall0
+    clocks = clk.stop()
+    dev_ms = sum(s["device_ms"] for s in stats)
+    execs = sum(s["executions"] for s in stats)
+    joins = sum(s["narrowed"] for s in stats)
+    rounds = [s["rounds"] for s in stats]
+    t_max = dist_max(dist, dev_ms / 1e3)
+    execs_all = dist_sum(dist, execs)
+    value = execs_all / t_max
+
+    # end to end through the C ABI: pinned host store in, fixpoint, store out
+    lb_h = cr.pinned(inst.nvars)
+    ub_h = cr.pinned(inst.nvars)
+    lb_o = cr.pinned(inst.nvars)
+    ub_o = cr.pinned(inst.nvars)
+    lb_h[:] = inst.lb
+    ub_h[:] = inst.ub
+    init_lb, init_ub = ctx.read_store()  # store after install (reified targets met with [0,1])
+    lb_h[:] = init_lb
+    ub_h[:] = init_ub
+    e2e_steps = max(1, min(args.steps, 3))
+    e2e_execs = 0
+    if dist:
+        dist.barrier()
+    cr.sync()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.load_store(lb_h, ub_h)
+        rc, st = ctx.fixpoint(**kw)
+        ctx._check(ctx._L.pir_read_store(ctx.h, lb_o.ctypes.data_as(pirgpu._I32P),
+                                         ub_o.ctypes.data_as(pirgpu._I32P)))
+        e2e_execs += st["executions"]
+    cr.sync()
+    e2e_t = dist_max(dist, time.perf_counter() - t0)
+    e2e_value = dist_sum(dist, e2e_execs) / e2e_t
+
+    if rank != 0:
+        return
+    hbm, hbm_src = peaks()
+    achieved = (execs * ALG_BYTES_PER_EXEC + joins * ALG_BYTES_PER_JOIN) / (dev_ms / 1e3) / 1e9
+    traffic = ncu_traffic("persistent_fixpoint_" + args.workload)
+    cpu = None
+    if ws == 1 and not args.no_cpu:
+        v, sw, secs, _ = cpu_sample(inst, args.cpu_seconds)
+        cpu = {"value": v, "unit": "executions/s", "cores": 1, "kind": "port",
+               "sample": "%d Gauss-Seidel sweeps (%d executions) of the same instance from its "
+                         "initial store, %.1f s, 1 host thread" % (sw, sw * nprops, secs)}
+    out = {
+        "metric": "propagator executions/sec", "value": value, "unit": "executions/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic: seeded generator, planted-solution instance",
+        "config": {"workload": args.workload + ": " + desc, "nvars": inst.nvars,
+                   "propagators": int(nprops), "parallelism": "replicas" if ws > 1 else "single",
+                   "mode": ["auto", "persistent", "hostloop", "smem"][args.mode],
+                   "l2": "flushed between steps (256 MiB cudaMemset); step timed with CUDA events",
+                   "rounds_per_step": rounds[0], "fixpoint": "bit-exact vs CPU oracle in tests"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "bytes_model": "40 B per execution + 4 B per narrowing join"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "executions/s",
+                "h2d_bytes_per_step": int(inst.nvars * 8), "d2h_bytes_per_step": int(inst.nvars * 8),
+                "steps": e2e_steps},
+        "gpu_launches": args.steps * (1 if args.mode in (0, 1, 3) else rounds[0] * 2),
+        "clocks": clocks,
+        "time_to_fixpoint_ms": dev_ms / args.steps,
+        "wall_s": wall,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    inst, desc = make_workload(args.workload)
+    from oracle import oracle as O
+    s0 = inst.store()
+    st, perm = O.install(inst.op, inst.x, inst.y, inst.z, s0)
+    op, x, y, z = (np.ascontiguousarray(a[perm]) for a in (inst.op, inst.x, inst.y, inst.z))
+    sweeps_per_step = args.ref_sweeps
+    for _ in range(args.warmup):
+        s = s0.copy()
+        O.sweeps(op, x, y, z, s, 1)
+    times, execs = [], 0
+    s = s0.copy()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.sweeps(op, x, y, z, s, sweeps_per_step)
+        times.append(time.perf_counter() - t0)
+        execs += sweeps_per_step * inst.nprops
+    tot = sum(times)
+    v = execs / tot
+    out = {
+        "metric": "propagator executions/sec", "value": v, "unit": "executions/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tot * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic: seeded generator, planted-solution instance",
+        "config": {"workload": args.workload + ": " + desc, "nvars": inst.nvars,
+                   "propagators": int(inst.nprops)},
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": "executions/s", "cores": 1, "kind": "port",
+                         "sample": "each step = %d Gauss-Seidel sweeps over the sorted bytecode "
+                                   "(the reference loop is sequential: 1 host thread)" % sweeps_per_step},
+        "e2e": {"value": v, "unit": "executions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="single_large")
+    ap.add_argument("--mode", type=int, default=1, help="0 auto, 1 persistent, 2 host loop, 3 smem")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-sweeps", type=int, default=3)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        log("note: fewer than 3 warm-up steps")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+/* pirgpu — C ABI of the GB300 (sm_103a) PIR propagation engine.
+ *
+ * Drop-in for lala-pc's PIR abstract domain (include/lala/pir.hpp:53-942) over
+ * a VStore<Interval<ZLB<int>>>: ternary propagators x = y <op> z plus reified
+ * x = (y == z) and x = (y <= z), propagated to a fixpoint over int32 interval
+ * bounds.  Plain pointers and sizes only; host buffers are caller-owned, device
+ * buffers engine-owned.  One CUDA stream per context; a context is not
+ * thread-safe.  Every call returns a pir_status; pir_last_error() gives the
+ * message of the last failing call.
+ *
+ * Variable stores are given as two int32 arrays lb[nvars], ub[nvars].
+ * INT32_MIN as lb and INT32_MAX as ub mean "no bound" (pir.hpp:403-404).
+ * Propagators are given as four int32 arrays (structure of arrays) op[], x[],
+ * y[], z[]: the bytecode_type {Sig op; AVar x, y, z} of pir.hpp:37-47.
+ */
+#ifndef PIRGPU_H
+#define PIRGPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Opcodes: the Sig values PIR accepts (pir.hpp:270-273). */
+enum pir_op {
+  PIR_ADD = 0,  /* x = y + z          pir.hpp:758-766 */
+  PIR_MUL = 1,  /* x = y * z          pir.hpp:767-779 */
+  PIR_TDIV = 2, /* x = y tdiv z       pir.hpp:780-792 */
+  PIR_FDIV = 3, /* x = y fdiv z */
+  PIR_CDIV = 4, /* x = y cdiv z */
+  PIR_EDIV = 5, /* x = y ediv z */
+  PIR_MIN = 6,  /* x = min(y, z)      pir.hpp:793-801 */
+  PIR_MAX = 7,  /* x = max(y, z)      pir.hpp:802-810 */
+  PIR_EQ = 8,   /* x = (y == z)       pir.hpp:730-744 */
+  PIR_LEQ = 9   /* x = (y <= z)       pir.hpp:745-757 */
+};
+
+typedef enum pir_status {
+  PIR_OK = 0,              /* fixpoint reached, store not empty */
+  PIR_FAILED = 1,          /* the store is empty (is_bot(), pir.hpp:831-833): a result, not an error */
+  PIR_TIMEOUT = 2,         /* opts.max_rounds reached before the fixpoint */
+  PIR_BARRIER_TIMEOUT = 3, /* a grid-barrier wait exceeded opts.barrier_timeout_ns */
+  PIR_EINVAL = 4,          /* bad argument (var index, opcode, size); nothing was changed */
+  PIR_ECUDA = 5,           /* CUDA error */
+  PIR_ENOMEM = 6           /* device allocation failed */
+} pir_status;
+
+/* Fixpoint drivers. */
+enum pir_mode {
+  PIR_MODE_AUTO = 0,       /* shared-memory kernel when the instance fits one SM, else persistent */
+  PIR_MODE_PERSISTENT = 1, /* one cooperative launch; AC-1 rounds separated by a bounded grid barrier */
+  PIR_MODE_HOSTLOOP = 2,   /* one launch per round, the host reads the change flag */
+  PIR_MODE_SMEM = 3        /* one CTA, store staged in shared memory (small instances) */
+};
+
+/* Propagator schedules. */
+enum pir_sched {
+  PIR_SCHED_AC1 = 0,      /* every propagator every round (plain AC-1 sweeps) */
+  PIR_SCHED_LEARNED = 1   /* wake set chosen by the trained scorer, certified by a full sweep */
+};
+
+typedef struct pir_opts {
+  int64_t max_rounds;         /* 0: no cap */
+  int64_t barrier_timeout_ns; /* 0: 2 s; bound on every grid-barrier wait */
+  int32_t mode;               /* enum pir_mode */
+  int32_t block;              /* threads per CTA, 0: tuned default */
+  int32_t ctas_per_sm;        /* persistent grid = SMs * ctas_per_sm, 0: occupancy limit */
+  int32_t sched;              /* enum pir_sched */
+  float wake_fraction;        /* learned schedule: fraction of propagators woken per round (0: 1/16) */
+  int32_t reserved[7];
+} pir_opts;
+
+typedef struct pir_stats {
+  int64_t rounds;      /* propagation rounds (AC-1 sweeps), including the final no-change one */
+  int64_t executions;  /* propagator executions */
+  int64_t narrowed;    /* bounds narrowed (atomic joins that changed the store) */
+  float device_ms;     /* device time of the fixpoint (CUDA events on the context stream) */
+  int32_t status;      /* pir_status of the run */
+} pir_stats;
+
+typedef struct pirgpu_ctx pirgpu_ctx;
+typedef struct pirgpu_snapshot pirgpu_snapshot;
+
+/* Context = one PIR over one VStore on one device (PIR::PIR, pir.hpp:158-163). */
+int pir_ctx_create(pirgpu_ctx **out, int device);
+void pir_ctx_destroy(pirgpu_ctx *ctx);
+const char *pir_last_error(const pirgpu_ctx *ctx);
+
+/* Replaces the variable store (VStore construction / sub-domain tell). */
+int pir_load_store(pirgpu_ctx *ctx, int32_t nvars, const int32_t *lb, const int32_t *ub);
+/* Copies the store out (operator[] over all variables, pir.hpp:840-842). */
+int pir_read_store(pirgpu_ctx *ctx, int32_t *lb, int32_t *ub);
+/* operator[](x) / project(x), pir.hpp:840-851. */
+int pir_project(pirgpu_ctx *ctx, int32_t var, int32_t *lb, int32_t *ub);
+/* embed(x, dom), pir.hpp:354-356: meet [lb, ub] into x; *changed = narrowed. */
+int pir_embed(pirgpu_ctx *ctx, int32_t var, int32_t lb, int32_t ub, int *changed);
+
+/* deduce(tell) for the bytecode part of a tell, pir.hpp:326-352: appends n
+ * propagators, meets x of every EQ/LEQ with [0,1] and re-sorts the whole
+ * bytecode by (op, y, x, z) (the CPU order of pir.hpp:343-347).  Var indices
+ * must be < nvars and opcodes valid (PIR_EINVAL otherwise, nothing appended).
+ * *changed is set to 1 when propagators were added (has_changed). */
+int pir_tell(pirgpu_ctx *ctx, int32_t n, const int32_t *op, const int32_t *x, const int32_t *y,
+             const int32_t *z, int *changed);
+/* num_deductions(), pir.hpp:382-384. */
+int64_t pir_num_deductions(const pirgpu_ctx *ctx);
+/* vars(), pir.hpp:853-855. */
+int32_t pir_vars(const pirgpu_ctx *ctx);
+/* The bytecode in engine order (the order deduce(i) and ask(i) index). */
+int pir_get_bytecode(pirgpu_ctx *ctx, int32_t *op, int32_t *x, int32_t *y, int32_t *z);
+
+/* Runs propagators to the fixpoint (the driver loop around deduce(i) of
+ * tests/pir_test.cpp:60-62).  Returns PIR_OK, PIR_FAILED, PIR_TIMEOUT or an
+ * error.  opts may be NULL (defaults); stats may be NULL. */
+int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts, pir_stats *stats);
+/* deduce(i), pir.hpp:387-390: one propagator; *changed = has_changed. */
+int pir_deduce_one(pirgpu_ctx *ctx, int64_t i, int *changed);
+
+/* ask(i), pir.hpp:368-370 and ask(bytecode), :417-438. */
+int pir_ask(pirgpu_ctx *ctx, int64_t i, int *entailed);
+/* ask(i) for every i (engine order); out has num_deductions() bytes. */
+int pir_ask_all(pirgpu_ctx *ctx, uint8_t *entailed);
+/* is_bot(), pir.hpp:831-833. */
+int pir_is_bot(pirgpu_ctx *ctx, int *bot);
+/* is_top(), pir.hpp:836-838. */
+int pir_is_top(pirgpu_ctx *ctx, int *top);
+/* is_extractable(), pir.hpp:874-884: not bot and every propagator entailed. */
+int pir_is_extractable(pirgpu_ctx *ctx, int *extractable);
+
+/* snapshot() / restore(), pir.hpp:857-870.  restore pops bytecodes from the
+ * end of the engine order back to the snapshot's count, as the reference pops
+ * from the end of its sorted vector, and restores the store. */
+int pir_snapshot(pirgpu_ctx *ctx, pirgpu_snapshot **out);
+int pir_restore(pirgpu_ctx *ctx, const pirgpu_snapshot *snap);
+void pir_snapshot_free(pirgpu_snapshot *snap);
+
+/* deduce(bytecode) applied to `count` independent private stores: bytecode
+ * k is (op[k], 0, 1, 2) over the three intervals in_lb/in_ub[3k..3k+2];
+ * results go to out_lb/out_ub, out_changed[k] (0/1) and out_failed[k] (0/1).
+ * The batched form of pir.hpp:721-817 for many candidate stores. */
+int pir_deduce_batch(pirgpu_ctx *ctx, int64_t count, const int32_t *op, const int32_t *in_lb,
+                     const int32_t *in_ub, int32_t *out_lb, int32_t *out_ub, uint8_t *out_changed,
+                     uint8_t *out_failed);
+
+/* Batched search nodes: the snapshot / embed / fixpoint / restore loop of
+ * tests/bound_consistency_test.hpp:175-196 over many nodes at once.  Node j
+ * starts from the context's store, meets its tightenings (var[k], lb[k], ub[k]
+ * for k in off[j] .. off[j+1]-1) and runs to its own fixpoint with the
+ * context's bytecode (shared by all nodes, as the shared copies of
+ * pir.hpp:182-195).  out_lb/out_ub (nnodes * nvars each, may be NULL) receive
+ * the node stores; out_status[j] a pir_status; out_rounds[j] (may be NULL) the
+ * rounds of node j.  The context's own store is not modified. */
+int pir_fixpoint_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, const int32_t *var,
+                       const int32_t *lb, const int32_t *ub, const pir_opts *opts,
+                       int32_t *out_lb, int32_t *out_ub, int32_t *out_status,
+                       int32_t *out_rounds, pir_stats *stats);
+
+/* Batched independent instances of uneven size, one launch: instance j owns
+ * propagators prop_off[j] .. prop_off[j+1]-1 (var indices local to the
+ * instance, already installed) and variables var_off[j] .. var_off[j+1]-1 of
+ * lb/ub, which are updated in place.  out_status[j] a pir_status,
+ * out_rounds[j] (may be NULL) its rounds, out_device_ms[j] (may be NULL) the
+ * device time from launch to that instance's fixpoint. */
+int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int64_t *prop_off,
+                           const int64_t *var_off, const int32_t *op, const int32_t *x,
+                           const int32_t *y, const int32_t *z, int32_t *lb, int32_t *ub,
+                           const pir_opts *opts, int32_t *out_status, int32_t *out_rounds,
+                           float *out_device_ms, pir_stats *stats);
+
+/* Number of SMs and the library's build string (for reports). */
+int pir_device_info(pirgpu_ctx *ctx, int32_t *num_sms, char *name, size_t name_len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,70 @@
+// Internal declarations shared by the pirgpu translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/pirgpu.h"
+#include "pir_kernels.cuh"
+
+namespace pirgpu {
+struct BatchState;
+struct SchedState;
+}  // namespace pirgpu
+
+// One PIR (bytecode + store) on one device.
+struct pirgpu_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int num_sms = 0;
+  int smem_optin = 0;
+  char dev_name[128] = {0};
+  char err[512] = {0};
+
+  // Store: nvars int2 {lb, ub} in HBM.
+  int nvars = 0;
+  int2 *d_store = nullptr;
+  size_t cap_store = 0;
+  int *d_io = nullptr;  // 2 * nvars int32 staging for pack / unpack
+  size_t cap_io = 0;
+  bool failed = false;  // is_bot()
+
+  // Bytecode in engine order (sorted by op, y, x, z), host copy and device SoA.
+  long long n = 0;
+  int max_var_used = -1;
+  long long bytecode_version = 0;
+  std::vector<int> h_op, h_x, h_y, h_z;
+  int *d_op = nullptr, *d_x = nullptr, *d_y = nullptr, *d_z = nullptr;
+  size_t cap_op = 0, cap_x = 0, cap_y = 0, cap_z = 0;
+
+  pirgpu::Control *d_ctl = nullptr;
+  void *d_scratch = nullptr;
+  size_t cap_scratch = 0;
+  int last_grid = 0;
+  int last_mode = 0;
+
+  pirgpu::BatchState *batch = nullptr;
+  pirgpu::SchedState *sched = nullptr;
+};
+
+namespace pirgpu {
+
+int set_err(pirgpu_ctx *ctx, int code, const char *fmt, ...);
+int cuda_err(pirgpu_ctx *ctx, cudaError_t e, const char *what);
+int ensure(pirgpu_ctx *ctx, void **ptr, size_t *cap, size_t bytes);
+int read_control(pirgpu_ctx *ctx, Control *h);
+int reset_control(pirgpu_ctx *ctx);
+Bytecode bytecode_view(const pirgpu_ctx *ctx);
+
+void destroy_batch_state(pirgpu_ctx *ctx);
+void destroy_sched_state(pirgpu_ctx *ctx);
+int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);
+
+}  // namespace pirgpu
+
+#define PIR_CK(call)                                                     \
+  do {                                                                   \
+    cudaError_t _e = (call);                                             \
+    if (_e != cudaSuccess) return pirgpu::cuda_err(ctx, _e, #call);      \
+  } while (0)

@@ -1,0 +1,140 @@
+// Fixpoint kernels of the plain (AC-1) propagation engine for sm_103a.
+//
+// Round structure (the GPU form of the Gauss-Seidel driver around
+// PIR::deduce(int), tests/pir_test.cpp:60-62, and of the per-block copies with
+// shared bytecode of pir.hpp:182-195): every round applies every propagator
+// once; bound joins are atomic and visible to later reads of the same round;
+// the round's "changed" and "failed" bits are OR-reduced (CTA: __syncthreads_or,
+// grid: the barrier word) and the loop stops after a round with no change, a
+// round that saw an empty interval, or the round cap.
+#pragma once
+#include "pir_device.cuh"
+
+namespace pirgpu {
+
+// Device-side control block of one fixpoint run (scratch memory).
+struct Control {
+  unsigned long long arrive;  // barrier: arrivals | changed-count << 20 | failed-count << 40
+  unsigned long long pad0[7];
+  unsigned int gen;           // barrier generation | decision bits
+  unsigned int pad1[15];
+  int status;                 // 0, or the pir_status error a CTA raised
+  int failed;                 // sticky failure flag (host loop / single-thread kernels)
+  int changed[4];             // host-loop change flags, one per round parity
+  long long rounds;           // rounds executed (written by CTA 0)
+  unsigned long long narrowed;
+  unsigned long long executions;
+};
+
+constexpr unsigned GEN_MASK = 0x1FFFFFFFu;
+constexpr unsigned BIT_CHANGED = 1u << 29;
+constexpr unsigned BIT_FAILED = 1u << 30;
+constexpr unsigned BIT_ERROR = 1u << 31;
+
+constexpr int ERR_BARRIER_TIMEOUT = 3;  // = PIR_BARRIER_TIMEOUT
+
+static __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+static __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+static __device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+
+static __device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid barrier with an OR-reduction of two bits, called by thread 0 of every
+// CTA.  Every wait is bounded by timeout_ns; on expiry the CTA records
+// PIR_BARRIER_TIMEOUT in ctl->status and the returned word carries BIT_ERROR.
+static __device__ __noinline__ unsigned grid_sync_or(Control *ctl, unsigned nblocks, int changed, int failed,
+                                              long long timeout_ns) {
+  const unsigned g0 = ld_acquire(&ctl->gen);
+  __threadfence();
+  const unsigned long long add =
+      1ull | ((unsigned long long)(changed != 0) << 20) | ((unsigned long long)(failed != 0) << 40);
+  const unsigned long long old = atomicAdd(&ctl->arrive, add);
+  if ((unsigned)(old & 0xFFFFFull) + 1u == nblocks) {
+    const unsigned long long tot = old + add;
+    const unsigned ch = (unsigned)((tot >> 20) & 0xFFFFFull), fl = (unsigned)((tot >> 40) & 0xFFFFFull);
+    ctl->arrive = 0ull;
+    unsigned next = ((g0 + 1u) & GEN_MASK) | (ch ? BIT_CHANGED : 0u) | (fl ? BIT_FAILED : 0u);
+    if (*(volatile int *)&ctl->status) next |= BIT_ERROR;
+    __threadfence();
+    st_release(&ctl->gen, next);
+    return next;
+  }
+  const unsigned long long t0 = globaltimer();
+  for (unsigned it = 0;; ++it) {
+    const unsigned g = ld_acquire(&ctl->gen);
+    if ((g & GEN_MASK) != (g0 & GEN_MASK)) return g;
+    if (it >= 32) __nanosleep(it < 256 ? 32 : 200);
+    if ((it & 63u) == 63u) {
+      if (*(volatile int *)&ctl->status) return BIT_ERROR;
+      if ((long long)(globaltimer() - t0) > timeout_ns) {
+        atomicCAS(&ctl->status, 0, ERR_BARRIER_TIMEOUT);
+        return BIT_ERROR;
+      }
+    }
+  }
+}
+
+// The bytecode as a structure of arrays, padded with OP_NOP to a multiple of 4
+// so that one thread reads four propagators with 128-bit loads.
+struct Bytecode {
+  const int4 *op, *x, *y, *z;
+  int nchunks;  // ceil(n / 4)
+};
+
+// Joins into the HBM store with fire-and-forget reductions (red.global): a
+// bound counts as narrowed when it is tighter than the value read.  A
+// concurrent tighter join can make that an over-count, which at worst costs
+// one more round; a round with no join at all is a true fixpoint because every
+// read in it saw the final store.
+struct RedStore {
+  int2 *s;
+  __device__ __forceinline__ Itv load(int v) const {
+    const int2 t = __ldcg(s + v);
+    return mk(t.x, t.y);
+  }
+  __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
+    int n = 0;
+    if (r.l > seen.l) {
+      asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(&s[v].x), "r"(r.l) : "memory");
+      ++n;
+    }
+    if (r.u < seen.u) {
+      asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(&s[v].y), "r"(r.u) : "memory");
+      ++n;
+    }
+    if (n && is_bot(mk(max(seen.l, r.l), min(seen.u, r.u)))) failed = 1;
+    return n;
+  }
+};
+
+// Four propagators of chunk c: all twelve intervals are gathered first (reads
+// may be stale within a round), then the four updates are applied in order.
+template <class S>
+static __device__ __forceinline__ int sweep_chunk(const Bytecode &bc, int c, S &st, int &failed) {
+  const int4 o = __ldg(bc.op + c), X = __ldg(bc.x + c), Y = __ldg(bc.y + c), Z = __ldg(bc.z + c);
+  Itv a0 = st.load(X.x), b0 = st.load(Y.x), c0 = st.load(Z.x);
+  Itv a1 = st.load(X.y), b1 = st.load(Y.y), c1 = st.load(Z.y);
+  Itv a2 = st.load(X.z), b2 = st.load(Y.z), c2 = st.load(Z.z);
+  Itv a3 = st.load(X.w), b3 = st.load(Y.w), c3 = st.load(Z.w);
+  int ch = 0;
+  ch += deduce_loaded(o.x, X.x, Y.x, Z.x, a0, b0, c0, st, failed);
+  ch += deduce_loaded(o.y, X.y, Y.y, Z.y, a1, b1, c1, st, failed);
+  ch += deduce_loaded(o.z, X.z, Y.z, Z.z, a2, b2, c2, st, failed);
+  ch += deduce_loaded(o.w, X.w, Y.w, Z.w, a3, b3, c3, st, failed);
+  return ch;
+}
+
+}  // namespace pirgpu
