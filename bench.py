@@ -243,12 +243,18 @@ def run_ours(args):
     ctx.tell(inst.op, inst.x, inst.y, inst.z)
     snap = ctx.snapshot()
     nprops = ctx.num_deductions()
-    kw = dict(mode=args.mode)
+    init_lb, init_ub = ctx.read_store()  # store after install (reified targets met with [0,1])
+    kw = dict(mode=args.mode, max_rounds=args.max_rounds, variant=args.variant)
+    tuned = None
+    if args.mode in (0, 1) and args.variant == 0:
+        tuned = ctx.autotune(16)
+        ctx.restore(snap)
+    ok = (pirgpu.OK, pirgpu.TIMEOUT) if args.max_rounds else (pirgpu.OK,)
 
     def step():
         ctx.restore(snap)
         rc, st = ctx.fixpoint(**kw)
-        if rc != pirgpu.OK:
+        if rc not in ok:
             raise RuntimeError("fixpoint status %s" % pirgpu.STATUS[rc])
         return st
 
@@ -281,12 +287,9 @@ def run_ours(args):
     ub_h = cr.pinned(inst.nvars)
     lb_o = cr.pinned(inst.nvars)
     ub_o = cr.pinned(inst.nvars)
-    lb_h[:] = inst.lb
-    ub_h[:] = inst.ub
-    init_lb, init_ub = ctx.read_store()  # store after install (reified targets met with [0,1])
     lb_h[:] = init_lb
     ub_h[:] = init_ub
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 3))
     e2e_execs = 0
     if dist:
         dist.barrier()
@@ -300,7 +303,7 @@ def run_ours(args):
         e2e_execs += st["executions"]
     cr.sync()
     e2e_t = dist_max(dist, time.perf_counter() - t0)
-    e2e_value = dist_sum(dist, e2e_execs) / e2e_t
+    e2e_value = dist_sum(dist, e2e_execs) / e2e_t if e2e_steps else None
 
     if rank != 0:
         return
@@ -323,7 +326,8 @@ def run_ours(args):
                    "propagators": int(nprops), "parallelism": "replicas" if ws > 1 else "single",
                    "mode": ["auto", "persistent", "hostloop", "smem"][args.mode],
                    "l2": "flushed between steps (256 MiB cudaMemset); step timed with CUDA events",
-                   "rounds_per_step": rounds[0], "fixpoint": "bit-exact vs CPU oracle in tests"},
+                   "rounds_per_step": rounds[0], "fixpoint": "bit-exact vs CPU oracle in tests",
+                   "kernel_variant": list(tuned) if tuned else args.variant},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
                      "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
@@ -336,6 +340,164 @@ def run_ours(args):
         "clocks": clocks,
         "time_to_fixpoint_ms": dev_ms / args.steps,
         "wall_s": wall,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def _nodes_workload():
+    import workloads as W
+    import pirgpu
+    base = W.plain(100_000, 400_000, 10**6, 0)
+    ctx = pirgpu.Context(dist_env()[2])
+    ctx.load_store(base.lb, base.ub)
+    ctx.tell(base.op, base.x, base.y, base.z)
+    rc, _ = ctx.fixpoint()
+    if rc != pirgpu.OK:
+        raise RuntimeError("base instance failed")
+    blb, bub = ctx.read_store()
+    _, off, var, lb, ub = W.nodes(100_000, 400_000, 4096, 0, 64, base_store=(blb, bub))
+    return ctx, base, (blb, bub), off, var, lb, ub
+
+
+def run_nodes(args):
+    """Batched search nodes: 4,096 nodes over a 100,000-var / 400,000-propagator
+    base at its fixpoint, each bisecting k ~ U[1, 64] variables."""
+    import pirgpu
+    ws, rank, local = dist_env()
+    cr = Cudart()
+    cr.set_device(local)
+    ctx, base, (blb, bub), off, var, lb, ub = _nodes_workload()
+    nn = len(off) - 1
+    for _ in range(args.warmup):
+        ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False)
+        cr.flush_l2()
+    clk = ClockSampler(local)
+    clk.start()
+    runs = []
+    for _ in range(args.steps):
+        status, _, _, rounds, st = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False)
+        runs.append(st)
+        cr.flush_l2()
+    clocks = clk.stop()
+    dev_s = sum(r["device_ms"] for r in runs) / 1e3
+    value = nn * args.steps / dev_s
+    execs = sum(r["executions"] for r in runs)
+    joins = sum(r["narrowed"] for r in runs)
+    # the plain single-instance GPU loop, node after node (sample)
+    snap = ctx.snapshot()
+    ctx.autotune(8)
+    sample = min(nn, args.seq_nodes)
+    seq_dev, t0 = 0.0, time.perf_counter()
+    for j in range(sample):
+        ctx.restore(snap)
+        ctx.embed_many(var[off[j]:off[j + 1]], lb[off[j]:off[j + 1]], ub[off[j]:off[j + 1]])
+        rc, st = ctx.fixpoint()
+        seq_dev += st["device_ms"] / 1e3
+    seq_wall = time.perf_counter() - t0
+    ctx.restore(snap)
+    seq_dev_rate = sample / seq_dev
+    seq_wall_rate = sample / seq_wall
+    # end to end: host tightenings in, node stores out
+    t0 = time.perf_counter()
+    status, olb, oub, rounds, st = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=True)
+    e2e_t = time.perf_counter() - t0
+    hbm, hbm_src = peaks()
+    achieved = (execs * ALG_BYTES_PER_EXEC + joins * ALG_BYTES_PER_JOIN) / dev_s / 1e9
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        op, x, y, z = ctx.bytecode()
+        bs = np.ascontiguousarray(np.stack([blb, bub], 1))
+        m = min(nn, args.cpu_nodes)
+        th = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ost, _, _ = O.fixpoint_nodes(op, x, y, z, bs, off[:m + 1], var, lb, ub, threads=th)
+        ct = time.perf_counter() - t0
+        cpu = {"value": m / ct, "unit": "nodes/s", "cores": th, "kind": "port",
+               "sample": "%d nodes, Gauss-Seidel per node, %d host threads, %.1f s" % (m, th, ct)}
+    out = {
+        "metric": "batched nodes/sec", "value": value, "unit": "nodes/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic: planted-solution base instance at its fixpoint, bisected nodes",
+        "config": {"workload": "nodes: 100,000 vars / 400,000 propagators (bounds scale 1e6) at its fixpoint, 4,096 nodes, k ~ U[1,64] bisections of unfixed vars",
+                   "nodes_ok": int((status == 0).sum()), "nodes_failed": int((status == 1).sum()),
+                   "max_rounds": int(rounds.max()), "mean_rounds": float(rounds.mean())},
+        "plain_sequential": {"nodes_per_s_device": seq_dev_rate, "nodes_per_s_wall": seq_wall_rate,
+                             "sample_nodes": sample,
+                             "batched_over_sequential_device": value / seq_dev_rate,
+                             "batched_over_sequential_wall": (nn / e2e_t) / seq_wall_rate},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": ncu_traffic("nodes_fixpoint"),
+                     "peak_source": hbm_src},
+        "cpu_baseline": cpu,
+        "e2e": {"value": nn / e2e_t, "unit": "nodes/s", "h2d_bytes_per_step": int(len(var) * 12 + len(off) * 4),
+                "d2h_bytes_per_step": int(nn * len(blb) * 8)},
+        "gpu_launches": args.steps, "clocks": clocks,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_uneven(args):
+    """512 independent instances, propagators log-uniform in [1e3, 2e5]."""
+    import pirgpu
+    import workloads as W
+    ws, rank, local = dist_env()
+    cr = Cudart()
+    cr.set_device(local)
+    insts = W.uneven(512, 1000, 200_000, 0)
+    prop_off, var_off, op, x, y, z, lb0, ub0 = W.pack(insts)
+    ctx = pirgpu.Context(local)
+    for _ in range(args.warmup):
+        lb, ub = lb0.copy(), ub0.copy()
+        ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
+    clk = ClockSampler(local)
+    clk.start()
+    runs, walls, per = [], [], []
+    for _ in range(args.steps):
+        lb, ub = lb0.copy(), ub0.copy()
+        t0 = time.perf_counter()
+        status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
+        walls.append(time.perf_counter() - t0)
+        runs.append(st)
+        per.append(ms)
+    clocks = clk.stop()
+    dev_s = sum(r["device_ms"] for r in runs) / 1e3
+    n = len(insts)
+    per = np.concatenate(per)
+    execs = sum(r["executions"] for r in runs)
+    hbm, hbm_src = peaks()
+    achieved = execs * ALG_BYTES_PER_EXEC / dev_s / 1e9
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        m = min(n, args.cpu_instances)
+        small = sorted(range(n), key=lambda j: insts[j].nprops)[:m]
+        sub = [insts[j] for j in small]
+        po, vo, o2, x2, y2, z2, l2, u2 = W.pack(sub)
+        s = np.ascontiguousarray(np.stack([l2, u2], 1))
+        th = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        O.fixpoint_instances(po, vo, o2, x2, y2, z2, s, threads=th)
+        ct = time.perf_counter() - t0
+        cpu = {"value": m / ct, "unit": "instances/s", "cores": th, "kind": "port",
+               "sample": "the %d smallest instances, %d host threads, %.1f s" % (m, th, ct)}
+    out = {
+        "metric": "batched instances/sec", "value": n * args.steps / dev_s, "unit": "instances/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic: planted-solution instances",
+        "config": {"workload": "uneven: 512 instances, propagators log-uniform [1e3, 2e5], vars = props/4, "
+                               "5% tdiv + 5% tmod", "propagators": int(prop_off[-1]),
+                   "instance_ms_p50": float(np.percentile(per, 50)), "instance_ms_p99": float(np.percentile(per, 99)),
+                   "failed": int((status == 1).sum())},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": ncu_traffic("instances_fixpoint"), "peak_source": hbm_src},
+        "cpu_baseline": cpu,
+        "e2e": {"value": n * args.steps / sum(walls), "unit": "instances/s",
+                "h2d_bytes_per_step": int(prop_off[-1] * 16 + var_off[-1] * 8),
+                "d2h_bytes_per_step": int(var_off[-1] * 8)},
+        "gpu_launches": args.steps, "clocks": clocks,
     }
     print(json.dumps(out), flush=True)
 
@@ -389,11 +551,21 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-sweeps", type=int, default=3)
+    ap.add_argument("--max-rounds", type=int, default=0, help="round cap (profiling runs)")
+    ap.add_argument("--variant", type=int, default=0, help="persistent kernel variant, 0: autotuned")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--seq-nodes", type=int, default=128, help="nodes timed in the sequential loop")
+    ap.add_argument("--cpu-nodes", type=int, default=256)
+    ap.add_argument("--cpu-instances", type=int, default=128)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "nodes":
+        run_nodes(args)
+    elif args.workload == "uneven":
+        run_uneven(args)
     else:
         run_ours(args)
 

@@ -68,7 +68,8 @@ typedef struct pir_opts {
   int32_t ctas_per_sm;        /* persistent grid = SMs * ctas_per_sm, 0: occupancy limit */
   int32_t sched;              /* enum pir_sched */
   float wake_fraction;        /* learned schedule: fraction of propagators woken per round (0: 1/16) */
-  int32_t reserved[7];
+  int32_t variant;            /* persistent kernel variant 1..N (0: autotuned, else the default) */
+  int32_t reserved[6];
 } pir_opts;
 
 typedef struct pir_stats {
@@ -96,6 +97,11 @@ int pir_project(pirgpu_ctx *ctx, int32_t var, int32_t *lb, int32_t *ub);
 /* embed(x, dom), pir.hpp:354-356: meet [lb, ub] into x; *changed = narrowed. */
 int pir_embed(pirgpu_ctx *ctx, int32_t var, int32_t lb, int32_t ub, int *changed);
 
+/* embed() applied to count (var, [lb, ub]) pairs in one call (pir.hpp:354-356
+ * repeated); *changed = some bound narrowed. */
+int pir_embed_many(pirgpu_ctx *ctx, int32_t count, const int32_t *var, const int32_t *lb,
+                   const int32_t *ub, int *changed);
+
 /* deduce(tell) for the bytecode part of a tell, pir.hpp:326-352: appends n
  * propagators, meets x of every EQ/LEQ with [0,1] and re-sorts the whole
  * bytecode by (op, y, x, z) (the CPU order of pir.hpp:343-347).  Var indices
@@ -114,6 +120,13 @@ int pir_get_bytecode(pirgpu_ctx *ctx, int32_t *op, int32_t *x, int32_t *y, int32
  * tests/pir_test.cpp:60-62).  Returns PIR_OK, PIR_FAILED, PIR_TIMEOUT or an
  * error.  opts may be NULL (defaults); stats may be NULL. */
 int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts, pir_stats *stats);
+/* Autotuner: times every persistent-kernel variant (propagators per thread
+ * and step, CTAs per SM) for `rounds` rounds (0: 16) from the current store,
+ * keeps the fastest for this context's later pir_fixpoint calls
+ * (opts.variant = 0) and puts the store back.  out_variant (1-based) and
+ * out_us_per_round may be NULL. */
+int pir_autotune(pirgpu_ctx *ctx, int32_t rounds, int32_t *out_variant, float *out_us_per_round);
+
 /* deduce(i), pir.hpp:387-390: one propagator; *changed = has_changed. */
 int pir_deduce_one(pirgpu_ctx *ctx, int64_t i, int *changed);
 
@@ -158,10 +171,12 @@ int pir_fixpoint_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, cons
 
 /* Batched independent instances of uneven size, one launch: instance j owns
  * propagators prop_off[j] .. prop_off[j+1]-1 (var indices local to the
- * instance, already installed) and variables var_off[j] .. var_off[j+1]-1 of
- * lb/ub, which are updated in place.  out_status[j] a pir_status,
- * out_rounds[j] (may be NULL) its rounds, out_device_ms[j] (may be NULL) the
- * device time from launch to that instance's fixpoint. */
+ * instance) and variables var_off[j] .. var_off[j+1]-1 of lb/ub, which are
+ * updated in place.  Each instance is installed on the device (reified targets
+ * met with [0, 1], pir.hpp:333-335) and run in the given propagator order.
+ * out_status[j] a pir_status, out_rounds[j] (may be NULL) its rounds,
+ * out_device_ms[j] (may be NULL) the device time of that instance's own
+ * fixpoint (from the moment a CTA takes it up). */
 int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int64_t *prop_off,
                            const int64_t *var_off, const int32_t *op, const int32_t *x,
                            const int32_t *y, const int32_t *z, int32_t *lb, int32_t *ub,

@@ -1,22 +1,614 @@
-// Batched fixpoints (search nodes, uneven instances).
+// Batched fixpoints for sm_103a.
+//
+// * Uneven independent instances (pir_fixpoint_instances): a persistent grid of
+//   CTAs steals instances, largest first; one CTA runs one instance's AC-1
+//   rounds separated by __syncthreads.  The instance's store is staged in
+//   shared memory when it fits (with its bytecode too when that also fits),
+//   otherwise it stays in the L2-resident global store.
+// * Search nodes (pir_fixpoint_nodes): the per-block store copies sharing one
+//   bytecode of pir.hpp:182-195, batched 32 nodes per warp.  The node stores
+//   are interleaved by node ([var][32 nodes] int2 per group), so one warp
+//   applying one propagator to its 32 nodes reads each interval with one
+//   coalesced 256-byte access and all lanes run the same opcode.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
 #include "pir_engine.h"
 
 namespace pirgpu {
-struct BatchState {};
+
+struct InstOut {
+  int status;
+  int rounds;
+  unsigned long long ns;
+  unsigned long long narrowed;
+};
+
+struct NodeOut {
+  int status;
+  int rounds;
+};
+
+struct BatchState {
+  int4 *d_bc = nullptr;
+  size_t cap_bc = 0;
+  long long *d_off = nullptr;  // chunk offsets | var offsets
+  size_t cap_off = 0;
+  int2 *d_store = nullptr;
+  size_t cap_store = 0;
+  int *d_aux = nullptr;  // order | next counter | lb/ub staging
+  size_t cap_aux = 0;
+  InstOut *d_iout = nullptr;
+  size_t cap_iout = 0;
+  int2 *d_nstore = nullptr;  // node groups
+  size_t cap_nstore = 0;
+  int *d_tight = nullptr;  // node tightenings: off | var | lb | ub
+  size_t cap_tight = 0;
+  NodeOut *d_nout = nullptr;
+  size_t cap_nout = 0;
+  int *d_nio = nullptr;  // per-node output staging
+  size_t cap_nio = 0;
+};
+
 void destroy_batch_state(pirgpu_ctx *ctx) {
-  delete ctx->batch;
+  BatchState *b = ctx->batch;
+  if (!b) return;
+  void *ptrs[] = {b->d_bc, b->d_off, b->d_store, b->d_aux, b->d_iout, b->d_nstore, b->d_tight, b->d_nout, b->d_nio};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete b;
   ctx->batch = nullptr;
 }
-}  // namespace pirgpu
 
-extern "C" int pir_fixpoint_nodes(pirgpu_ctx *ctx, int32_t, const int32_t *, const int32_t *, const int32_t *,
-                                  const int32_t *, const pir_opts *, int32_t *, int32_t *, int32_t *, int32_t *,
-                                  pir_stats *) {
-  return pirgpu::set_err(ctx, PIR_EINVAL, "pir_fixpoint_nodes: not built");
+// ------------------------------------------------------ instance kernel -----
+
+struct InstArgs {
+  const int4 *op, *x, *y, *z;  // padded chunks; instance j owns [coff[j], coff[j+1])
+  const long long *coff, *voff;
+  int2 *store;
+  const int *order;
+  int ninst;
+  int *next;
+  InstOut *out;
+  long long max_rounds;
+  int smem_cap;
+};
+
+// pir.hpp:333-335 on the device: reified targets are met with [0, 1].
+template <class S>
+__device__ __forceinline__ void install_chunks(const Bytecode &bc, S &st) {
+  int dummy = 0;
+  for (int c = threadIdx.x; c < bc.nchunks; c += blockDim.x) {
+    const int4 o = bc.op[c], X = bc.x[c];
+    const int ops[4] = {o.x, o.y, o.z, o.w}, xs[4] = {X.x, X.y, X.z, X.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (ops[k] == OP_EQ || ops[k] == OP_LEQ) {
+        const Itv seen = st.load(xs[k]);
+        st.embed(xs[k], seen, mk(0, 1), dummy);
+      }
+  }
 }
 
-extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t, const int64_t *, const int64_t *, const int32_t *,
-                                      const int32_t *, const int32_t *, const int32_t *, int32_t *, int32_t *,
-                                      const pir_opts *, int32_t *, int32_t *, float *, pir_stats *) {
-  return pirgpu::set_err(ctx, PIR_EINVAL, "pir_fixpoint_instances: not built");
+template <class S>
+__device__ __forceinline__ void cta_rounds(const Bytecode &bc, S &st, long long max_rounds, long long &rounds,
+                                           int &failed, int &changed, unsigned long long &narrowed) {
+  rounds = 0;
+  for (;;) {
+    int ch = 0, f = 0;
+    for (int c = threadIdx.x; c < bc.nchunks; c += blockDim.x) ch += sweep_chunk(bc, c, st, f);
+    narrowed += ch;
+    const int any_ch = __syncthreads_or(ch);
+    const int any_f = __syncthreads_or(f);
+    ++rounds;
+    if (any_f || !any_ch || (max_rounds > 0 && rounds >= max_rounds)) {
+      failed = any_f;
+      changed = any_ch;
+      return;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(512) k_instances(InstArgs a) {
+  extern __shared__ int4 sm[];
+  __shared__ int s_k;
+  for (;;) {
+    if (threadIdx.x == 0) s_k = atomicAdd(a.next, 1);
+    __syncthreads();
+    const int k = s_k;
+    __syncthreads();
+    if (k >= a.ninst) return;
+    const int j = a.order[k];
+    const long long c0 = a.coff[j];
+    const int nch = (int)(a.coff[j + 1] - c0);
+    const long long v0 = a.voff[j];
+    const int nv = (int)(a.voff[j + 1] - v0);
+    const unsigned long long t0 = globaltimer();
+    int2 *gs = a.store + v0;
+    Bytecode bc;
+    bc.op = a.op + c0;
+    bc.x = a.x + c0;
+    bc.y = a.y + c0;
+    bc.z = a.z + c0;
+    bc.nchunks = nch;
+    long long rounds = 0;
+    int failed = 0, changed = 0;
+    unsigned long long narrowed = 0;
+    const int store_bytes = ((nv * 8 + 15) / 16) * 16;
+    if (store_bytes <= a.smem_cap) {
+      int2 *ss = reinterpret_cast<int2 *>(sm);
+      for (int v = threadIdx.x; v < nv; v += blockDim.x) ss[v] = gs[v];
+      Bytecode sb = bc;
+      if (store_bytes + nch * 64 <= a.smem_cap) {
+        int4 *b4 = sm + store_bytes / 16;
+        int4 *sop = b4, *sx = b4 + nch, *sy = b4 + 2 * nch, *sz = b4 + 3 * nch;
+        for (int c = threadIdx.x; c < nch; c += blockDim.x) {
+          sop[c] = bc.op[c];
+          sx[c] = bc.x[c];
+          sy[c] = bc.y[c];
+          sz[c] = bc.z[c];
+        }
+        sb.op = sop;
+        sb.x = sx;
+        sb.y = sy;
+        sb.z = sz;
+      }
+      __syncthreads();
+      SmemStore st{ss};
+      install_chunks(sb, st);
+      __syncthreads();
+      cta_rounds(sb, st, a.max_rounds, rounds, failed, changed, narrowed);
+      for (int v = threadIdx.x; v < nv; v += blockDim.x) gs[v] = ss[v];
+    } else {
+      GlobalStore gst{gs};
+      install_chunks(bc, gst);
+      __syncthreads();
+      RedStore st{gs};
+      cta_rounds(bc, st, a.max_rounds, rounds, failed, changed, narrowed);
+    }
+    narrowed = warp_sum64(narrowed);
+    if ((threadIdx.x & 31) == 0 && narrowed) atomicAdd(&a.out[j].narrowed, narrowed);
+    if (threadIdx.x == 0) {
+      a.out[j].status = failed ? PIR_FAILED : (changed ? PIR_TIMEOUT : PIR_OK);
+      a.out[j].rounds = (int)rounds;
+      a.out[j].ns = globaltimer() - t0;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------- node kernel -----
+
+// One node's column of a node group: var v of the node of lane `lane` lives at
+// s[v * 32 + lane].  Several warps update the same node, so joins are
+// device-scope reductions.
+struct NodeStore {
+  int2 *s;  // already offset by the lane
+  __device__ __forceinline__ Itv load(int v) const {
+    const int2 t = __ldcg(s + (size_t)v * 32);
+    return mk(t.x, t.y);
+  }
+  __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
+    int n = 0;
+    int2 *p = s + (size_t)v * 32;
+    if (r.l > seen.l) {
+      asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(&p->x), "r"(r.l) : "memory");
+      ++n;
+    }
+    if (r.u < seen.u) {
+      asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(&p->y), "r"(r.u) : "memory");
+      ++n;
+    }
+    if (n && is_bot(mk(max(seen.l, r.l), min(seen.u, r.u)))) failed = 1;
+    return n;
+  }
+};
+
+struct NodeArgs {
+  Bytecode bc;
+  int nvars;
+  const int2 *base;
+  int2 *nstore;
+  const int *off, *var, *lb, *ub;
+  int nnodes, ngroups;
+  int *next;
+  NodeOut *out;
+  unsigned long long *narrowed;
+  long long max_rounds;
+};
+
+__global__ void __launch_bounds__(512) k_nodes(NodeArgs a) {
+  __shared__ int s_g;
+  __shared__ unsigned s_changed[2], s_failed[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (;;) {
+    if (threadIdx.x == 0) s_g = atomicAdd(a.next, 1);
+    __syncthreads();
+    const int g = s_g;
+    __syncthreads();
+    if (g >= a.ngroups) return;
+    const int node = g * 32 + lane;
+    const bool valid = node < a.nnodes;
+    int2 *S = a.nstore + (size_t)g * a.nvars * 32;
+    for (int v = warp; v < a.nvars; v += nwarps) S[(size_t)v * 32 + lane] = a.base[v];
+    if (threadIdx.x < 2) {
+      s_changed[threadIdx.x] = 0;
+      s_failed[threadIdx.x] = 0;
+    }
+    __syncthreads();
+    unsigned failed_mask = 0;
+    if (warp == 0) {
+      int f = 0;
+      if (valid) {
+        for (int k = a.off[node]; k < a.off[node + 1]; ++k) {
+          int2 *p = S + (size_t)a.var[k] * 32 + lane;
+          int2 t = *p;
+          t.x = max(t.x, a.lb[k]);
+          t.y = min(t.y, a.ub[k]);
+          *p = t;
+          f |= is_bot(mk(t.x, t.y));
+        }
+      }
+      failed_mask = __ballot_sync(0xFFFFFFFFu, f);
+      if (lane == 0) s_failed[1] = failed_mask;
+    }
+    __syncthreads();
+    failed_mask = s_failed[1];
+    const unsigned valid_mask = (g * 32 + 32 <= a.nnodes) ? 0xFFFFFFFFu : ((1u << (a.nnodes - g * 32)) - 1u);
+    unsigned active = valid_mask & ~failed_mask;
+    unsigned timeout_mask = 0;
+    int node_rounds = 0;  // meaningful in warp 0
+    long long round = 0;
+    unsigned long long narrowed = 0;
+    NodeStore st{S + lane};
+    __syncthreads();
+    while (active) {
+      const int par = (int)(round & 1);
+      if (threadIdx.x == 0) {
+        s_changed[par ^ 1] = 0;
+        s_failed[par ^ 1] = 0;
+      }
+      const bool me = (active >> lane) & 1u;
+      int ch = 0, f = 0;
+      for (int c = warp; c < a.bc.nchunks; c += nwarps) {
+        const int4 o = __ldg(a.bc.op + c), X = __ldg(a.bc.x + c), Y = __ldg(a.bc.y + c), Z = __ldg(a.bc.z + c);
+        if (!me) continue;
+        const Itv a0 = st.load(X.x), b0 = st.load(Y.x), c0 = st.load(Z.x);
+        const Itv a1 = st.load(X.y), b1 = st.load(Y.y), c1 = st.load(Z.y);
+        const Itv a2 = st.load(X.z), b2 = st.load(Y.z), c2 = st.load(Z.z);
+        const Itv a3 = st.load(X.w), b3 = st.load(Y.w), c3 = st.load(Z.w);
+        ch += deduce_loaded(o.x, X.x, Y.x, Z.x, a0, b0, c0, st, f);
+        ch += deduce_loaded(o.y, X.y, Y.y, Z.y, a1, b1, c1, st, f);
+        ch += deduce_loaded(o.z, X.z, Y.z, Z.z, a2, b2, c2, st, f);
+        ch += deduce_loaded(o.w, X.w, Y.w, Z.w, a3, b3, c3, st, f);
+      }
+      narrowed += ch;
+      const unsigned cb = __ballot_sync(0xFFFFFFFFu, ch != 0), fb = __ballot_sync(0xFFFFFFFFu, f != 0);
+      if (lane == 0) {
+        if (cb) atomicOr(&s_changed[par], cb);
+        if (fb) atomicOr(&s_failed[par], fb);
+      }
+      __syncthreads();
+      const unsigned changed = s_changed[par] & active, failed = s_failed[par] & active;
+      ++round;
+      if ((active >> lane) & 1u) node_rounds = (int)round;
+      failed_mask |= failed;
+      active &= changed & ~failed;
+      if (active && a.max_rounds > 0 && round >= a.max_rounds) {
+        timeout_mask = active;
+        active = 0;
+      }
+      __syncthreads();
+    }
+    narrowed = warp_sum64(narrowed);
+    if (lane == 0 && narrowed) atomicAdd(a.narrowed, narrowed);
+    if (warp == 0 && valid) {
+      const unsigned bit = 1u << lane;
+      a.out[node].status = (failed_mask & bit) ? PIR_FAILED : ((timeout_mask & bit) ? PIR_TIMEOUT : PIR_OK);
+      a.out[node].rounds = node_rounds;
+    }
+    __syncthreads();
+  }
+}
+
+// Node-major output: out[node][v] = group store[v][lane].
+__global__ void k_nodes_unpack(const int2 *nstore, int nvars, int nnodes, int *out_lb, int *out_ub) {
+  const long long total = (long long)nnodes * nvars;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int node = (int)(i / nvars), v = (int)(i % nvars);
+    const int2 t = nstore[((size_t)(node >> 5) * nvars + v) * 32 + (node & 31)];
+    out_lb[i] = t.x;
+    out_ub[i] = t.y;
+  }
+}
+
+__global__ void k_pack_int2(const int *lb, const int *ub, long long n, int2 *out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = make_int2(lb[i], ub[i]);
+}
+
+__global__ void k_unpack_int2(const int2 *in, long long n, int *lb, int *ub) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int2 t = in[i];
+    lb[i] = t.x;
+    ub[i] = t.y;
+  }
+}
+
+BatchState *batch(pirgpu_ctx *ctx) {
+  if (!ctx->batch) ctx->batch = new BatchState();
+  return ctx->batch;
+}
+
+}  // namespace pirgpu
+
+using namespace pirgpu;
+
+extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int64_t *prop_off, const int64_t *var_off,
+                                      const int32_t *op, const int32_t *x, const int32_t *y, const int32_t *z,
+                                      int32_t *lb, int32_t *ub, const pir_opts *opts_in, int32_t *out_status,
+                                      int32_t *out_rounds, float *out_device_ms, pir_stats *stats) {
+  if (!ctx) return PIR_EINVAL;
+  if (ninst < 0 || (ninst > 0 && (!prop_off || !var_off || !lb || !ub || !out_status)))
+    return set_err(ctx, PIR_EINVAL, "bad arguments");
+  if (ninst == 0) return PIR_OK;
+  pir_opts opts;
+  std::memset(&opts, 0, sizeof(opts));
+  if (opts_in) opts = *opts_in;
+  if (prop_off[0] != 0 || var_off[0] != 0) return set_err(ctx, PIR_EINVAL, "offsets must start at 0");
+  for (int j = 0; j < ninst; ++j) {
+    if (prop_off[j + 1] < prop_off[j] || var_off[j + 1] < var_off[j])
+      return set_err(ctx, PIR_EINVAL, "offsets of instance %d decrease", j);
+    if (var_off[j + 1] - var_off[j] > INT32_MAX / 64) return set_err(ctx, PIR_EINVAL, "instance %d too large", j);
+  }
+  const long long nprops = prop_off[ninst], nvars = var_off[ninst];
+  if (nprops > 0 && (!op || !x || !y || !z)) return set_err(ctx, PIR_EINVAL, "null bytecode");
+  for (int j = 0; j < ninst; ++j) {
+    const long long nv = var_off[j + 1] - var_off[j];
+    for (long long i = prop_off[j]; i < prop_off[j + 1]; ++i) {
+      if (op[i] < 0 || op[i] >= OP_COUNT) return set_err(ctx, PIR_EINVAL, "instance %d: bad opcode", j);
+      if (x[i] < 0 || x[i] >= nv || y[i] < 0 || y[i] >= nv || z[i] < 0 || z[i] >= nv)
+        return set_err(ctx, PIR_EINVAL, "instance %d: var index out of range", j);
+    }
+  }
+  PIR_CK(cudaSetDevice(ctx->device));
+  BatchState *b = batch(ctx);
+  // Padded chunk layout: instance j owns chunks coff[j] .. coff[j+1]-1.
+  std::vector<long long> off(2 * (size_t)(ninst + 1));
+  long long *coff = off.data(), *voff = off.data() + ninst + 1;
+  coff[0] = 0;
+  for (int j = 0; j < ninst; ++j) {
+    coff[j + 1] = coff[j] + (prop_off[j + 1] - prop_off[j] + 3) / 4;
+    voff[j] = var_off[j];
+  }
+  voff[ninst] = var_off[ninst];
+  const long long nchunks = coff[ninst];
+  std::vector<int> hb((size_t)std::max<long long>(nchunks, 1) * 16);
+  int *hop = hb.data(), *hx = hop + 4 * nchunks, *hy = hx + 4 * nchunks, *hz = hy + 4 * nchunks;
+  for (int j = 0; j < ninst; ++j) {
+    const long long p0 = prop_off[j], p1 = prop_off[j + 1], d0 = coff[j] * 4, d1 = coff[j + 1] * 4;
+    for (long long i = p0; i < p1; ++i) {
+      const long long d = d0 + (i - p0);
+      hop[d] = op[i];
+      hx[d] = x[i];
+      hy[d] = y[i];
+      hz[d] = z[i];
+    }
+    for (long long d = d0 + (p1 - p0); d < d1; ++d) {
+      hop[d] = OP_NOP;
+      hx[d] = hy[d] = hz[d] = 0;
+    }
+  }
+  std::vector<int> order(ninst);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
+    return prop_off[p + 1] - prop_off[p] > prop_off[q + 1] - prop_off[q];
+  });
+  int r;
+  if ((r = ensure(ctx, (void **)&b->d_bc, &b->cap_bc, (size_t)std::max<long long>(nchunks, 1) * 64))) return r;
+  if ((r = ensure(ctx, (void **)&b->d_off, &b->cap_off, off.size() * sizeof(long long)))) return r;
+  if ((r = ensure(ctx, (void **)&b->d_store, &b->cap_store, (size_t)std::max<long long>(nvars, 1) * 8))) return r;
+  const size_t aux_ints = (size_t)ninst + 4 + 2 * (size_t)nvars;
+  if ((r = ensure(ctx, (void **)&b->d_aux, &b->cap_aux, aux_ints * sizeof(int)))) return r;
+  if ((r = ensure(ctx, (void **)&b->d_iout, &b->cap_iout, (size_t)ninst * sizeof(InstOut)))) return r;
+  int *d_order = b->d_aux, *d_next = d_order + ninst, *d_lb = d_next + 4, *d_ub = d_lb + nvars;
+  PIR_CK(cudaMemcpyAsync(b->d_bc, hb.data(), (size_t)nchunks * 64, cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaMemcpyAsync(b->d_off, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaMemcpyAsync(d_order, order.data(), ninst * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaMemsetAsync(d_next, 0, 4 * sizeof(int), ctx->stream));
+  PIR_CK(cudaMemsetAsync(b->d_iout, 0, (size_t)ninst * sizeof(InstOut), ctx->stream));
+  if (nvars) {
+    PIR_CK(cudaMemcpyAsync(d_lb, lb, nvars * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    PIR_CK(cudaMemcpyAsync(d_ub, ub, nvars * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    k_pack_int2<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(d_lb, d_ub, nvars, b->d_store);
+    PIR_CK(cudaGetLastError());
+  }
+  const int block = opts.block > 0 ? std::min(opts.block, 512) : 512;
+  // CTAs per SM: as asked (default 2), lowered until registers and shared
+  // memory let that many stay resident; each gets an equal share of the SM's
+  // shared memory.
+  int per_sm = opts.ctas_per_sm > 0 ? opts.ctas_per_sm : 2;
+  int smem = 0;
+  for (;;) {
+    smem = std::min(ctx->smem_optin, (int)((228 * 1024) / per_sm) - 2048);
+    smem = (smem / 16) * 16;
+    PIR_CK(cudaFuncSetAttribute(k_instances, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int occ = 0;
+    PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_instances, block, smem));
+    if (occ >= per_sm || per_sm == 1) break;
+    per_sm = std::max(1, occ);
+  }
+  InstArgs a;
+  a.op = b->d_bc;
+  a.x = b->d_bc + nchunks;
+  a.y = b->d_bc + 2 * nchunks;
+  a.z = b->d_bc + 3 * nchunks;
+  a.coff = b->d_off;
+  a.voff = b->d_off + ninst + 1;
+  a.store = b->d_store;
+  a.order = d_order;
+  a.ninst = ninst;
+  a.next = d_next;
+  a.out = b->d_iout;
+  a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
+  a.smem_cap = smem;
+  const int grid = std::max(1, std::min(ninst, ctx->num_sms * per_sm));
+  PIR_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  k_instances<<<grid, block, smem, ctx->stream>>>(a);
+  PIR_CK(cudaGetLastError());
+  PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  if (nvars) {
+    k_unpack_int2<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(b->d_store, nvars, d_lb, d_ub);
+    PIR_CK(cudaMemcpyAsync(lb, d_lb, nvars * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PIR_CK(cudaMemcpyAsync(ub, d_ub, nvars * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  std::vector<InstOut> hout(ninst);
+  PIR_CK(cudaMemcpyAsync(hout.data(), b->d_iout, ninst * sizeof(InstOut), cudaMemcpyDeviceToHost, ctx->stream));
+  PIR_CK(cudaStreamSynchronize(ctx->stream));
+  pir_stats st;
+  std::memset(&st, 0, sizeof(st));
+  PIR_CK(cudaEventElapsedTime(&st.device_ms, ctx->ev0, ctx->ev1));
+  int worst = PIR_OK;
+  for (int j = 0; j < ninst; ++j) {
+    out_status[j] = hout[j].status;
+    if (out_rounds) out_rounds[j] = hout[j].rounds;
+    if (out_device_ms) out_device_ms[j] = (float)(hout[j].ns * 1e-6);
+    st.rounds = std::max<int64_t>(st.rounds, hout[j].rounds);
+    st.executions += (int64_t)hout[j].rounds * (prop_off[j + 1] - prop_off[j]);
+    st.narrowed += (int64_t)hout[j].narrowed;
+    if (hout[j].status == PIR_TIMEOUT) worst = PIR_TIMEOUT;
+  }
+  st.status = worst;
+  if (stats) *stats = st;
+  return PIR_OK;
+}
+
+extern "C" int pir_fixpoint_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, const int32_t *var,
+                                  const int32_t *lb, const int32_t *ub, const pir_opts *opts_in, int32_t *out_lb,
+                                  int32_t *out_ub, int32_t *out_status, int32_t *out_rounds, pir_stats *stats) {
+  if (!ctx) return PIR_EINVAL;
+  if (nnodes < 0 || (nnodes > 0 && (!off || !out_status))) return set_err(ctx, PIR_EINVAL, "bad arguments");
+  if ((out_lb == nullptr) != (out_ub == nullptr)) return set_err(ctx, PIR_EINVAL, "out_lb and out_ub go together");
+  if (nnodes == 0) return PIR_OK;
+  if (off[0] != 0) return set_err(ctx, PIR_EINVAL, "off[0] must be 0");
+  for (int j = 0; j < nnodes; ++j)
+    if (off[j + 1] < off[j]) return set_err(ctx, PIR_EINVAL, "node %d: offsets decrease", j);
+  const int ntight = off[nnodes];
+  if (ntight > 0 && (!var || !lb || !ub)) return set_err(ctx, PIR_EINVAL, "null tightenings");
+  for (int k = 0; k < ntight; ++k)
+    if (var[k] < 0 || var[k] >= ctx->nvars) return set_err(ctx, PIR_EINVAL, "tightening %d: var out of range", k);
+  pir_opts opts;
+  std::memset(&opts, 0, sizeof(opts));
+  if (opts_in) opts = *opts_in;
+  PIR_CK(cudaSetDevice(ctx->device));
+  pir_stats st;
+  std::memset(&st, 0, sizeof(st));
+  if (ctx->failed || ctx->n == 0) {
+    // every node inherits the empty store, or there is nothing to propagate
+    std::vector<int32_t> blb(ctx->nvars), bub(ctx->nvars);
+    int r = pir_read_store(ctx, blb.data(), bub.data());
+    if (r) return r;
+    for (int j = 0; j < nnodes; ++j) {
+      bool f = ctx->failed;
+      std::vector<int32_t> nl(blb), nu(bub);
+      for (int k = off[j]; k < off[j + 1]; ++k) {
+        nl[var[k]] = std::max(nl[var[k]], lb[k]);
+        nu[var[k]] = std::min(nu[var[k]], ub[k]);
+        f |= nl[var[k]] > nu[var[k]] || nl[var[k]] == INF || nu[var[k]] == MINF;
+      }
+      out_status[j] = f ? PIR_FAILED : PIR_OK;
+      if (out_rounds) out_rounds[j] = 0;
+      if (out_lb) {
+        std::copy(nl.begin(), nl.end(), out_lb + (size_t)j * ctx->nvars);
+        std::copy(nu.begin(), nu.end(), out_ub + (size_t)j * ctx->nvars);
+      }
+    }
+    if (stats) *stats = st;
+    return PIR_OK;
+  }
+  BatchState *b = batch(ctx);
+  const int ngroups = (nnodes + 31) / 32;
+  const size_t group_bytes = (size_t)ctx->nvars * 32 * sizeof(int2);
+  int r;
+  if ((r = ensure(ctx, (void **)&b->d_nstore, &b->cap_nstore, group_bytes * ngroups))) return r;
+  if ((r = ensure(ctx, (void **)&b->d_tight, &b->cap_tight, ((size_t)nnodes + 1 + 3 * (size_t)ntight + 8) * sizeof(int))))
+    return r;
+  if ((r = ensure(ctx, (void **)&b->d_nout, &b->cap_nout, (size_t)nnodes * sizeof(NodeOut) + 64))) return r;
+  int *d_off = b->d_tight, *d_var = d_off + nnodes + 1, *d_lb = d_var + ntight, *d_ub = d_lb + ntight;
+  int *d_next = d_ub + ntight;
+  static_assert(sizeof(NodeOut) == 8, "NodeOut packs to 8 bytes");
+  unsigned long long *d_nar =
+      reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(b->d_nout) + (size_t)nnodes * sizeof(NodeOut));
+  PIR_CK(cudaMemcpyAsync(d_off, off, (nnodes + 1) * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  if (ntight) {
+    PIR_CK(cudaMemcpyAsync(d_var, var, ntight * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    PIR_CK(cudaMemcpyAsync(d_lb, lb, ntight * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    PIR_CK(cudaMemcpyAsync(d_ub, ub, ntight * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  PIR_CK(cudaMemsetAsync(d_next, 0, 4 * sizeof(int), ctx->stream));
+  PIR_CK(cudaMemsetAsync(d_nar, 0, sizeof(unsigned long long), ctx->stream));
+  NodeArgs a;
+  a.bc = bytecode_view(ctx);
+  a.nvars = ctx->nvars;
+  a.base = ctx->d_store;
+  a.nstore = b->d_nstore;
+  a.off = d_off;
+  a.var = d_var;
+  a.lb = d_lb;
+  a.ub = d_ub;
+  a.nnodes = nnodes;
+  a.ngroups = ngroups;
+  a.next = d_next;
+  a.out = b->d_nout;
+  a.narrowed = d_nar;
+  a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
+  const int block = opts.block > 0 ? std::min(opts.block, 512) : 512;
+  int occ = 0;
+  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nodes, block, 0));
+  const int per_sm = opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
+  const int grid = std::max(1, std::min(ngroups, ctx->num_sms * per_sm));
+  PIR_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  k_nodes<<<grid, block, 0, ctx->stream>>>(a);
+  PIR_CK(cudaGetLastError());
+  PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  std::vector<NodeOut> hout(nnodes);
+  unsigned long long hnar = 0;
+  PIR_CK(cudaMemcpyAsync(hout.data(), b->d_nout, nnodes * sizeof(NodeOut), cudaMemcpyDeviceToHost, ctx->stream));
+  PIR_CK(cudaMemcpyAsync(&hnar, d_nar, sizeof(hnar), cudaMemcpyDeviceToHost, ctx->stream));
+  if (out_lb) {
+    // stage node-major outputs in chunks of nodes to bound the staging buffer
+    int per = (int)std::min<long long>(nnodes, (256ll << 20) / std::max<long long>(8ll * ctx->nvars, 1));
+    if (per < nnodes) per = std::max(32, (per / 32) * 32);
+    if ((r = ensure(ctx, (void **)&b->d_nio, &b->cap_nio, (size_t)per * ctx->nvars * 2 * sizeof(int)))) return r;
+    for (int j0 = 0; j0 < nnodes; j0 += per) {
+      const int cnt = std::min(per, nnodes - j0);
+      // the unpack kernel indexes groups from node 0; offset the store by whole groups
+      const int2 *src = b->d_nstore + (size_t)(j0 / 32) * ctx->nvars * 32;
+      if (j0 % 32 != 0) return set_err(ctx, PIR_EINVAL, "internal: unaligned node chunk");
+      k_nodes_unpack<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(src, ctx->nvars, cnt, b->d_nio,
+                                                                  b->d_nio + (size_t)cnt * ctx->nvars);
+      PIR_CK(cudaGetLastError());
+      PIR_CK(cudaMemcpyAsync(out_lb + (size_t)j0 * ctx->nvars, b->d_nio, (size_t)cnt * ctx->nvars * sizeof(int),
+                             cudaMemcpyDeviceToHost, ctx->stream));
+      PIR_CK(cudaMemcpyAsync(out_ub + (size_t)j0 * ctx->nvars, b->d_nio + (size_t)cnt * ctx->nvars,
+                             (size_t)cnt * ctx->nvars * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+  }
+  PIR_CK(cudaStreamSynchronize(ctx->stream));
+  PIR_CK(cudaEventElapsedTime(&st.device_ms, ctx->ev0, ctx->ev1));
+  int worst = PIR_OK;
+  for (int j = 0; j < nnodes; ++j) {
+    out_status[j] = hout[j].status;
+    if (out_rounds) out_rounds[j] = hout[j].rounds;
+    st.rounds = std::max<int64_t>(st.rounds, hout[j].rounds);
+    st.executions += (int64_t)hout[j].rounds * ctx->n;
+    if (hout[j].status == PIR_TIMEOUT) worst = PIR_TIMEOUT;
+  }
+  st.narrowed = (int64_t)hnar;
+  st.status = worst;
+  if (stats) *stats = st;
+  return PIR_OK;
 }

@@ -16,19 +16,22 @@ using namespace pirgpu;
 // ============================================================== kernels =====
 
 // Persistent AC-1 fixpoint: one cooperative launch, rounds separated by the
-// bounded grid barrier.  Thread 0 of CTA 0 writes the round count.
-__global__ void __launch_bounds__(256) k_fixpoint_persistent(Bytecode bc, int2 *store, Control *ctl,
-                                                             long long max_rounds,
-                                                             long long timeout_ns) {
+// bounded grid barrier.  PPI propagators per thread and step; MINB CTAs of 256
+// threads per SM bound the register budget.  Thread 0 of CTA 0 writes the
+// round count.
+template <int PPI, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_fixpoint_persistent(Bytecode bc, int2 *store, Control *ctl,
+                                                                   long long max_rounds, long long timeout_ns) {
   __shared__ unsigned s_word;
   RedStore st{store};
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gstride = gridDim.x * blockDim.x;
+  const int nsteps = steps_of<PPI>(bc);
   unsigned long long narrowed = 0;
   long long round = 0;
   for (;;) {
     int changed = 0, failed = 0;
-    for (int c = gtid; c < bc.nchunks; c += gstride) changed += sweep_chunk(bc, c, st, failed);
+    for (int c = gtid; c < nsteps; c += gstride) changed += sweep_step<PPI>(bc, c, st, failed);
     narrowed += changed;
     const int any_changed = __syncthreads_or(changed);
     const int any_failed = __syncthreads_or(failed);
@@ -49,6 +52,20 @@ __global__ void __launch_bounds__(256) k_fixpoint_persistent(Bytecode bc, int2 *
   narrowed = warp_sum64(narrowed);
   if ((threadIdx.x & 31) == 0 && narrowed) atomicAdd(&ctl->narrowed, narrowed);
 }
+
+// The persistent variants the autotuner chooses from: (propagators per thread
+// and step, minimum resident CTAs per SM).
+struct PersistentVariant {
+  int ppi, minb;
+  const void *fn;
+};
+static const PersistentVariant kPersistent[] = {
+    {4, 2, (const void *)k_fixpoint_persistent<4, 2>}, {4, 3, (const void *)k_fixpoint_persistent<4, 3>},
+    {2, 3, (const void *)k_fixpoint_persistent<2, 3>}, {2, 4, (const void *)k_fixpoint_persistent<2, 4>},
+    {1, 4, (const void *)k_fixpoint_persistent<1, 4>}, {1, 6, (const void *)k_fixpoint_persistent<1, 6>},
+    {4, 1, (const void *)k_fixpoint_persistent<4, 1>}, {2, 2, (const void *)k_fixpoint_persistent<2, 2>},
+};
+static const int kNumPersistent = sizeof(kPersistent) / sizeof(kPersistent[0]);
 
 // One AC-1 round per launch (host-driven loop).  Change flag per round parity.
 __global__ void __launch_bounds__(256) k_sweep_round(Bytecode bc, int2 *store, Control *ctl, int parity) {
@@ -413,6 +430,18 @@ int pir_embed(pirgpu_ctx *ctx, int32_t var, int32_t lb, int32_t ub, int *changed
   return apply_meets(ctx, v, l, u, changed);
 }
 
+int pir_embed_many(pirgpu_ctx *ctx, int32_t count, const int32_t *var, const int32_t *lb, const int32_t *ub,
+                   int *changed) {
+  if (!ctx) return PIR_EINVAL;
+  if (changed) *changed = 0;
+  if (count < 0 || (count > 0 && (!var || !lb || !ub))) return set_err(ctx, PIR_EINVAL, "bad arguments");
+  for (int32_t k = 0; k < count; ++k)
+    if (var[k] < 0 || var[k] >= ctx->nvars) return set_err(ctx, PIR_EINVAL, "var %d out of range", var[k]);
+  CK(cudaSetDevice(ctx->device));
+  std::vector<int> v(var, var + count), l(lb, lb + count), u(ub, ub + count);
+  return apply_meets(ctx, v, l, u, changed);
+}
+
 int pir_tell(pirgpu_ctx *ctx, int32_t n, const int32_t *op, const int32_t *x, const int32_t *y, const int32_t *z,
              int *changed) {
   if (!ctx) return PIR_EINVAL;
@@ -540,15 +569,20 @@ int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
     CK(cudaGetLastError());
   } else if (mode == PIR_MODE_PERSISTENT) {
     const int block = 256;
+    int vi = opts.variant > 0 ? opts.variant - 1 : (ctx->tuned_variant >= 0 ? ctx->tuned_variant : 0);
+    if (vi < 0 || vi >= kNumPersistent) return set_err(ctx, PIR_EINVAL, "unknown kernel variant %d", opts.variant);
+    const PersistentVariant &pv = kPersistent[vi];
     int occ = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fixpoint_persistent, block, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pv.fn, block, 0));
     if (occ < 1) return set_err(ctx, PIR_ECUDA, "persistent kernel does not fit on an SM");
     int per_sm = opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ;
     int grid = ctx->num_sms * per_sm;
-    grid = std::max(1, std::min(grid, (bc.nchunks + block - 1) / block));
+    const int nsteps = bc.nchunks * (4 / pv.ppi);
+    grid = std::max(1, std::min(grid, (nsteps + block - 1) / block));
     void *args[] = {&bc, &ctx->d_store, &ctx->d_ctl, (void *)&max_rounds, (void *)&timeout};
-    CK(cudaLaunchCooperativeKernel((void *)k_fixpoint_persistent, dim3(grid), dim3(block), args, 0, ctx->stream));
+    CK(cudaLaunchCooperativeKernel(pv.fn, dim3(grid), dim3(block), args, 0, ctx->stream));
     ctx->last_grid = grid;
+    ctx->last_variant = vi;
   } else if (mode == PIR_MODE_HOSTLOOP) {
     const int block = opts.block > 0 ? opts.block : 256;
     const int grid = std::max(1, std::min(ctx->num_sms * 8, (bc.nchunks + block - 1) / block));
@@ -585,6 +619,63 @@ int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
   if (stats) *stats = st;
   if (status == PIR_BARRIER_TIMEOUT) set_err(ctx, status, "grid barrier wait exceeded %lld ns", timeout);
   return status;
+}
+
+int pir_autotune(pirgpu_ctx *ctx, int32_t rounds, int32_t *out_variant, float *out_us_per_round) {
+  if (!ctx) return PIR_EINVAL;
+  if (out_variant) *out_variant = 0;
+  if (out_us_per_round) *out_us_per_round = 0.f;
+  if (ctx->n == 0 || ctx->failed || ctx->nvars == 0) return PIR_OK;
+  if (rounds <= 0) rounds = 16;
+  CK(cudaSetDevice(ctx->device));
+  int2 *saved = nullptr;
+  if (cudaMalloc(&saved, (size_t)ctx->nvars * sizeof(int2)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, PIR_ENOMEM, "autotune: no room to save the store");
+  }
+  const size_t bytes = (size_t)ctx->nvars * sizeof(int2);
+  CK(cudaMemcpyAsync(saved, ctx->d_store, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  const bool failed0 = ctx->failed;
+  int best = -1;
+  float best_us = 0.f;
+  int rc = PIR_OK;
+  for (int v = 0; v < kNumPersistent && rc == PIR_OK; ++v) {
+    float us = -1.f;
+    for (int rep = 0; rep < 2; ++rep) {
+      if (cudaMemcpyAsync(ctx->d_store, saved, bytes, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess) {
+        rc = cuda_err(ctx, cudaGetLastError(), "autotune restore");
+        break;
+      }
+      ctx->failed = failed0;
+      pir_opts o;
+      std::memset(&o, 0, sizeof(o));
+      o.mode = PIR_MODE_PERSISTENT;
+      o.max_rounds = rounds;
+      o.variant = v + 1;
+      pir_stats st;
+      const int r = pir_fixpoint(ctx, &o, &st);
+      if (r != PIR_OK && r != PIR_TIMEOUT && r != PIR_FAILED) {
+        rc = r;
+        break;
+      }
+      const float t = st.rounds > 0 ? st.device_ms * 1e3f / (float)st.rounds : 0.f;
+      if (us < 0.f || t < us) us = t;
+    }
+    if (rc == PIR_OK && us >= 0.f && (best < 0 || us < best_us)) {
+      best = v;
+      best_us = us;
+    }
+  }
+  cudaMemcpyAsync(ctx->d_store, saved, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(saved);
+  ctx->failed = failed0;
+  if (rc != PIR_OK) return rc;
+  ctx->tuned_variant = best;
+  ctx->tuned_version = ctx->bytecode_version;
+  if (out_variant) *out_variant = best + 1;
+  if (out_us_per_round) *out_us_per_round = best_us;
+  return PIR_OK;
 }
 
 int pir_deduce_one(pirgpu_ctx *ctx, int64_t i, int *changed) {

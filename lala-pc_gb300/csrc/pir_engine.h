@@ -43,6 +43,9 @@ struct pirgpu_ctx {
   size_t cap_scratch = 0;
   int last_grid = 0;
   int last_mode = 0;
+  int last_variant = 0;
+  int tuned_variant = -1;      // autotuned persistent variant (index), -1: none
+  long long tuned_version = -1;  // bytecode_version the tuning was made for
 
   pirgpu::BatchState *batch = nullptr;
   pirgpu::SchedState *sched = nullptr;

@@ -77,7 +77,7 @@ static __device__ __noinline__ unsigned grid_sync_or(Control *ctl, unsigned nblo
     const unsigned g = ld_acquire(&ctl->gen);
     if ((g & GEN_MASK) != (g0 & GEN_MASK)) return g;
     if (it >= 32) __nanosleep(it < 256 ? 32 : 200);
-    if ((it & 63u) == 63u) {
+    if ((it & 7u) == 0u) {
       if (*(volatile int *)&ctl->status) return BIT_ERROR;
       if ((long long)(globaltimer() - t0) > timeout_ns) {
         atomicCAS(&ctl->status, 0, ERR_BARRIER_TIMEOUT);
@@ -120,21 +120,59 @@ struct RedStore {
   }
 };
 
-// Four propagators of chunk c: all twelve intervals are gathered first (reads
-// may be stale within a round), then the four updates are applied in order.
-template <class S>
-static __device__ __forceinline__ int sweep_chunk(const Bytecode &bc, int c, S &st, int &failed) {
-  const int4 o = __ldg(bc.op + c), X = __ldg(bc.x + c), Y = __ldg(bc.y + c), Z = __ldg(bc.z + c);
-  Itv a0 = st.load(X.x), b0 = st.load(Y.x), c0 = st.load(Z.x);
-  Itv a1 = st.load(X.y), b1 = st.load(Y.y), c1 = st.load(Z.y);
-  Itv a2 = st.load(X.z), b2 = st.load(Y.z), c2 = st.load(Z.z);
-  Itv a3 = st.load(X.w), b3 = st.load(Y.w), c3 = st.load(Z.w);
+// Propagators c*PPI .. c*PPI+PPI-1 (PPI = 1, 2 or 4 per thread and step): all
+// intervals are gathered first (reads may be stale within a round), then the
+// updates are applied in order.  The bytecode arrays are read with 32-, 64- or
+// 128-bit loads.
+template <int PPI>
+struct Vec;
+template <>
+struct Vec<1> {
+  using T = int;
+  static __device__ __forceinline__ int get(const T &v, int) { return v; }
+};
+template <>
+struct Vec<2> {
+  using T = int2;
+  static __device__ __forceinline__ int get(const T &v, int k) { return k == 0 ? v.x : v.y; }
+};
+template <>
+struct Vec<4> {
+  using T = int4;
+  static __device__ __forceinline__ int get(const T &v, int k) {
+    return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+  }
+};
+
+template <int PPI, class S>
+__device__ __forceinline__ int sweep_step(const Bytecode &bc, int c, S &st, int &failed) {
+  using V = typename Vec<PPI>::T;
+  const V o = __ldg(reinterpret_cast<const V *>(bc.op) + c), X = __ldg(reinterpret_cast<const V *>(bc.x) + c);
+  const V Y = __ldg(reinterpret_cast<const V *>(bc.y) + c), Z = __ldg(reinterpret_cast<const V *>(bc.z) + c);
+  Itv a[PPI], b[PPI], d[PPI];
+#pragma unroll
+  for (int k = 0; k < PPI; ++k) {
+    a[k] = st.load(Vec<PPI>::get(X, k));
+    b[k] = st.load(Vec<PPI>::get(Y, k));
+    d[k] = st.load(Vec<PPI>::get(Z, k));
+  }
   int ch = 0;
-  ch += deduce_loaded(o.x, X.x, Y.x, Z.x, a0, b0, c0, st, failed);
-  ch += deduce_loaded(o.y, X.y, Y.y, Z.y, a1, b1, c1, st, failed);
-  ch += deduce_loaded(o.z, X.z, Y.z, Z.z, a2, b2, c2, st, failed);
-  ch += deduce_loaded(o.w, X.w, Y.w, Z.w, a3, b3, c3, st, failed);
+#pragma unroll
+  for (int k = 0; k < PPI; ++k)
+    ch += deduce_loaded(Vec<PPI>::get(o, k), Vec<PPI>::get(X, k), Vec<PPI>::get(Y, k), Vec<PPI>::get(Z, k), a[k],
+                        b[k], d[k], st, failed);
   return ch;
+}
+
+// Number of PPI-wide steps covering the (4-padded) bytecode.
+template <int PPI>
+__device__ __forceinline__ int steps_of(const Bytecode &bc) {
+  return bc.nchunks * (4 / PPI);
+}
+
+template <class S>
+__device__ __forceinline__ int sweep_chunk(const Bytecode &bc, int c, S &st, int &failed) {
+  return sweep_step<4>(bc, c, st, failed);
 }
 
 }  // namespace pirgpu

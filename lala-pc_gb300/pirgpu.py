@@ -33,7 +33,8 @@ class Opts(ctypes.Structure):
     _fields_ = [("max_rounds", ctypes.c_int64), ("barrier_timeout_ns", ctypes.c_int64),
                 ("mode", ctypes.c_int32), ("block", ctypes.c_int32),
                 ("ctas_per_sm", ctypes.c_int32), ("sched", ctypes.c_int32),
-                ("wake_fraction", ctypes.c_float), ("reserved", ctypes.c_int32 * 7)]
+                ("wake_fraction", ctypes.c_float), ("variant", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
 
 
 class Stats(ctypes.Structure):
@@ -63,12 +64,15 @@ SIGNATURES = [
     ("pir_project", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P]),
     ("pir_embed", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                  ctypes.POINTER(ctypes.c_int)]),
+    ("pir_embed_many", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P,
+                                      ctypes.POINTER(ctypes.c_int)]),
     ("pir_tell", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P, _I32P,
                                 ctypes.POINTER(ctypes.c_int)]),
     ("pir_num_deductions", ctypes.c_int64, [_P]),
     ("pir_vars", ctypes.c_int32, [_P]),
     ("pir_get_bytecode", ctypes.c_int, [_P, _I32P, _I32P, _I32P, _I32P]),
     ("pir_fixpoint", ctypes.c_int, [_P, ctypes.POINTER(Opts), ctypes.POINTER(Stats)]),
+    ("pir_autotune", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _F32P]),
     ("pir_deduce_one", ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
     ("pir_ask", ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
     ("pir_ask_all", ctypes.c_int, [_P, _U8P]),
@@ -114,10 +118,10 @@ def _c32(a):
 
 
 def make_opts(mode=MODE_AUTO, max_rounds=0, barrier_timeout_ns=0, block=0, ctas_per_sm=0,
-              sched=SCHED_AC1, wake_fraction=0.0):
+              sched=SCHED_AC1, wake_fraction=0.0, variant=0):
     o = Opts()
     o.max_rounds, o.barrier_timeout_ns, o.mode, o.block = max_rounds, barrier_timeout_ns, mode, block
-    o.ctas_per_sm, o.sched, o.wake_fraction = ctas_per_sm, sched, wake_fraction
+    o.ctas_per_sm, o.sched, o.wake_fraction, o.variant = ctas_per_sm, sched, wake_fraction, variant
     return o
 
 
@@ -177,6 +181,13 @@ class Context:
         self._check(self._L.pir_embed(self.h, v, lb, ub, ctypes.byref(ch)))
         return bool(ch.value)
 
+    def embed_many(self, var, lb, ub):
+        var, lb, ub = map(_c32, (var, lb, ub))
+        ch = ctypes.c_int(0)
+        self._check(self._L.pir_embed_many(self.h, len(var), _p32(var), _p32(lb), _p32(ub),
+                                           ctypes.byref(ch)))
+        return bool(ch.value)
+
     def vars(self):
         return self._L.pir_vars(self.h)
 
@@ -204,6 +215,13 @@ class Context:
         rc = self._L.pir_fixpoint(self.h, ctypes.byref(o), ctypes.byref(s))
         self._check(rc, (OK, FAILED, TIMEOUT, BARRIER_TIMEOUT))
         return rc, s.asdict()
+
+    def autotune(self, rounds=16):
+        """Times the persistent-kernel variants; returns (variant, us per round)."""
+        v = ctypes.c_int32(0)
+        us = ctypes.c_float(0)
+        self._check(self._L.pir_autotune(self.h, rounds, ctypes.byref(v), ctypes.byref(us)))
+        return v.value, us.value
 
     def deduce_one(self, i):
         ch = ctypes.c_int(0)

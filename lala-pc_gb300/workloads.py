@@ -304,22 +304,28 @@ def single_large(seed=0, variant="planted", nvars=1_000_000, nprops=4_000_000, c
     return add_chain(inst, chain, 1_000_000, seed) if chain else inst
 
 
-def nodes(base_vars=100_000, base_props=400_000, nnodes=4096, seed=0, kmax=64, base_store=None):
-    """Search nodes over a base instance: node j bisects k_j ~ U[1, kmax]
-    random variables of `base_store` (lb, ub arrays; the base instance's
-    fixpoint in practice) at mid = lb + (ub - lb) / 2, keeping the lower half
-    [lb, mid] or the upper half [mid + 1, ub] by a coin flip.  Returns
-    (base Instance, off, var, lb, ub) with the tightenings in CSR form."""
-    base = plain(base_vars, base_props, 1000, seed)
+def nodes(base_vars=100_000, base_props=400_000, nnodes=4096, seed=0, kmax=64, base_store=None,
+          scale=1_000_000):
+    """Search nodes over a base instance (bounds scale 1e6: at scale 1e3 the
+    planted base's fixpoint fixes nearly every variable and leaves nothing to
+    branch on): node j bisects k_j ~ U[1, kmax]
+    random unfixed variables (lb < ub) of `base_store` (lb, ub arrays; the base
+    instance's fixpoint in practice) at mid = lb + (ub - lb) / 2, keeping the
+    lower half [lb, mid] or the upper half [mid + 1, ub] by a coin flip.
+    Returns (base Instance, off, var, lb, ub) with the tightenings in CSR form."""
+    base = plain(base_vars, base_props, scale, seed)
     if base_store is None:
         blb, bub = base.lb.astype(np.int64), base.ub.astype(np.int64)
     else:
         blb, bub = (np.asarray(a, np.int64) for a in base_store)
+    free = np.nonzero(blb[:base_vars] < bub[:base_vars])[0]
+    if len(free) == 0:
+        raise ValueError("every variable of the base store is fixed")
     rng = Rng(seed, 101)
     k = rng.integers(1, kmax, nnodes)
     off = np.concatenate([[0], np.cumsum(k)]).astype(np.int32)
     tot = int(off[-1])
-    var = rng.integers(0, base_vars - 1, tot)
+    var = free[rng.integers(0, len(free) - 1, tot)]
     lo, hi = blb[var], bub[var]
     mid = lo + (hi - lo) // 2
     upper = rng.integers(0, 1, tot) == 1

@@ -1,0 +1,120 @@
+"""Batched fixpoints (search nodes, uneven instances) against the CPU oracle:
+bit-exact stores of the nodes / instances that reach a fixpoint and identical
+status flags."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def P():
+    import pirgpu
+    return pirgpu
+
+
+def _uneven_set(seed, n=24, pmin=500, pmax=20_000, spec_every=0):
+    import workloads as W
+    insts = W.uneven(ninst=n, pmin=pmin, pmax=pmax, seed=seed)
+    if spec_every:
+        for j in range(0, n, spec_every):
+            p = insts[j].nprops
+            insts[j] = W.plain(max(p // 4, 8), p, 1000, 1000 + j, variant="spec", mix=W.MIX_UNEVEN)
+    return insts
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_instances_parity(seed, P, oracle):
+    import workloads as W
+    insts = _uneven_set(seed, spec_every=7)
+    prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
+    glb, gub = lb.copy(), ub.copy()
+    ctx = P.Context(0)
+    status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, glb, gub)
+    nfail = 0
+    for j, inst in enumerate(insts):
+        s = inst.store()
+        orc, info = oracle.install(inst.op, inst.x, inst.y, inst.z, s)
+        if orc != oracle.FAILED:
+            # same propagator order as the GPU: the given one
+            orc, info = oracle.fixpoint(inst.op, inst.x, inst.y, inst.z, s)
+        assert status[j] == orc, j
+        v0, v1 = var_off[j], var_off[j + 1]
+        if orc == oracle.OK:
+            np.testing.assert_array_equal(glb[v0:v1], s[:, 0])
+            np.testing.assert_array_equal(gub[v0:v1], s[:, 1])
+        else:
+            nfail += 1
+    assert nfail >= 3  # the spec-variant instances fail
+    assert np.all(ms > 0)
+    assert st["executions"] == int(sum(rounds[j] * insts[j].nprops for j in range(len(insts))))
+
+
+def test_instances_smem_and_global_paths(P, oracle):
+    """Small instances run from shared memory, the largest from the global
+    store: both agree with the oracle."""
+    import workloads as W
+    insts = [W.plain(200, 800, 1000, 1), W.plain(60_000, 240_000, 1000, 2, mix=W.MIX_UNEVEN),
+             W.plain(3000, 12_000, 1000, 3, mix=W.MIX_UNEVEN)]
+    prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
+    ctx = P.Context(0)
+    status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
+    for j, inst in enumerate(insts):
+        s = inst.store()
+        oracle.install(inst.op, inst.x, inst.y, inst.z, s)
+        orc, _ = oracle.fixpoint(inst.op, inst.x, inst.y, inst.z, s)
+        assert status[j] == orc == oracle.OK
+        np.testing.assert_array_equal(lb[var_off[j]:var_off[j + 1]], s[:, 0])
+        np.testing.assert_array_equal(ub[var_off[j]:var_off[j + 1]], s[:, 1])
+
+
+def test_instances_round_cap(P):
+    import workloads as W
+    insts = [W.add_chain(W.plain(2000, 8000, 1000, 4), 100, 1000, 4)]
+    prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
+    ctx = P.Context(0)
+    status, rounds, _, _ = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub, max_rounds=7)
+    assert status[0] == P.TIMEOUT and rounds[0] == 7
+
+
+def _nodes_setup(P, nvars=5000, nprops=20_000, nnodes=200, kmax=48, seed=0):
+    import workloads as W
+    base = W.plain(nvars, nprops, 10**6, seed)
+    ctx = P.Context(0)
+    ctx.load_store(base.lb, base.ub)
+    ctx.tell(base.op, base.x, base.y, base.z)
+    rc, _ = ctx.fixpoint()
+    assert rc == P.OK
+    blb, bub = ctx.read_store()
+    _, off, var, lb, ub = W.nodes(nvars, nprops, nnodes, seed, kmax, base_store=(blb, bub))
+    return ctx, (blb, bub), off, var, lb, ub
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_nodes_parity(seed, P, oracle):
+    ctx, (blb, bub), off, var, lb, ub = _nodes_setup(P, seed=seed)
+    status, olb, oub, rounds, st = ctx.fixpoint_nodes(off, var, lb, ub)
+    op, x, y, z = ctx.bytecode()
+    base = np.ascontiguousarray(np.stack([blb, bub], 1))
+    ostatus, ostore, ostats = oracle.fixpoint_nodes(op, x, y, z, base, off, var, lb, ub)
+    np.testing.assert_array_equal(status, ostatus)
+    ok = ostatus == oracle.OK
+    assert ok.sum() > 0 and (~ok).sum() > 0  # both outcomes are exercised
+    np.testing.assert_array_equal(olb[ok], ostore[ok, :, 0])
+    np.testing.assert_array_equal(oub[ok], ostore[ok, :, 1])
+    # the context's own store is untouched
+    l2, u2 = ctx.read_store()
+    np.testing.assert_array_equal(l2, blb)
+
+
+def test_nodes_partial_group_and_cap(P, oracle):
+    ctx, (blb, bub), off, var, lb, ub = _nodes_setup(P, nnodes=45, seed=5)
+    status, olb, oub, rounds, st = ctx.fixpoint_nodes(off, var, lb, ub)
+    op, x, y, z = ctx.bytecode()
+    base = np.ascontiguousarray(np.stack([blb, bub], 1))
+    ostatus, ostore, _ = oracle.fixpoint_nodes(op, x, y, z, base, off, var, lb, ub)
+    np.testing.assert_array_equal(status, ostatus)
+    ok = ostatus == oracle.OK
+    np.testing.assert_array_equal(olb[ok], ostore[ok, :, 0])
+    capped, _, _, r2, _ = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, max_rounds=1)
+    assert np.all((capped != P.OK) | (r2 <= 1))

@@ -157,7 +157,7 @@ def test_barrier_timeout_is_reported(P):
     """A grid-barrier wait bounded to 1 ns runs out: the kernel returns
     BARRIER_TIMEOUT and the context stays usable."""
     import workloads as W
-    inst = W.add_chain(W.plain(200_000, 800_000, 1000, 2), 50, 1000, 2)
+    inst = W.add_chain(W.plain(1_000_000, 4_000_000, 1000, 2), 150, 1000, 2)
     ctx = P.Context(0)
     ctx.load_store(inst.lb, inst.ub)
     ctx.tell(inst.op, inst.x, inst.y, inst.z)
@@ -214,3 +214,28 @@ def test_engine_order_is_reference_sort(P, oracle):
     _, perm = oracle.install(inst.op, inst.x, inst.y, inst.z, inst.store())
     for a, b in zip(ctx.bytecode(), (inst.op, inst.x, inst.y, inst.z)):
         np.testing.assert_array_equal(a, b[perm])
+
+
+@pytest.mark.parametrize("variant", range(1, 9))
+def test_persistent_variants(variant, P, oracle):
+    """Every autotuner candidate computes the same fixpoint."""
+    import workloads as W
+    inst = W.add_chain(W.plain(30_000, 120_000, 1000, 8), 100, 1000, 8)
+    rc, s, _, _ = _gpu_fixpoint(P, inst, mode=P.MODE_PERSISTENT, variant=variant)
+    orc, os_, _ = _oracle_fixpoint(oracle, inst)
+    assert rc == orc == P.OK
+    np.testing.assert_array_equal(s, os_)
+
+
+def test_autotune_keeps_store(P):
+    import workloads as W
+    inst = W.plain(30_000, 120_000, 1000, 9)
+    ctx = P.Context(0)
+    ctx.load_store(inst.lb, inst.ub)
+    ctx.tell(inst.op, inst.x, inst.y, inst.z)
+    before = ctx.read_store()
+    v, us = ctx.autotune(8)
+    assert 1 <= v <= 8 and us > 0
+    after = ctx.read_store()
+    np.testing.assert_array_equal(before[0], after[0])
+    np.testing.assert_array_equal(before[1], after[1])
