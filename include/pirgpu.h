@@ -134,6 +134,10 @@ int pir_deduce_one(pirgpu_ctx *ctx, int64_t i, int *changed);
 int pir_ask(pirgpu_ctx *ctx, int64_t i, int *entailed);
 /* ask(i) for every i (engine order); out has num_deductions() bytes. */
 int pir_ask_all(pirgpu_ctx *ctx, uint8_t *entailed);
+/* ask(ask_type) for its bytecode part, pir.hpp:372-380 with :417-438: the
+ * entailment of n given propagators (not installed) against the store. */
+int pir_ask_bytecodes(pirgpu_ctx *ctx, int32_t n, const int32_t *op, const int32_t *x,
+                      const int32_t *y, const int32_t *z, uint8_t *entailed);
 /* is_bot(), pir.hpp:831-833. */
 int pir_is_bot(pirgpu_ctx *ctx, int *bot);
 /* is_top(), pir.hpp:836-838. */

@@ -92,13 +92,14 @@ __device__ __forceinline__ void install_chunks(const Bytecode &bc, S &st) {
   }
 }
 
-template <class S>
+// GBC: the bytecode is in global memory (else it may be staged in shared memory).
+template <bool GBC, class S>
 __device__ __forceinline__ void cta_rounds(const Bytecode &bc, S &st, long long max_rounds, long long &rounds,
                                            int &failed, int &changed, unsigned long long &narrowed) {
   rounds = 0;
   for (;;) {
     int ch = 0, f = 0;
-    for (int c = threadIdx.x; c < bc.nchunks; c += blockDim.x) ch += sweep_chunk(bc, c, st, f);
+    for (int c = threadIdx.x; c < bc.nchunks; c += blockDim.x) ch += sweep_chunk<S, GBC>(bc, c, st, f);
     narrowed += ch;
     const int any_ch = __syncthreads_or(ch);
     const int any_f = __syncthreads_or(f);
@@ -141,7 +142,8 @@ __global__ void __launch_bounds__(512) k_instances(InstArgs a) {
       int2 *ss = reinterpret_cast<int2 *>(sm);
       for (int v = threadIdx.x; v < nv; v += blockDim.x) ss[v] = gs[v];
       Bytecode sb = bc;
-      if (store_bytes + nch * 64 <= a.smem_cap) {
+      const bool bc_in_smem = store_bytes + nch * 64 <= a.smem_cap;
+      if (bc_in_smem) {
         int4 *b4 = sm + store_bytes / 16;
         int4 *sop = b4, *sx = b4 + nch, *sy = b4 + 2 * nch, *sz = b4 + 3 * nch;
         for (int c = threadIdx.x; c < nch; c += blockDim.x) {
@@ -159,14 +161,17 @@ __global__ void __launch_bounds__(512) k_instances(InstArgs a) {
       SmemStore st{ss};
       install_chunks(sb, st);
       __syncthreads();
-      cta_rounds(sb, st, a.max_rounds, rounds, failed, changed, narrowed);
+      if (bc_in_smem)
+        cta_rounds<false>(sb, st, a.max_rounds, rounds, failed, changed, narrowed);
+      else
+        cta_rounds<true>(sb, st, a.max_rounds, rounds, failed, changed, narrowed);
       for (int v = threadIdx.x; v < nv; v += blockDim.x) gs[v] = ss[v];
     } else {
       GlobalStore gst{gs};
       install_chunks(bc, gst);
       __syncthreads();
       RedStore st{gs};
-      cta_rounds(bc, st, a.max_rounds, rounds, failed, changed, narrowed);
+      cta_rounds<true>(bc, st, a.max_rounds, rounds, failed, changed, narrowed);
     }
     narrowed = warp_sum64(narrowed);
     if ((threadIdx.x & 31) == 0 && narrowed) atomicAdd(&a.out[j].narrowed, narrowed);

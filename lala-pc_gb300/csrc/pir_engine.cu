@@ -709,6 +709,33 @@ int pir_ask_all(pirgpu_ctx *ctx, uint8_t *entailed) {
   return PIR_OK;
 }
 
+int pir_ask_bytecodes(pirgpu_ctx *ctx, int32_t n, const int32_t *op, const int32_t *x, const int32_t *y,
+                      const int32_t *z, uint8_t *entailed) {
+  if (!ctx) return PIR_EINVAL;
+  if (n < 0 || (n > 0 && (!op || !x || !y || !z || !entailed))) return set_err(ctx, PIR_EINVAL, "bad arguments");
+  if (n == 0) return PIR_OK;
+  for (int32_t i = 0; i < n; ++i) {
+    if (op[i] < 0 || op[i] >= OP_COUNT) return set_err(ctx, PIR_EINVAL, "bytecode %d: bad opcode %d", i, op[i]);
+    if (x[i] < 0 || x[i] >= ctx->nvars || y[i] < 0 || y[i] >= ctx->nvars || z[i] < 0 || z[i] >= ctx->nvars)
+      return set_err(ctx, PIR_EINVAL, "bytecode %d: var index out of range [0, %d)", i, ctx->nvars);
+  }
+  CK(cudaSetDevice(ctx->device));
+  int r;
+  if ((r = ensure(ctx, &ctx->d_scratch, &ctx->cap_scratch, (size_t)n * 17))) return r;
+  int *d = (int *)ctx->d_scratch;
+  unsigned char *out = (unsigned char *)(d + 4 * (size_t)n);
+  CK(cudaMemcpyAsync(d, op, n * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(d + n, x, n * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(d + 2 * (size_t)n, y, n * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(d + 3 * (size_t)n, z, n * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  const int grid = std::min(ctx->num_sms * 8, (n + 255) / 256);
+  k_ask_all<<<grid, 256, 0, ctx->stream>>>(d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n, n, ctx->d_store, out);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(entailed, out, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PIR_OK;
+}
+
 int pir_ask(pirgpu_ctx *ctx, int64_t i, int *entailed) {
   if (!ctx || !entailed) return PIR_EINVAL;
   if (i < 0 || i >= ctx->n) return set_err(ctx, PIR_EINVAL, "ask(%lld) out of range", (long long)i);

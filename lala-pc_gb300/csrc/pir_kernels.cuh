@@ -144,11 +144,19 @@ struct Vec<4> {
   }
 };
 
-template <int PPI, class S>
+// Bytecode loads: the read-only global path (ld.global.nc) when the bytecode is
+// in global memory (GBC), generic loads when it may be staged in shared memory.
+template <bool GBC, class V>
+__device__ __forceinline__ V bc_load(const V *p) {
+  if (GBC) return __ldg(p);
+  return *p;
+}
+
+template <int PPI, class S, bool GBC = true>
 __device__ __forceinline__ int sweep_step(const Bytecode &bc, int c, S &st, int &failed) {
   using V = typename Vec<PPI>::T;
-  const V o = __ldg(reinterpret_cast<const V *>(bc.op) + c), X = __ldg(reinterpret_cast<const V *>(bc.x) + c);
-  const V Y = __ldg(reinterpret_cast<const V *>(bc.y) + c), Z = __ldg(reinterpret_cast<const V *>(bc.z) + c);
+  const V o = bc_load<GBC>(reinterpret_cast<const V *>(bc.op) + c), X = bc_load<GBC>(reinterpret_cast<const V *>(bc.x) + c);
+  const V Y = bc_load<GBC>(reinterpret_cast<const V *>(bc.y) + c), Z = bc_load<GBC>(reinterpret_cast<const V *>(bc.z) + c);
   Itv a[PPI], b[PPI], d[PPI];
 #pragma unroll
   for (int k = 0; k < PPI; ++k) {
@@ -170,9 +178,9 @@ __device__ __forceinline__ int steps_of(const Bytecode &bc) {
   return bc.nchunks * (4 / PPI);
 }
 
-template <class S>
+template <class S, bool GBC = true>
 __device__ __forceinline__ int sweep_chunk(const Bytecode &bc, int c, S &st, int &failed) {
-  return sweep_step<4>(bc, c, st, failed);
+  return sweep_step<4, S, GBC>(bc, c, st, failed);
 }
 
 }  // namespace pirgpu

@@ -76,6 +76,7 @@ SIGNATURES = [
     ("pir_deduce_one", ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
     ("pir_ask", ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
     ("pir_ask_all", ctypes.c_int, [_P, _U8P]),
+    ("pir_ask_bytecodes", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P, _I32P, _U8P]),
     ("pir_is_bot", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     ("pir_is_top", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     ("pir_is_extractable", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
@@ -236,6 +237,14 @@ class Context:
     def ask_all(self):
         out = np.zeros(self.num_deductions(), np.uint8)
         self._check(self._L.pir_ask_all(self.h, out.ctypes.data_as(_U8P)))
+        return out.astype(bool)
+
+    def ask_bytecodes(self, op, x, y, z):
+        """Entailment of the given propagators against the store (ask(ask_type))."""
+        op, x, y, z = map(_c32, (op, x, y, z))
+        out = np.zeros(len(op), np.uint8)
+        self._check(self._L.pir_ask_bytecodes(self.h, len(op), _p32(op), _p32(x), _p32(y), _p32(z),
+                                              out.ctypes.data_as(_U8P)))
         return out.astype(bool)
 
     def _flag(self, fn):

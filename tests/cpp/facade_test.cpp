@@ -1,0 +1,154 @@
+// Known-answer cases of lala-pc's tests/pir_test.cpp written against the
+// lala_gpu::PIR facade (include/pirgpu.hpp), the way the reference's tests use
+// lala::PIR: interpret_tell, deduce(tell), then the fixpoint, then operator[]
+// and is_extractable.  Exit code 0 iff every expectation holds.
+#include <cstdio>
+#include <vector>
+
+#include "pirgpu.hpp"
+
+using namespace lala_gpu;
+
+static int failures = 0;
+#define EXPECT(cond)                                                    \
+  do {                                                                  \
+    if (!(cond)) {                                                      \
+      std::printf("FAIL %s:%d: %s\n", __FILE__, __LINE__, #cond);       \
+      ++failures;                                                       \
+    }                                                                   \
+  } while (0)
+
+static void tell(PIR &pir, const Formula &f) {
+  IDiagnostics d;
+  PIR::tell_type t;
+  EXPECT(pir.interpret_tell(f, t, d));
+  pir.deduce(t);
+}
+
+// tests/pir_test.cpp:175-182: x, y in [0, 10], z = 5, x + y = z.
+static void ternary_problem() {
+  PIR pir(std::vector<Itv>{Itv(0, 10), Itv(0, 10), Itv(5, 5)});
+  tell(pir, Formula::ternary(2, Sig::ADD, 0, 1));
+  EXPECT(pir.num_deductions() == 1);
+  EXPECT(pir[0] == Itv(0, 10));
+  EXPECT(pir.fixpoint() == PIR_OK);
+  EXPECT(pir[0] == Itv(0, 5));
+  EXPECT(pir[1] == Itv(0, 5));
+  EXPECT(pir[2] == Itv(5, 5));
+  EXPECT(!pir.is_extractable());
+}
+
+// tests/pir_test.cpp:321-329: x, y, z in [3, 10], x + y + z <= 8 fails.
+static void top_prop() {
+  PIR pir(std::vector<Itv>{Itv(3, 10), Itv(3, 10), Itv(3, 10), Itv::top(), Itv(INT32_MIN, 8)});
+  tell(pir, Formula::ternary(3, Sig::ADD, 0, 1));
+  tell(pir, Formula::ternary(4, Sig::ADD, 3, 2));
+  EXPECT(pir.num_deductions() == 2);
+  EXPECT(pir.fixpoint() == PIR_FAILED);
+  EXPECT(pir.is_bot());
+}
+
+// tests/pir_test.cpp:936-946: b = (x <= 5); then b = 0 gives x >= 6.
+static void infinite_domain2() {
+  PIR pir(std::vector<Itv>{Itv::top(), Itv::top(), Itv(5, 5)});  // x, b, the constant 5
+  tell(pir, Formula::ternary(1, Sig::LEQ, 0, 2));
+  EXPECT(pir[1] == Itv(0, 1));  // reified target forced to [0, 1] at install
+  EXPECT(pir.fixpoint() == PIR_OK);
+  EXPECT(pir[0] == Itv::top());
+  tell(pir, Formula::bound(1, Formula::EQ_CONST, 0));
+  EXPECT(pir.fixpoint() == PIR_OK);
+  EXPECT(pir[0] == Itv(6, INT32_MAX));
+  EXPECT(pir.is_extractable());
+}
+
+// tests/pir_test.cpp:625-640: min(x, y) = z with incremental tells.
+static void min_constraint1() {
+  PIR pir(std::vector<Itv>{Itv(0, 4), Itv(2, 5), Itv(0, 10)});
+  tell(pir, Formula::ternary(2, Sig::MIN, 0, 1));
+  pir.fixpoint();
+  EXPECT(pir[2] == Itv(0, 4));
+  tell(pir, Formula::bound(2, Formula::LEQ_CONST, 3));
+  pir.fixpoint();
+  EXPECT(pir[0] == Itv(0, 4) && pir[1] == Itv(2, 5) && pir[2] == Itv(0, 3));
+  tell(pir, Formula::bound(0, Formula::LEQ_CONST, 1));
+  pir.fixpoint();
+  EXPECT(pir[2] == Itv(0, 1));
+  tell(pir, Formula::bound(0, Formula::LEQ_CONST, 0));
+  pir.fixpoint();
+  EXPECT(pir[2] == Itv(0, 0));
+  EXPECT(pir.is_extractable());
+}
+
+// tests/pir_test.cpp:895-903: x = y tdiv z with x in [2,10], y in [-25,25], z in [-2,3].
+static void int_tdiv1() {
+  PIR pir(std::vector<Itv>{Itv(2, 10), Itv(-25, 25), Itv(-2, 3)});
+  tell(pir, Formula::ternary(0, Sig::TDIV, 1, 2));
+  pir.fixpoint();
+  EXPECT(pir[1] == Itv(-21, 25));
+}
+
+// The snapshot / embed / fixpoint / restore loop of
+// tests/bound_consistency_test.hpp:162-196 on int_times over [-3, 3].
+static void snapshot_loop() {
+  PIR pir(std::vector<Itv>{Itv(-3, 3), Itv(-3, 3), Itv(-3, 3)});
+  tell(pir, Formula::ternary(0, Sig::MUL, 1, 2));
+  auto snap = pir.snapshot();
+  int checked = 0;
+  for (int yl = -3; yl <= 3; ++yl)
+    for (int zl = -3; zl <= 3; zl += 2) {
+      pir.restore(snap);
+      pir.embed(1, Itv(yl, yl));
+      pir.embed(2, Itv(zl, zl));
+      EXPECT(pir.fixpoint() == (yl * zl >= -3 && yl * zl <= 3 ? PIR_OK : PIR_FAILED));
+      if (!pir.is_bot()) {
+        EXPECT(pir[0] == Itv(yl * zl, yl * zl));
+        EXPECT(pir.is_extractable());
+      }
+      ++checked;
+    }
+  pir.restore(snap);
+  EXPECT(pir[1] == Itv(-3, 3));
+  EXPECT(checked == 28);
+}
+
+// deduce(i) driven the way the reference tests drive it (a Gauss-Seidel loop
+// over i) reaches the fixpoint the GPU driver reaches.
+static void gauss_seidel_drop_in() {
+  std::vector<Itv> store{Itv(0, 10), Itv(0, 10), Itv(INT32_MIN, 5), Itv(-4, 3), Itv(2, 2), Itv::top()};
+  PIR a(store), b(store);
+  for (PIR *p : {&a, &b}) {
+    tell(*p, Formula::ternary(2, Sig::ADD, 0, 1));
+    tell(*p, Formula::ternary(5, Sig::MUL, 3, 4));
+    tell(*p, Formula::ternary(0, Sig::MAX, 3, 4));
+  }
+  bool changed = true;
+  while (changed) {
+    changed = false;
+    for (int64_t i = 0; i < a.num_deductions(); ++i) changed |= a.deduce(i);
+  }
+  EXPECT(b.fixpoint() == PIR_OK);
+  for (int v = 0; v < 6; ++v) EXPECT(a[v] == b[v]);
+}
+
+// Interpretation errors go to IDiagnostics (pir.hpp:282-286).
+static void interpretation_error() {
+  PIR pir(3);
+  IDiagnostics d;
+  PIR::tell_type t;
+  EXPECT(!pir.interpret_tell(Formula::ternary(0, Sig::ADD, 1, 7), t, d));
+  EXPECT(d.has_error());
+  EXPECT(t.bytecodes.empty());
+}
+
+int main() {
+  ternary_problem();
+  top_prop();
+  infinite_domain2();
+  min_constraint1();
+  int_tdiv1();
+  snapshot_loop();
+  gauss_seidel_drop_in();
+  interpretation_error();
+  std::printf("%d failures\n", failures);
+  return failures ? 1 : 0;
+}
