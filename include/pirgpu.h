@@ -187,6 +187,27 @@ int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int64_t *prop_o
                            const pir_opts *opts, int32_t *out_status, int32_t *out_rounds,
                            float *out_device_ms, pir_stats *stats);
 
+/* The plain fixpoint for callers that cannot allocate device memory.  No
+ * counterpart in the reference: lala-pc's PIR leaves the fixpoint loop and its
+ * memory to the caller.  Some callers own all device memory themselves (a
+ * solver that gives the engine slices of its own pool, or a search loop on many
+ * streams that cannot afford cudaMalloc / cudaFree, which may synchronize the
+ * device).  This call takes caller-owned device pointers: the bytecode d_op,
+ * d_x, d_y, d_z (n int32 each, already installed, any order) and the store
+ * d_store (nvars {lb, ub} int32 pairs, 8-byte aligned), which is updated in
+ * place, and allocates nothing: its scratch is a fixed array of about 8.5 KB
+ * per device inside the library, which holds it until exit.  The grid is at
+ * most 1024 CTAs; opts->ctas_per_sm asking for more (or for more than fit on an
+ * SM) is rejected with PIR_EINVAL, as are invalid opcodes or var indices
+ * (checked on the device; the store is left untouched).  The first call on a
+ * device looks up the scratch address (cudaGetSymbolAddress) and should come
+ * before any stream capture.  Calls share the scratch: calls that overlap on
+ * the GPU race and must not be issued.  stream may be NULL (default stream);
+ * the call returns once the fixpoint is done, with the status and stats. */
+int pir_fixpoint_static(const int32_t *d_op, const int32_t *d_x, const int32_t *d_y,
+                        const int32_t *d_z, int64_t n, int32_t *d_store, int32_t nvars,
+                        const pir_opts *opts, pir_stats *stats, void *stream);
+
 /* Number of SMs and the library's build string (for reports). */
 int pir_device_info(pirgpu_ctx *ctx, int32_t *num_sms, char *name, size_t name_len);
 

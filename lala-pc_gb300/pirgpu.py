@@ -92,6 +92,8 @@ SIGNATURES = [
                                               _I32P, _I32P, _I32P, _I32P, ctypes.POINTER(Opts),
                                               _I32P, _I32P, _F32P, ctypes.POINTER(Stats)]),
     ("pir_device_info", ctypes.c_int, [_P, _I32P, ctypes.c_char_p, ctypes.c_size_t]),
+    ("pir_fixpoint_static", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, _P, ctypes.c_int32,
+                                           ctypes.POINTER(Opts), ctypes.POINTER(Stats), _P]),
 ]
 
 
