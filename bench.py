@@ -438,6 +438,58 @@ def run_nodes(args):
     print(json.dumps(out), flush=True)
 
 
+def run_learned(args):
+    """Learned scheduler on search nodes of the 100,000-var / 400,000-propagator
+    base: trained on change traces of the plain fixpoint of 1,024 nodes (up to
+    1M samples), compared with plain AC-1 rounds on 256 held-out nodes."""
+    import pirgpu
+    ws, rank, local = dist_env()
+    cr = Cudart()
+    cr.set_device(local)
+    ctx, base, (blb, bub), off, var, lb, ub = _nodes_workload()
+    ntrain, ntest = 1024, 256
+    t0 = time.perf_counter()
+    ns, npos = ctx.sched_collect(off[:ntrain + 1], var, lb, ub, max_samples=1_000_000, keep_negative=0.01)
+    t_collect = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = ctx.sched_train(epochs=args.epochs, batch=8192, lr=3e-3, pos_weight=4.0)
+    t_train = time.perf_counter() - t0
+    snap = ctx.snapshot()
+
+    def run(sched, frac=0.0):
+        ex, dev, outs = 0, 0.0, []
+        for j in range(ntrain, ntrain + ntest):
+            ctx.restore(snap)
+            ctx.embed_many(var[off[j]:off[j + 1]], lb[off[j]:off[j + 1]], ub[off[j]:off[j + 1]])
+            rc, st = ctx.fixpoint(mode=1, sched=sched, wake_fraction=frac)
+            ex += st["executions"]
+            dev += st["device_ms"]
+            outs.append((rc, ctx.read_store()))
+        return ex, dev, outs
+
+    run(pirgpu.SCHED_AC1)  # warm-up
+    e0, d0, o0 = run(pirgpu.SCHED_AC1)
+    e1, d1, o1 = run(pirgpu.SCHED_LEARNED, args.wake_fraction)
+    same = sum(1 for (a, (l0, u0)), (b, (l1, u1)) in zip(o0, o1)
+               if a == b and (a != pirgpu.OK or (np.array_equal(l0, l1) and np.array_equal(u0, u1))))
+    ctx.restore(snap)
+    out = {
+        "metric": "propagator executions to fixpoint (learned vs AC-1)", "value": e0 / max(e1, 1),
+        "unit": "x fewer executions", "n_gpus": 1, "steps": ntest, "warmup": ntest,
+        "ms_per_step": d1 / ntest, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32 propagation, bf16 weights / fp32 accumulate scorer",
+        "data": "synthetic: planted-solution base at its fixpoint, bisected nodes",
+        "config": {"workload": "learned: 100,000 vars / 400,000 propagators, trained on %d nodes, tested on %d held-out nodes" % (ntrain, ntest),
+                   "samples": ns, "positives": npos, "collect_s": t_collect, "train_s": t_train,
+                   "epochs": args.epochs, "loss": [float(v) for v in loss], "wake_fraction": args.wake_fraction},
+        "ac1": {"executions": e0, "device_ms": d0},
+        "learned": {"executions": e1, "device_ms": d1},
+        "wall_ratio_ac1_over_learned": d0 / max(d1, 1e-9),
+        "bit_exact_nodes": same, "nodes": ntest,
+    }
+    print(json.dumps(out), flush=True)
+
+
 def run_uneven(args):
     """512 independent instances, propagators log-uniform in [1e3, 2e5]."""
     import pirgpu
@@ -471,9 +523,8 @@ def run_uneven(args):
     cpu = None
     if not args.no_cpu:
         from oracle import oracle as O
-        m = min(n, args.cpu_instances)
-        small = sorted(range(n), key=lambda j: insts[j].nprops)[:m]
-        sub = [insts[j] for j in small]
+        m = n
+        sub = insts
         po, vo, o2, x2, y2, z2, l2, u2 = W.pack(sub)
         s = np.ascontiguousarray(np.stack([l2, u2], 1))
         th = os.cpu_count() or 1
@@ -481,7 +532,7 @@ def run_uneven(args):
         O.fixpoint_instances(po, vo, o2, x2, y2, z2, s, threads=th)
         ct = time.perf_counter() - t0
         cpu = {"value": m / ct, "unit": "instances/s", "cores": th, "kind": "port",
-               "sample": "the %d smallest instances, %d host threads, %.1f s" % (m, th, ct)}
+               "sample": "all %d instances (install + Gauss-Seidel each), %d host threads, %.1f s" % (m, th, ct)}
     out = {
         "metric": "batched instances/sec", "value": n * args.steps / dev_s, "unit": "instances/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
@@ -557,6 +608,8 @@ def main():
     ap.add_argument("--seq-nodes", type=int, default=128, help="nodes timed in the sequential loop")
     ap.add_argument("--cpu-nodes", type=int, default=256)
     ap.add_argument("--cpu-instances", type=int, default=128)
+    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--wake-fraction", type=float, default=1 / 32)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")
@@ -566,6 +619,8 @@ def main():
         run_nodes(args)
     elif args.workload == "uneven":
         run_uneven(args)
+    elif args.workload == "learned":
+        run_learned(args)
     else:
         run_ours(args)
 

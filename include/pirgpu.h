@@ -176,8 +176,9 @@ int pir_fixpoint_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, cons
 /* Batched independent instances of uneven size, one launch: instance j owns
  * propagators prop_off[j] .. prop_off[j+1]-1 (var indices local to the
  * instance) and variables var_off[j] .. var_off[j+1]-1 of lb/ub, which are
- * updated in place.  Each instance is installed on the device (reified targets
- * met with [0, 1], pir.hpp:333-335) and run in the given propagator order.
+ * updated in place.  Each instance is installed: its propagators are grouped by
+ * opcode (stable, the GPU order of pir.hpp:339-341) and its reified targets
+ * met with [0, 1] on the device (pir.hpp:333-335).
  * out_status[j] a pir_status, out_rounds[j] (may be NULL) its rounds,
  * out_device_ms[j] (may be NULL) the device time of that instance's own
  * fixpoint (from the moment a CTA takes it up). */
@@ -207,6 +208,33 @@ int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int64_t *prop_o
 int pir_fixpoint_static(const int32_t *d_op, const int32_t *d_x, const int32_t *d_y,
                         const int32_t *d_z, int64_t n, int32_t *d_store, int32_t nvars,
                         const pir_opts *opts, pir_stats *stats, void *stream);
+
+/* Learned propagator scheduler (used by pir_fixpoint with opts.sched =
+ * PIR_SCHED_LEARNED; no counterpart in the reference, whose fixpoint loop is
+ * the caller's).  An 8 -> 32 -> 32 -> 1 MLP with BF16 weights scores every
+ * propagator each round; the top opts.wake_fraction of them run; a round of
+ * woken propagators without change is followed by a full certifying sweep,
+ * so the fixpoint is the plain one bit for bit.
+ *
+ * pir_sched_collect: change traces of the plain AC-1 fixpoint, node by node
+ * (each node = the context's store + its tightenings, as pir_fixpoint_nodes);
+ * every positive (a propagator that narrowed a bound in that round) and a
+ * keep_negative fraction of the negatives are kept, up to max_samples.  The
+ * context's store is left as it was. */
+int pir_sched_collect(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, const int32_t *var,
+                      const int32_t *lb, const int32_t *ub, int64_t max_samples,
+                      float keep_negative, int64_t *out_samples, int64_t *out_positives);
+/* Trains the scorer on the collected samples with the device kernels
+ * (weighted binary cross-entropy, Adam); out_loss[e] = mean loss of epoch e. */
+int pir_sched_train(pirgpu_ctx *ctx, int32_t epochs, int32_t batch, float lr, float pos_weight,
+                    float *out_loss);
+/* Loss and parameter gradient of the current BF16 weights on count samples
+ * (X: count x 8 features, Y: labels), for checking the training kernels. */
+int pir_sched_grad(pirgpu_ctx *ctx, int32_t count, const float *X, const float *Y, float pos_weight,
+                   float *grad_out, float *loss_out);
+/* Reads (set = 0) or writes (set = 1) the FP32 master parameters (count must
+ * be the parameter count, 1377: W1[32][8], b1[32], W2[32][32], b2[32], W3[32], b3). */
+int pir_sched_params(pirgpu_ctx *ctx, float *params, int32_t count, int32_t set);
 
 /* Number of SMs and the library's build string (for reports). */
 int pir_device_info(pirgpu_ctx *ctx, int32_t *num_sms, char *name, size_t name_len);

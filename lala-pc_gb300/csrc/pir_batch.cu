@@ -393,10 +393,16 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   const long long nchunks = coff[ninst];
   std::vector<int> hb((size_t)std::max<long long>(nchunks, 1) * 16);
   int *hop = hb.data(), *hx = hop + 4 * nchunks, *hy = hx + 4 * nchunks, *hz = hy + 4 * nchunks;
+  // Install order: each instance's propagators grouped by opcode with a
+  // stable counting sort (the order the reference's GPU path sorts by,
+  // pir.hpp:339-341), so that warps run one opcode at a time.
   for (int j = 0; j < ninst; ++j) {
     const long long p0 = prop_off[j], p1 = prop_off[j + 1], d0 = coff[j] * 4, d1 = coff[j + 1] * 4;
+    long long start[OP_COUNT + 1] = {0};
+    for (long long i = p0; i < p1; ++i) ++start[op[i] + 1];
+    for (int o = 0; o < OP_COUNT; ++o) start[o + 1] += start[o];
     for (long long i = p0; i < p1; ++i) {
-      const long long d = d0 + (i - p0);
+      const long long d = d0 + start[op[i]]++;
       hop[d] = op[i];
       hx[d] = x[i];
       hy[d] = y[i];

@@ -427,6 +427,7 @@ int pir_embed(pirgpu_ctx *ctx, int32_t var, int32_t lb, int32_t ub, int *changed
   if (var < 0 || var >= ctx->nvars) return set_err(ctx, PIR_EINVAL, "var %d out of range", var);
   CK(cudaSetDevice(ctx->device));
   std::vector<int> v{var}, l{lb}, u{ub};
+  note_embedded(ctx, &var, 1);
   return apply_meets(ctx, v, l, u, changed);
 }
 
@@ -439,6 +440,7 @@ int pir_embed_many(pirgpu_ctx *ctx, int32_t count, const int32_t *var, const int
     if (var[k] < 0 || var[k] >= ctx->nvars) return set_err(ctx, PIR_EINVAL, "var %d out of range", var[k]);
   CK(cudaSetDevice(ctx->device));
   std::vector<int> v(var, var + count), l(lb, lb + count), u(ub, ub + count);
+  note_embedded(ctx, var, count);
   return apply_meets(ctx, v, l, u, changed);
 }
 

@@ -1,13 +1,790 @@
-// Learned propagator scheduler.
+// Learned propagator scheduler for sm_103a.
+//
+// A small MLP (8 -> 32 -> 32 -> 1, BF16 weights, FP32 accumulation) scores
+// every propagator at the start of a round from eight features:
+//   0-2  opcode class one-hot: {ADD}, {MUL, TDIV, FDIV, CDIV, EDIV}, {MIN, MAX, EQ, LEQ}
+//   3-5  log2(width + 1) / 32 of x, y, z
+//   6    rounds since any of x, y, z last narrowed, clamped to 64, / 64
+//   7    log2(deg x + deg y + deg z) / 16 (static)
+// and the round runs only the top-scored propagators (a wake fraction of the
+// bytecode).  When a round of woken propagators changes nothing, one full AC-1
+// sweep certifies the fixpoint; if it changes anything, the learned rounds
+// resume.  Propagators are monotone, so any fair schedule that ends with a
+// no-change full sweep reaches the same fixpoint as the plain method: the
+// result is the AC-1 fixpoint bit for bit.
+//
+// Training data are change traces of the plain AC-1 fixpoint (features at the
+// start of a round, label = the propagator narrowed a bound in that round),
+// and the network is trained on the device by the kernels below (forward,
+// backward with a per-CTA reduction of the weight gradients, Adam).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <vector>
+
 #include "pir_engine.h"
 
 namespace pirgpu {
-struct SchedState {};
+
+// Parameter layout (floats): W1[32][8], b1[32], W2[32][32], b2[32], W3[32], b3.
+constexpr int NF = 8, NH = 32;
+constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH * NF, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH,
+              OFF_W3 = OFF_B2 + NH, OFF_B3 = OFF_W3 + NH, NPARAM = OFF_B3 + 1;
+constexpr int HIST_BINS = 2048;
+constexpr float HIST_LO = -16.f, HIST_HI = 16.f;
+constexpr int TRAIN_CTA = 128;
+
+struct SchedState {
+  int nvars = 0;
+  long long n = 0;
+  long long bc_version = -1;
+  float *d_param = nullptr, *d_m = nullptr, *d_v = nullptr, *d_grad = nullptr, *d_loss = nullptr;
+  __nv_bfloat16 *d_wbf = nullptr;
+  int adam_t = 0;
+  bool trained = false;
+  int *d_var_last = nullptr;  // round of the last narrowing of each variable
+  int *d_deg = nullptr;       // variable degree
+  unsigned char *d_pdeg = nullptr;  // per-propagator degree feature (x16 fixed point)
+  float *d_score = nullptr;
+  unsigned *d_hist = nullptr;  // 2 x HIST_BINS
+  unsigned long long *d_counts = nullptr;  // woken executions, samples
+  float *d_tx = nullptr, *d_ty = nullptr;  // trace samples
+  long long tcap = 0, tcount = 0;
+  std::vector<int> dirty;  // variables embedded since the last learned fixpoint
+};
+
 void destroy_sched_state(pirgpu_ctx *ctx) {
-  delete ctx->sched;
+  SchedState *s = ctx->sched;
+  if (!s) return;
+  void *ptrs[] = {s->d_param, s->d_m, s->d_v, s->d_grad, s->d_loss, s->d_wbf, s->d_var_last, s->d_deg,
+                  s->d_pdeg, s->d_score, s->d_hist, s->d_counts, s->d_tx, s->d_ty};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete s;
   ctx->sched = nullptr;
 }
-int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &, pir_stats *) {
-  return set_err(ctx, PIR_EINVAL, "learned schedule: not built");
+
+// --------------------------------------------------------------- device -----
+
+__device__ __forceinline__ float log2w(Itv a) {
+  if (a.l == MINF || a.u == INF) return 1.f;
+  const long long w = (long long)a.u - (long long)a.l;
+  return w <= 0 ? 0.f : __log2f((float)w + 1.f) * (1.f / 32.f);
 }
+
+__device__ __forceinline__ void features(int op, Itv a, Itv b, Itv c, int last, int round, unsigned char pdeg,
+                                         float f[NF]) {
+  const int cls = op == OP_ADD ? 0 : ((op >= OP_MUL && op <= OP_EDIV) ? 1 : 2);
+  f[0] = cls == 0;
+  f[1] = cls == 1;
+  f[2] = cls == 2;
+  f[3] = log2w(a);
+  f[4] = log2w(b);
+  f[5] = log2w(c);
+  f[6] = (float)min(max(round - last, 0), 64) * (1.f / 64.f);
+  f[7] = (float)pdeg * (1.f / 256.f);
+}
+
+// Weights staged in shared memory as FP32 (converted from BF16).
+__device__ __forceinline__ void stage_weights(const __nv_bfloat16 *wbf, float *sw) {
+  for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) sw[i] = __bfloat162float(wbf[i]);
+}
+
+__device__ __forceinline__ float mlp_forward(const float *sw, const float f[NF]) {
+  float h1[NH];
+#pragma unroll
+  for (int j = 0; j < NH; ++j) {
+    float a = sw[OFF_B1 + j];
+#pragma unroll
+    for (int i = 0; i < NF; ++i) a = fmaf(sw[OFF_W1 + j * NF + i], f[i], a);
+    h1[j] = fmaxf(a, 0.f);
+  }
+  float z = sw[OFF_B3];
+#pragma unroll 4
+  for (int j = 0; j < NH; ++j) {
+    float a = sw[OFF_B2 + j];
+#pragma unroll
+    for (int i = 0; i < NH; ++i) a = fmaf(sw[OFF_W2 + j * NH + i], h1[i], a);
+    z = fmaf(sw[OFF_W3 + j], fmaxf(a, 0.f), z);
+  }
+  return z;
+}
+
+__device__ __forceinline__ int hist_bin(float z) {
+  const float t = (fminf(fmaxf(z, HIST_LO), HIST_HI - 1e-3f) - HIST_LO) * ((float)HIST_BINS / (HIST_HI - HIST_LO));
+  return min(HIST_BINS - 1, max(0, (int)t));
+}
+
+// Joins into the HBM store that also stamp the variable's last-change round.
+struct StampStore {
+  int2 *s;
+  int *last;
+  int round;
+  __device__ __forceinline__ Itv load(int v) const {
+    const int2 t = __ldcg(s + v);
+    return mk(t.x, t.y);
+  }
+  __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
+    int n = 0;
+    if (r.l > seen.l) {
+      asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(&s[v].x), "r"(r.l) : "memory");
+      ++n;
+    }
+    if (r.u < seen.u) {
+      asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(&s[v].y), "r"(r.u) : "memory");
+      ++n;
+    }
+    if (n) {
+      last[v] = round;
+      if (is_bot(mk(max(seen.l, r.l), min(seen.u, r.u)))) failed = 1;
+    }
+    return n;
+  }
+};
+
+__device__ __forceinline__ int bc_get(const int *a, long long i) { return __ldg(a + i); }
+
+// Threshold bin of the top-k: the highest bin b such that the count of scores
+// in bins >= b reaches k.  Computed redundantly by every CTA from the global
+// histogram (2048 bins), in shared memory.
+__device__ int select_bin(const unsigned *hist, unsigned long long k, unsigned *sh) {
+  for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x) sh[i] = __ldcg(hist + i);
+  __syncthreads();
+  __shared__ int s_bin;
+  if (threadIdx.x == 0) {
+    unsigned long long acc = 0;
+    int b = HIST_BINS - 1;
+    for (; b > 0; --b) {
+      acc += sh[b];
+      if (acc >= k) break;
+    }
+    s_bin = b;
+  }
+  __syncthreads();
+  return s_bin;
+}
+
+struct LearnedArgs {
+  const int *op, *x, *y, *z;
+  long long n;
+  int2 *store;
+  int *var_last;
+  const unsigned char *pdeg;
+  const __nv_bfloat16 *wbf;
+  float *score;
+  unsigned *hist;  // 2 x HIST_BINS, zeroed
+  unsigned long long *counts;  // [0] woken executions
+  Control *ctl;
+  long long max_rounds;
+  long long timeout_ns;
+  unsigned long long k;  // woken per round
+};
+
+// Persistent learned fixpoint: per learned round, (A) score every propagator
+// and build the score histogram, grid barrier, (B) every CTA derives the top-k
+// threshold, (C) run the woken propagators, grid barrier with the change bit.
+// A learned round without change is followed by a certifying full sweep.
+__global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
+  __shared__ float sw[NPARAM];
+  __shared__ unsigned sh[HIST_BINS];
+  __shared__ unsigned s_word;
+  stage_weights(a.wbf, sw);
+  const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long gstride = (long long)gridDim.x * blockDim.x;
+  unsigned long long woken = 0, narrowed = 0;
+  long long round = 0;
+  bool certify = false;
+  int par = 0;
+  for (;;) {
+    ++round;
+    const int r = (int)round;
+    StampStore st{a.store, a.var_last, r};
+    int changed = 0, failed = 0;
+    if (!certify) {
+      // (A) scores and histogram
+      for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x) sh[i] = 0;
+      __syncthreads();
+      for (long long p = gtid; p < a.n; p += gstride) {
+        const int o = bc_get(a.op, p), X = bc_get(a.x, p), Y = bc_get(a.y, p), Z = bc_get(a.z, p);
+        const Itv ia = st.load(X), ib = st.load(Y), ic = st.load(Z);
+        const int last = max(__ldcg(a.var_last + X), max(__ldcg(a.var_last + Y), __ldcg(a.var_last + Z)));
+        float f[NF];
+        features(o, ia, ib, ic, last, r, a.pdeg[p], f);
+        const float s = mlp_forward(sw, f);
+        a.score[p] = s;
+        atomicAdd(&sh[hist_bin(s)], 1u);
+      }
+      __syncthreads();
+      unsigned *gh = a.hist + par * HIST_BINS;
+      for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x)
+        if (sh[i]) atomicAdd(gh + i, sh[i]);
+      __syncthreads();
+      if (threadIdx.x == 0) s_word = grid_sync_or(a.ctl, gridDim.x, 0, 0, a.timeout_ns);
+      __syncthreads();
+      if (s_word & BIT_ERROR) break;
+      // (B) threshold; CTA 0 clears the other histogram for the next round
+      const int bin = select_bin(gh, a.k, sh);
+      if (blockIdx.x == 0)
+        for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x) a.hist[(par ^ 1) * HIST_BINS + i] = 0;
+      // (C) woken propagators
+      for (long long p = gtid; p < a.n; p += gstride) {
+        if (hist_bin(__ldcg(a.score + p)) < bin) continue;
+        ++woken;
+        const int o = bc_get(a.op, p), X = bc_get(a.x, p), Y = bc_get(a.y, p), Z = bc_get(a.z, p);
+        const Itv ia = st.load(X), ib = st.load(Y), ic = st.load(Z);
+        changed += deduce_loaded(o, X, Y, Z, ia, ib, ic, st, failed);
+      }
+      par ^= 1;
+    } else {
+      // certifying full sweep
+      for (long long p = gtid; p < a.n; p += gstride) {
+        const int o = bc_get(a.op, p), X = bc_get(a.x, p), Y = bc_get(a.y, p), Z = bc_get(a.z, p);
+        const Itv ia = st.load(X), ib = st.load(Y), ic = st.load(Z);
+        changed += deduce_loaded(o, X, Y, Z, ia, ib, ic, st, failed);
+      }
+    }
+    narrowed += changed;
+    const int any_changed = __syncthreads_or(changed);
+    const int any_failed = __syncthreads_or(failed);
+    if (threadIdx.x == 0) s_word = grid_sync_or(a.ctl, gridDim.x, any_changed, any_failed, a.timeout_ns);
+    __syncthreads();
+    const unsigned w = s_word;
+    if (w & BIT_ERROR) break;
+    bool stop = false;
+    if (w & BIT_FAILED) {
+      stop = true;
+      if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->failed = 1;
+    } else if (certify) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.counts + 1, 1ull);
+      if (!(w & BIT_CHANGED)) stop = true;  // certified fixpoint
+      certify = false;
+    } else if (!(w & BIT_CHANGED)) {
+      certify = true;
+    }
+    if (!stop && a.max_rounds > 0 && round >= a.max_rounds) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->changed[0] = 1;
+      stop = true;
+    }
+    if (stop) break;
+    __syncthreads();
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->rounds = round;
+  woken = warp_sum64(woken);
+  narrowed = warp_sum64(narrowed);
+  if ((threadIdx.x & 31) == 0) {
+    if (woken) atomicAdd(a.counts, woken);
+    if (narrowed) atomicAdd(&a.ctl->narrowed, narrowed);
+  }
+}
+
+// One traced AC-1 round: features at the time each propagator is read, then
+// the propagator; label = it narrowed a bound.  Positives are always kept,
+// negatives with probability keep_neg (a hash of round and index).
+__global__ void __launch_bounds__(256) k_trace_round(const int *op, const int *x, const int *y, const int *z,
+                                                     long long n, int2 *store, int *var_last,
+                                                     const unsigned char *pdeg, int round, float keep_neg,
+                                                     unsigned seed, float *tx, float *ty, long long tcap,
+                                                     unsigned long long *tcount, Control *ctl) {
+  StampStore st{store, var_last, round};
+  int changed = 0, failed = 0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const int o = op[p], X = x[p], Y = y[p], Z = z[p];
+    const Itv ia = st.load(X), ib = st.load(Y), ic = st.load(Z);
+    const int last = max(__ldcg(var_last + X), max(__ldcg(var_last + Y), __ldcg(var_last + Z)));
+    float f[NF];
+    features(o, ia, ib, ic, last, round, pdeg[p], f);
+    const int ch = deduce_loaded(o, X, Y, Z, ia, ib, ic, st, failed);
+    changed += ch;
+    unsigned h = (unsigned)p * 0x9E3779B1u ^ ((unsigned)round * 0x85EBCA77u) ^ seed;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    const bool keep = ch > 0 || (float)(h & 0xFFFFFF) < keep_neg * 16777216.f;
+    if (keep) {
+      const unsigned long long slot = atomicAdd(tcount, 1ull);
+      if ((long long)slot < tcap) {
+#pragma unroll
+        for (int i = 0; i < NF; ++i) tx[slot * NF + i] = f[i];
+        ty[slot] = ch > 0 ? 1.f : 0.f;
+      }
+    }
+  }
+  const unsigned any_ch = __any_sync(0xFFFFFFFFu, changed), any_f = __any_sync(0xFFFFFFFFu, failed);
+  if ((threadIdx.x & 31) == 0) {
+    if (any_ch) atomicOr(&ctl->changed[0], 1);
+    if (any_f) atomicOr(&ctl->failed, 1);
+  }
+}
+
+// Weighted binary cross-entropy with logits: one sample per thread; weight
+// gradients reduced over the CTA in shared memory, then added to `grad`.
+__global__ void __launch_bounds__(TRAIN_CTA) k_mlp_grad(const float *X, const float *Y, const int *idx,
+                                                       long long count, const __nv_bfloat16 *wbf, float pos_weight,
+                                                       float inv_batch, float *grad, float *loss) {
+  extern __shared__ float smem[];
+  float *sw = smem;                                // NPARAM
+  float *H1 = sw + ((NPARAM + 31) / 32) * 32;      // TRAIN_CTA x (NH+1)
+  float *H2 = H1 + TRAIN_CTA * (NH + 1);
+  float *D2 = H2 + TRAIN_CTA * (NH + 1);           // dL/d(pre-activation 2)
+  float *D1 = D2 + TRAIN_CTA * (NH + 1);           // dL/d(pre-activation 1)
+  float *XS = D1 + TRAIN_CTA * (NH + 1);           // TRAIN_CTA x NF
+  float *DZ = XS + TRAIN_CTA * NF;                 // TRAIN_CTA
+  __shared__ float s_loss;
+  stage_weights(wbf, sw);
+  if (threadIdx.x == 0) s_loss = 0.f;
+  __syncthreads();
+  const int t = threadIdx.x;
+  const long long sidx = blockIdx.x * (long long)TRAIN_CTA + t;
+  float f[NF];
+  float yv = 0.f;
+  const bool valid = sidx < count;
+  if (valid) {
+    const long long s = idx ? idx[sidx] : sidx;
+#pragma unroll
+    for (int i = 0; i < NF; ++i) f[i] = X[s * NF + i];
+    yv = Y[s];
+  } else {
+#pragma unroll
+    for (int i = 0; i < NF; ++i) f[i] = 0.f;
+  }
+#pragma unroll
+  for (int i = 0; i < NF; ++i) XS[t * NF + i] = f[i];
+  float h1[NH], h2[NH];
+#pragma unroll
+  for (int j = 0; j < NH; ++j) {
+    float a = sw[OFF_B1 + j];
+#pragma unroll
+    for (int i = 0; i < NF; ++i) a = fmaf(sw[OFF_W1 + j * NF + i], f[i], a);
+    h1[j] = fmaxf(a, 0.f);
+    H1[t * (NH + 1) + j] = h1[j];
+  }
+  float z = sw[OFF_B3];
+#pragma unroll
+  for (int j = 0; j < NH; ++j) {
+    float a = sw[OFF_B2 + j];
+#pragma unroll
+    for (int i = 0; i < NH; ++i) a = fmaf(sw[OFF_W2 + j * NH + i], h1[i], a);
+    h2[j] = fmaxf(a, 0.f);
+    H2[t * (NH + 1) + j] = h2[j];
+    z = fmaf(sw[OFF_W3 + j], h2[j], z);
+  }
+  // loss = w * (softplus(z) - y z), dz = w * (sigmoid(z) - y) / batch
+  const float w = valid ? (yv > 0.5f ? pos_weight : 1.f) : 0.f;
+  const float sp = z > 0.f ? z + log1pf(__expf(-z)) : log1pf(__expf(z));
+  const float sig = 1.f / (1.f + __expf(-z));
+  const float dz = w * (sig - yv) * inv_batch;
+  DZ[t] = dz;
+  atomicAdd(&s_loss, w * (sp - yv * z));
+#pragma unroll
+  for (int j = 0; j < NH; ++j) D2[t * (NH + 1) + j] = h2[j] > 0.f ? dz * sw[OFF_W3 + j] : 0.f;
+#pragma unroll
+  for (int i = 0; i < NH; ++i) {
+    float a = 0.f;
+#pragma unroll
+    for (int j = 0; j < NH; ++j) a = fmaf(sw[OFF_W2 + j * NH + i], D2[t * (NH + 1) + j], a);
+    D1[t * (NH + 1) + i] = h1[i] > 0.f ? a : 0.f;
+  }
+  __syncthreads();
+  // weight gradients: reductions over the CTA's samples
+  for (int e = t; e < NPARAM; e += TRAIN_CTA) {
+    float g = 0.f;
+    if (e < OFF_B1) {
+      const int j = e / NF, i = e % NF;
+      for (int s = 0; s < TRAIN_CTA; ++s) g = fmaf(D1[s * (NH + 1) + j], XS[s * NF + i], g);
+    } else if (e < OFF_W2) {
+      const int j = e - OFF_B1;
+      for (int s = 0; s < TRAIN_CTA; ++s) g += D1[s * (NH + 1) + j];
+    } else if (e < OFF_B2) {
+      const int j = (e - OFF_W2) / NH, i = (e - OFF_W2) % NH;
+      for (int s = 0; s < TRAIN_CTA; ++s) g = fmaf(D2[s * (NH + 1) + j], H1[s * (NH + 1) + i], g);
+    } else if (e < OFF_W3) {
+      const int j = e - OFF_B2;
+      for (int s = 0; s < TRAIN_CTA; ++s) g += D2[s * (NH + 1) + j];
+    } else if (e < OFF_B3) {
+      const int j = e - OFF_W3;
+      for (int s = 0; s < TRAIN_CTA; ++s) g = fmaf(DZ[s], H2[s * (NH + 1) + j], g);
+    } else {
+      for (int s = 0; s < TRAIN_CTA; ++s) g += DZ[s];
+    }
+    atomicAdd(grad + e, g);
+  }
+  if (threadIdx.x == 0) atomicAdd(loss, s_loss);
+}
+
+// Adam on the FP32 master parameters; the BF16 copy is refreshed.
+__global__ void k_adam(float *param, float *grad, float *m, float *v, __nv_bfloat16 *wbf, float lr, float b1,
+                       float b2, float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NPARAM) return;
+  const float g = grad[i];
+  const float mi = b1 * m[i] + (1.f - b1) * g, vi = b2 * v[i] + (1.f - b2) * g * g;
+  m[i] = mi;
+  v[i] = vi;
+  const float p = param[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  param[i] = p;
+  wbf[i] = __float2bfloat16_rn(p);
+  grad[i] = 0.f;
+}
+
+__global__ void k_to_bf16(const float *param, __nv_bfloat16 *wbf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < NPARAM) wbf[i] = __float2bfloat16_rn(param[i]);
+}
+
+__global__ void k_degree(const int *x, const int *y, const int *z, long long n, int *deg) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    atomicAdd(deg + x[p], 1);
+    atomicAdd(deg + y[p], 1);
+    atomicAdd(deg + z[p], 1);
+  }
+}
+
+__global__ void k_prop_degree(const int *x, const int *y, const int *z, long long n, const int *deg,
+                              unsigned char *pdeg) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const float d = (float)(deg[x[p]] + deg[y[p]] + deg[z[p]]);
+    pdeg[p] = (unsigned char)min(255.f, __log2f(d + 1.f) * 16.f);
+  }
+}
+
+__global__ void k_fill_int(int *a, long long n, int v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+
+__global__ void k_mark(int *a, const int *idx, int count, int v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) a[idx[i]] = v;
+}
+
+// ------------------------------------------------------------------ host -----
+
+SchedState *sched(pirgpu_ctx *ctx) {
+  if (!ctx->sched) ctx->sched = new SchedState();
+  return ctx->sched;
+}
+
+// Parameters: allocated once per context, initialized with a fixed-seed
+// He-uniform draw.
+int ensure_params(pirgpu_ctx *ctx) {
+  SchedState *s = sched(ctx);
+  if (s->d_param) return PIR_OK;
+  const size_t b = NPARAM * sizeof(float);
+  if (cudaMalloc(&s->d_param, b) != cudaSuccess || cudaMalloc(&s->d_m, b) != cudaSuccess ||
+      cudaMalloc(&s->d_v, b) != cudaSuccess || cudaMalloc(&s->d_grad, b) != cudaSuccess ||
+      cudaMalloc(&s->d_loss, sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&s->d_wbf, NPARAM * sizeof(__nv_bfloat16)) != cudaSuccess ||
+      cudaMalloc(&s->d_hist, 2 * HIST_BINS * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&s->d_counts, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, PIR_ENOMEM, "scheduler parameters");
+  }
+  std::vector<float> p(NPARAM, 0.f);
+  std::mt19937 g(12345);
+  auto fill = [&](int off, int cnt, int fan_in) {
+    std::uniform_real_distribution<float> u(-std::sqrt(6.f / fan_in), std::sqrt(6.f / fan_in));
+    for (int i = 0; i < cnt; ++i) p[off + i] = u(g);
+  };
+  fill(OFF_W1, NH * NF, NF);
+  fill(OFF_W2, NH * NH, NH);
+  fill(OFF_W3, NH, NH);
+  PIR_CK(cudaMemcpyAsync(s->d_param, p.data(), b, cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaMemsetAsync(s->d_m, 0, b, ctx->stream));
+  PIR_CK(cudaMemsetAsync(s->d_v, 0, b, ctx->stream));
+  PIR_CK(cudaMemsetAsync(s->d_grad, 0, b, ctx->stream));
+  k_to_bf16<<<(NPARAM + 255) / 256, 256, 0, ctx->stream>>>(s->d_param, s->d_wbf);
+  PIR_CK(cudaGetLastError());
+  s->adam_t = 0;
+  return PIR_OK;
+}
+
+// Per-variable and per-propagator buffers for the current bytecode.
+int ensure_graph(pirgpu_ctx *ctx) {
+  SchedState *s = sched(ctx);
+  if (s->bc_version == ctx->bytecode_version && s->nvars == ctx->nvars && s->d_var_last) return PIR_OK;
+  void *ptrs[] = {s->d_var_last, s->d_deg, s->d_pdeg, s->d_score};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  s->d_var_last = s->d_deg = nullptr;
+  s->d_pdeg = nullptr;
+  s->d_score = nullptr;
+  const size_t nv = std::max(ctx->nvars, 1), n = (size_t)std::max<long long>(ctx->n, 1);
+  if (cudaMalloc(&s->d_var_last, nv * sizeof(int)) != cudaSuccess || cudaMalloc(&s->d_deg, nv * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->d_pdeg, n) != cudaSuccess || cudaMalloc(&s->d_score, n * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, PIR_ENOMEM, "scheduler buffers");
+  }
+  PIR_CK(cudaMemsetAsync(s->d_deg, 0, nv * sizeof(int), ctx->stream));
+  const int grid = ctx->num_sms * 4;
+  if (ctx->n > 0) {
+    k_degree<<<grid, 256, 0, ctx->stream>>>(ctx->d_x, ctx->d_y, ctx->d_z, ctx->n, s->d_deg);
+    k_prop_degree<<<grid, 256, 0, ctx->stream>>>(ctx->d_x, ctx->d_y, ctx->d_z, ctx->n, s->d_deg, s->d_pdeg);
+  }
+  PIR_CK(cudaGetLastError());
+  s->bc_version = ctx->bytecode_version;
+  s->nvars = ctx->nvars;
+  s->n = ctx->n;
+  return PIR_OK;
+}
+
+// Start-of-fixpoint stamps: every variable "long ago", the variables embedded
+// since the last fixpoint "just changed" (round 0).
+int reset_stamps(pirgpu_ctx *ctx) {
+  SchedState *s = sched(ctx);
+  k_fill_int<<<ctx->num_sms * 2, 256, 0, ctx->stream>>>(s->d_var_last, ctx->nvars, -64);
+  if (!s->dirty.empty()) {
+    const int cnt = (int)s->dirty.size();
+    int r;
+    if ((r = ensure(ctx, &ctx->d_scratch, &ctx->cap_scratch, cnt * sizeof(int)))) return r;
+    PIR_CK(cudaMemcpyAsync(ctx->d_scratch, s->dirty.data(), cnt * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    k_mark<<<(cnt + 255) / 256, 256, 0, ctx->stream>>>(s->d_var_last, (const int *)ctx->d_scratch, cnt, 0);
+    s->dirty.clear();
+  }
+  PIR_CK(cudaGetLastError());
+  return PIR_OK;
+}
+
+void note_embedded(pirgpu_ctx *ctx, const int32_t *var, int count) {
+  SchedState *s = sched(ctx);
+  if (s->dirty.size() > (size_t)1 << 22) return;
+  s->dirty.insert(s->dirty.end(), var, var + count);
+}
+
+int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
+  int r;
+  if ((r = ensure_params(ctx)) || (r = ensure_graph(ctx)) || (r = reset_stamps(ctx))) return r;
+  SchedState *s = sched(ctx);
+  if ((r = reset_control(ctx))) return r;
+  PIR_CK(cudaMemsetAsync(s->d_hist, 0, 2 * HIST_BINS * sizeof(unsigned), ctx->stream));
+  PIR_CK(cudaMemsetAsync(s->d_counts, 0, 4 * sizeof(unsigned long long), ctx->stream));
+  const float frac = opts.wake_fraction > 0.f ? std::min(opts.wake_fraction, 1.f) : 1.f / 16.f;
+  LearnedArgs a;
+  a.op = ctx->d_op;
+  a.x = ctx->d_x;
+  a.y = ctx->d_y;
+  a.z = ctx->d_z;
+  a.n = ctx->n;
+  a.store = ctx->d_store;
+  a.var_last = s->d_var_last;
+  a.pdeg = s->d_pdeg;
+  a.wbf = s->d_wbf;
+  a.score = s->d_score;
+  a.hist = s->d_hist;
+  a.counts = s->d_counts;
+  a.ctl = ctx->d_ctl;
+  a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
+  a.timeout_ns = opts.barrier_timeout_ns > 0 ? opts.barrier_timeout_ns : 2000000000ll;
+  a.k = (unsigned long long)std::max(1.0, std::ceil((double)frac * (double)ctx->n));
+  int occ = 0;
+  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fixpoint_learned, 256, 0));
+  if (occ < 1) return set_err(ctx, PIR_ECUDA, "learned kernel does not fit on an SM");
+  const int per_sm = opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ;
+  const int grid = std::max(1, (int)std::min<long long>((long long)ctx->num_sms * per_sm, (ctx->n + 255) / 256));
+  void *args[] = {&a};
+  PIR_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  PIR_CK(cudaLaunchCooperativeKernel((const void *)k_fixpoint_learned, dim3(grid), dim3(256), args, 0, ctx->stream));
+  PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  Control h;
+  unsigned long long cnt[4];
+  PIR_CK(cudaMemcpyAsync(cnt, s->d_counts, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+  if ((r = read_control(ctx, &h))) return r;
+  pir_stats st;
+  std::memset(&st, 0, sizeof(st));
+  PIR_CK(cudaEventElapsedTime(&st.device_ms, ctx->ev0, ctx->ev1));
+  // executions: woken propagators of the learned rounds + full certifying sweeps
+  st.rounds = h.rounds;
+  st.narrowed = (int64_t)h.narrowed;
+  st.executions = (int64_t)cnt[0] + (int64_t)cnt[1] * ctx->n;
+  int status = h.status ? h.status : (h.failed ? PIR_FAILED : (h.changed[0] ? PIR_TIMEOUT : PIR_OK));
+  st.status = status;
+  if (status == PIR_FAILED) ctx->failed = true;
+  if (stats) *stats = st;
+  return status;
+}
+
 }  // namespace pirgpu
+
+using namespace pirgpu;
+
+extern "C" int pir_sched_collect(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, const int32_t *var,
+                                 const int32_t *lb, const int32_t *ub, int64_t max_samples, float keep_negative,
+                                 int64_t *out_samples, int64_t *out_positives) {
+  if (!ctx || nnodes < 0 || max_samples <= 0 || (nnodes > 0 && (!off || !var || !lb || !ub)))
+    return PIR_EINVAL;
+  for (int j = 0; j < nnodes; ++j)
+    if (off[j + 1] < off[j]) return set_err(ctx, PIR_EINVAL, "node offsets decrease");
+  for (int k = 0; k < (nnodes ? off[nnodes] : 0); ++k)
+    if (var[k] < 0 || var[k] >= ctx->nvars) return set_err(ctx, PIR_EINVAL, "tightening var out of range");
+  if (ctx->n == 0 || ctx->failed) return set_err(ctx, PIR_EINVAL, "nothing to trace");
+  PIR_CK(cudaSetDevice(ctx->device));
+  int r;
+  if ((r = ensure_params(ctx)) || (r = ensure_graph(ctx))) return r;
+  SchedState *s = sched(ctx);
+  if (s->tcap < max_samples) {
+    if (s->d_tx) cudaFree(s->d_tx);
+    if (s->d_ty) cudaFree(s->d_ty);
+    s->d_tx = s->d_ty = nullptr;
+    if (cudaMalloc(&s->d_tx, (size_t)max_samples * NF * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&s->d_ty, (size_t)max_samples * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      s->tcap = 0;
+      return set_err(ctx, PIR_ENOMEM, "trace buffer");
+    }
+    s->tcap = max_samples;
+  }
+  // base store saved, restored before every node
+  int2 *base = nullptr;
+  const size_t sb = (size_t)ctx->nvars * sizeof(int2);
+  if (cudaMalloc(&base, sb) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, PIR_ENOMEM, "trace base store");
+  }
+  PIR_CK(cudaMemcpyAsync(base, ctx->d_store, sb, cudaMemcpyDeviceToDevice, ctx->stream));
+  PIR_CK(cudaMemsetAsync(s->d_counts, 0, 4 * sizeof(unsigned long long), ctx->stream));
+  const int grid = std::max(1, (int)std::min<long long>(ctx->num_sms * 8, (ctx->n + 255) / 256));
+  unsigned long long tcount = 0;
+  long long positives = 0;
+  for (int j = 0; j < nnodes && (long long)tcount < max_samples; ++j) {
+    PIR_CK(cudaMemcpyAsync(ctx->d_store, base, sb, cudaMemcpyDeviceToDevice, ctx->stream));
+    const int cnt = off[j + 1] - off[j];
+    std::vector<int> v(var + off[j], var + off[j + 1]), l(lb + off[j], lb + off[j + 1]), u(ub + off[j], ub + off[j + 1]);
+    ctx->failed = false;
+    if (cnt && (r = pir_embed_many(ctx, cnt, v.data(), l.data(), u.data(), nullptr))) break;
+    if ((r = reset_stamps(ctx))) break;
+    if (ctx->failed) continue;
+    for (int round = 1; round < 100000; ++round) {
+      if ((r = reset_control(ctx))) break;
+      k_trace_round<<<grid, 256, 0, ctx->stream>>>(ctx->d_op, ctx->d_x, ctx->d_y, ctx->d_z, ctx->n, ctx->d_store,
+                                                   s->d_var_last, s->d_pdeg, round, keep_negative,
+                                                   0x5EED0000u + (unsigned)j, s->d_tx, s->d_ty, s->tcap, s->d_counts,
+                                                   ctx->d_ctl);
+      PIR_CK(cudaGetLastError());
+      Control h;
+      if ((r = read_control(ctx, &h))) break;
+      if (h.failed || !h.changed[0]) break;
+    }
+    if (r) break;
+  }
+  PIR_CK(cudaMemcpyAsync(ctx->d_store, base, sb, cudaMemcpyDeviceToDevice, ctx->stream));
+  PIR_CK(cudaMemcpyAsync(&tcount, s->d_counts, sizeof(tcount), cudaMemcpyDeviceToHost, ctx->stream));
+  PIR_CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(base);
+  ctx->failed = false;
+  if (r) return r;
+  s->tcount = std::min<long long>((long long)tcount, s->tcap);
+  if (s->tcount > 0) {
+    std::vector<float> ys((size_t)s->tcount);
+    PIR_CK(cudaMemcpy(ys.data(), s->d_ty, ys.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (float y : ys) positives += y > 0.5f;
+  }
+  if (out_samples) *out_samples = s->tcount;
+  if (out_positives) *out_positives = positives;
+  return PIR_OK;
+}
+
+extern "C" int pir_sched_train(pirgpu_ctx *ctx, int32_t epochs, int32_t batch, float lr, float pos_weight,
+                               float *out_loss) {
+  if (!ctx || epochs < 0 || batch <= 0) return PIR_EINVAL;
+  PIR_CK(cudaSetDevice(ctx->device));
+  int r;
+  if ((r = ensure_params(ctx))) return r;
+  SchedState *s = sched(ctx);
+  if (s->tcount <= 0) return set_err(ctx, PIR_EINVAL, "no trace samples: call pir_sched_collect first");
+  const long long N = s->tcount;
+  batch = (int)std::min<long long>(((long long)batch + TRAIN_CTA - 1) / TRAIN_CTA * TRAIN_CTA, ((N + TRAIN_CTA - 1) / TRAIN_CTA) * TRAIN_CTA);
+  std::vector<int> perm((size_t)N);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::mt19937 g(777);
+  int *d_idx = nullptr;
+  if (cudaMalloc(&d_idx, (size_t)N * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, PIR_ENOMEM, "training index");
+  }
+  const size_t smem = (((NPARAM + 31) / 32) * 32 + 4 * TRAIN_CTA * (NH + 1) + TRAIN_CTA * NF + TRAIN_CTA) * sizeof(float);
+  r = PIR_OK;
+  if (cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    r = cuda_err(ctx, cudaGetLastError(), "k_mlp_grad smem");
+  for (int e = 0; e < epochs && !r; ++e) {
+    std::shuffle(perm.begin(), perm.end(), g);
+    if (cudaMemcpyAsync(d_idx, perm.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(s->d_loss, 0, sizeof(float), ctx->stream) != cudaSuccess) {
+      r = cuda_err(ctx, cudaGetLastError(), "training epoch setup");
+      break;
+    }
+    for (long long b0 = 0; b0 < N; b0 += batch) {
+      const long long cnt = std::min<long long>(batch, N - b0);
+      const int blocks = (int)((cnt + TRAIN_CTA - 1) / TRAIN_CTA);
+      k_mlp_grad<<<blocks, TRAIN_CTA, smem, ctx->stream>>>(s->d_tx, s->d_ty, d_idx + b0, cnt, s->d_wbf, pos_weight,
+                                                           1.f / (float)cnt, s->d_grad, s->d_loss);
+      ++s->adam_t;
+      const float b1 = 0.9f, b2 = 0.999f;
+      k_adam<<<(NPARAM + 255) / 256, 256, 0, ctx->stream>>>(s->d_param, s->d_grad, s->d_m, s->d_v, s->d_wbf, lr, b1, b2,
+                                                            1e-8f, 1.f - std::pow(b1, (float)s->adam_t),
+                                                            1.f - std::pow(b2, (float)s->adam_t));
+    }
+    if (cudaGetLastError() != cudaSuccess) {
+      r = set_err(ctx, PIR_ECUDA, "training kernels");
+      break;
+    }
+    float loss = 0.f;
+    if (cudaMemcpyAsync(&loss, s->d_loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+      r = cuda_err(ctx, cudaGetLastError(), "training loss");
+      break;
+    }
+    if (out_loss) out_loss[e] = loss / (float)N;
+  }
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(d_idx);
+  if (!r) s->trained = true;
+  return r;
+}
+
+extern "C" int pir_sched_grad(pirgpu_ctx *ctx, int32_t count, const float *X, const float *Y, float pos_weight,
+                              float *grad_out, float *loss_out) {
+  if (!ctx || count <= 0 || !X || !Y || !grad_out) return PIR_EINVAL;
+  PIR_CK(cudaSetDevice(ctx->device));
+  int r;
+  if ((r = ensure_params(ctx))) return r;
+  SchedState *s = sched(ctx);
+  const size_t bytes = (size_t)count * (NF + 1) * sizeof(float);
+  if ((r = ensure(ctx, &ctx->d_scratch, &ctx->cap_scratch, bytes))) return r;
+  float *dx = (float *)ctx->d_scratch, *dy = dx + (size_t)count * NF;
+  PIR_CK(cudaMemcpyAsync(dx, X, (size_t)count * NF * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaMemcpyAsync(dy, Y, (size_t)count * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaMemsetAsync(s->d_grad, 0, NPARAM * sizeof(float), ctx->stream));
+  PIR_CK(cudaMemsetAsync(s->d_loss, 0, sizeof(float), ctx->stream));
+  const size_t smem = (((NPARAM + 31) / 32) * 32 + 4 * TRAIN_CTA * (NH + 1) + TRAIN_CTA * NF + TRAIN_CTA) * sizeof(float);
+  PIR_CK(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_mlp_grad<<<(count + TRAIN_CTA - 1) / TRAIN_CTA, TRAIN_CTA, smem, ctx->stream>>>(
+      dx, dy, nullptr, count, s->d_wbf, pos_weight, 1.f / (float)count, s->d_grad, s->d_loss);
+  PIR_CK(cudaGetLastError());
+  PIR_CK(cudaMemcpyAsync(grad_out, s->d_grad, NPARAM * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  float loss = 0.f;
+  PIR_CK(cudaMemcpyAsync(&loss, s->d_loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  PIR_CK(cudaMemsetAsync(s->d_grad, 0, NPARAM * sizeof(float), ctx->stream));
+  PIR_CK(cudaStreamSynchronize(ctx->stream));
+  if (loss_out) *loss_out = loss / (float)count;
+  return PIR_OK;
+}
+
+extern "C" int pir_sched_params(pirgpu_ctx *ctx, float *params, int32_t count, int32_t set) {
+  if (!ctx || !params || count != NPARAM) return ctx ? set_err(ctx, PIR_EINVAL, "the scorer has %d parameters", NPARAM) : PIR_EINVAL;
+  PIR_CK(cudaSetDevice(ctx->device));
+  int r;
+  if ((r = ensure_params(ctx))) return r;
+  SchedState *s = sched(ctx);
+  if (set) {
+    PIR_CK(cudaMemcpyAsync(s->d_param, params, NPARAM * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    k_to_bf16<<<(NPARAM + 255) / 256, 256, 0, ctx->stream>>>(s->d_param, s->d_wbf);
+    PIR_CK(cudaGetLastError());
+  } else {
+    PIR_CK(cudaMemcpyAsync(params, s->d_param, NPARAM * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  PIR_CK(cudaStreamSynchronize(ctx->stream));
+  return PIR_OK;
+}

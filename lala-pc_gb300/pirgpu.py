@@ -92,6 +92,13 @@ SIGNATURES = [
                                               _I32P, _I32P, _I32P, _I32P, ctypes.POINTER(Opts),
                                               _I32P, _I32P, _F32P, ctypes.POINTER(Stats)]),
     ("pir_device_info", ctypes.c_int, [_P, _I32P, ctypes.c_char_p, ctypes.c_size_t]),
+    ("pir_sched_collect", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P, _I32P,
+                                         ctypes.c_int64, ctypes.c_float, _I64P, _I64P]),
+    ("pir_sched_train", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
+                                       ctypes.c_float, _F32P]),
+    ("pir_sched_grad", ctypes.c_int, [_P, ctypes.c_int32, _F32P, _F32P, ctypes.c_float, _F32P,
+                                      _F32P]),
+    ("pir_sched_params", ctypes.c_int, [_P, _F32P, ctypes.c_int32, ctypes.c_int32]),
     ("pir_fixpoint_static", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, _P, ctypes.c_int32,
                                            ctypes.POINTER(Opts), ctypes.POINTER(Stats), _P]),
 ]
@@ -323,6 +330,41 @@ class Context:
                                             ctypes.byref(s))
         self._check(rc)
         return status, rounds, ms, s.asdict()
+
+    # -- learned scheduler ---------------------------------------------
+    NPARAM = 1377
+
+    def sched_collect(self, off, var, lb, ub, max_samples=1_000_000, keep_negative=0.05):
+        off, var, lb, ub = map(_c32, (off, var, lb, ub))
+        ns, npos = ctypes.c_int64(0), ctypes.c_int64(0)
+        self._check(self._L.pir_sched_collect(self.h, len(off) - 1, _p32(off), _p32(var), _p32(lb),
+                                              _p32(ub), max_samples, keep_negative,
+                                              ctypes.byref(ns), ctypes.byref(npos)))
+        return ns.value, npos.value
+
+    def sched_train(self, epochs=8, batch=8192, lr=3e-3, pos_weight=1.0):
+        loss = np.zeros(max(epochs, 1), np.float32)
+        self._check(self._L.pir_sched_train(self.h, epochs, batch, lr, pos_weight,
+                                            loss.ctypes.data_as(_F32P)))
+        return loss[:epochs]
+
+    def sched_grad(self, X, Y, pos_weight=1.0):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.ascontiguousarray(Y, np.float32)
+        g = np.zeros(self.NPARAM, np.float32)
+        loss = ctypes.c_float(0)
+        self._check(self._L.pir_sched_grad(self.h, len(Y), X.ctypes.data_as(_F32P),
+                                           Y.ctypes.data_as(_F32P), pos_weight,
+                                           g.ctypes.data_as(_F32P), ctypes.byref(loss)))
+        return g, loss.value
+
+    def sched_params(self, params=None):
+        if params is None:
+            p = np.zeros(self.NPARAM, np.float32)
+            self._check(self._L.pir_sched_params(self.h, p.ctypes.data_as(_F32P), self.NPARAM, 0))
+            return p
+        p = np.ascontiguousarray(params, np.float32)
+        self._check(self._L.pir_sched_params(self.h, p.ctypes.data_as(_F32P), self.NPARAM, 1))
 
     def device_info(self):
         n = ctypes.c_int32()

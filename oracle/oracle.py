@@ -43,7 +43,7 @@ def lib():
                                          _I32P, _I32P, _I32P, _I32P, i64, i32, _I32P, _I32P,
                                          _I64P]
         L.orc_fixpoint_instances.argtypes = [i32, _I64P, _I64P, _I32P, _I32P, _I32P, _I32P,
-                                             _I32P, i64, i32, _I32P, _I64P]
+                                             _I32P, i64, i32, i32, _I32P, _I64P]
         for f in ("orc_check_exhaustive",):
             getattr(L, f).argtypes = [i32, i32, i32, i32, _I64P]
             getattr(L, f).restype = i64
@@ -134,8 +134,10 @@ def fixpoint_nodes(op, x, y, z, base_store, off, var, lb, ub, max_sweeps=1 << 40
     return out_status, out_store, out_stats
 
 
-def fixpoint_instances(prop_off, var_off, op, x, y, z, store, max_sweeps=1 << 40, threads=0):
-    """Independent instances packed back to back; `store` updated in place."""
+def fixpoint_instances(prop_off, var_off, op, x, y, z, store, max_sweeps=1 << 40, threads=0,
+                       install=True):
+    """Independent instances packed back to back; `store` updated in place.
+    With install=True each instance is installed (reified meets, CPU sort) first."""
     prop_off = np.ascontiguousarray(prop_off, np.int64)
     var_off = np.ascontiguousarray(var_off, np.int64)
     op, x, y, z = map(_c32, (op, x, y, z))
@@ -145,7 +147,7 @@ def fixpoint_instances(prop_off, var_off, op, x, y, z, store, max_sweeps=1 << 40
     out_stats = np.zeros((ninst, 4), np.int64)
     lib().orc_fixpoint_instances(ninst, _p64(prop_off), _p64(var_off), _p32(op), _p32(x),
                                  _p32(y), _p32(z), _p32(store), max_sweeps, threads,
-                                 _p32(out_status), _p64(out_stats))
+                                 int(install), _p32(out_status), _p64(out_stats))
     return out_status, out_stats
 
 

@@ -770,12 +770,32 @@ int orc_fixpoint_nodes(int32_t n, const int32_t *op, const int32_t *x, const int
 int orc_fixpoint_instances(int32_t ninst, const int64_t *prop_off, const int64_t *var_off,
                            const int32_t *op, const int32_t *x, const int32_t *y,
                            const int32_t *z, int32_t *store, int64_t max_sweeps,
-                           int32_t threads, int32_t *out_status, int64_t *out_stats) {
+                           int32_t threads, int32_t install, int32_t *out_status,
+                           int64_t *out_stats) {
   parallel_for(ninst, resolve_threads(threads), [&](i64 j) {
     i64 p0 = prop_off[j], p1 = prop_off[j + 1];
     i64 v0 = var_off[j], v1 = var_off[j + 1];
-    out_status[j] = gs_fixpoint((i32)(p1 - p0), op + p0, x + p0, y + p0, z + p0,
-                                (i32)(v1 - v0), store + 2 * v0, max_sweeps, out_stats + 4 * j);
+    const i32 n = (i32)(p1 - p0), nv = (i32)(v1 - v0);
+    i32 *s = store + 2 * v0;
+    if (!install) {
+      out_status[j] = gs_fixpoint(n, op + p0, x + p0, y + p0, z + p0, nv, s, max_sweeps, out_stats + 4 * j);
+      return;
+    }
+    // install (pir.hpp:326-352): reified meets and the CPU sort, then Gauss-Seidel
+    std::vector<i32> perm((size_t)n), o((size_t)n), a((size_t)n), b((size_t)n), c((size_t)n);
+    int st = orc_install(n, op + p0, x + p0, y + p0, z + p0, nv, s, perm.data());
+    if (st != ORC_OK) {
+      out_status[j] = st;
+      for (int k = 0; k < 4; ++k) out_stats[4 * j + k] = 0;
+      return;
+    }
+    for (i32 i = 0; i < n; ++i) {
+      o[i] = op[p0 + perm[i]];
+      a[i] = x[p0 + perm[i]];
+      b[i] = y[p0 + perm[i]];
+      c[i] = z[p0 + perm[i]];
+    }
+    out_status[j] = gs_fixpoint(n, o.data(), a.data(), b.data(), c.data(), nv, s, max_sweeps, out_stats + 4 * j);
   });
   return ORC_OK;
 }

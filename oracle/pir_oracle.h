@@ -68,7 +68,7 @@ int orc_fixpoint(int32_t n, const int32_t *op, const int32_t *x, const int32_t *
                  const int32_t *z, int32_t nvars, int32_t *store,
                  int64_t max_sweeps, int64_t *out);
 
-/* Same, executing only the first `n_exec` propagators of each sweep count —
+/* Exactly `sweeps` Gauss-Seidel sweeps in the given order (no stop test) —
  * used to time a bounded sample of sweeps. */
 int orc_sweeps(int32_t n, const int32_t *op, const int32_t *x, const int32_t *y,
                const int32_t *z, int32_t *store, int64_t sweeps, int64_t *out);
@@ -89,11 +89,13 @@ int orc_fixpoint_nodes(int32_t n, const int32_t *op, const int32_t *x, const int
 
 /* Batched independent instances: instance j owns bytecodes
  * prop_off[j]..prop_off[j+1]-1 (var indices local to the instance) and store
- * entries var_off[j]..var_off[j+1]-1 of `store` (updated in place). */
+ * entries var_off[j]..var_off[j+1]-1 of `store` (updated in place).  With
+ * install != 0 each instance is installed first (reified meets, CPU sort). */
 int orc_fixpoint_instances(int32_t ninst, const int64_t *prop_off, const int64_t *var_off,
                            const int32_t *op, const int32_t *x, const int32_t *y,
                            const int32_t *z, int32_t *store, int64_t max_sweeps,
-                           int32_t threads, int32_t *out_status, int64_t *out_stats);
+                           int32_t threads, int32_t install, int32_t *out_status,
+                           int64_t *out_stats);
 
 /* Exhaustive property checks restating tests/bound_consistency_test.hpp.
  * pred: 0 eq_reif, 1 le_reif, 2 plus, 3 min, 4 max, 5 times, 6 ediv, 7 tdiv,

@@ -36,7 +36,6 @@ def test_instances_parity(seed, P, oracle):
         s = inst.store()
         orc, info = oracle.install(inst.op, inst.x, inst.y, inst.z, s)
         if orc != oracle.FAILED:
-            # same propagator order as the GPU: the given one
             orc, info = oracle.fixpoint(inst.op, inst.x, inst.y, inst.z, s)
         assert status[j] == orc, j
         v0, v1 = var_off[j], var_off[j + 1]
