@@ -368,17 +368,20 @@ def run_nodes(args):
     cr.set_device(local)
     ctx, base, (blb, bub), off, var, lb, ub = _nodes_workload()
     nn = len(off) - 1
+    sched = pirgpu.SCHED_EVENTS if args.node_sched == "events" else pirgpu.SCHED_AC1
     for _ in range(args.warmup):
-        ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False)
+        ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=sched)
         cr.flush_l2()
     clk = ClockSampler(local)
     clk.start()
     runs = []
     for _ in range(args.steps):
-        status, _, _, rounds, st = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False)
+        status, _, _, rounds, st = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=sched)
         runs.append(st)
         cr.flush_l2()
     clocks = clk.stop()
+    # the batched AC-1 kernel, for reference
+    _, _, _, _, st_ac1 = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=pirgpu.SCHED_AC1)
     dev_s = sum(r["device_ms"] for r in runs) / 1e3
     value = nn * args.steps / dev_s
     execs = sum(r["executions"] for r in runs)
@@ -399,7 +402,7 @@ def run_nodes(args):
     seq_wall_rate = sample / seq_wall
     # end to end: host tightenings in, node stores out
     t0 = time.perf_counter()
-    status, olb, oub, rounds, st = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=True)
+    status, olb, oub, rounds2, st = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=True, sched=sched)
     e2e_t = time.perf_counter() - t0
     hbm, hbm_src = peaks()
     achieved = (execs * ALG_BYTES_PER_EXEC + joins * ALG_BYTES_PER_JOIN) / dev_s / 1e9
@@ -422,7 +425,9 @@ def run_nodes(args):
         "data": "synthetic: planted-solution base instance at its fixpoint, bisected nodes",
         "config": {"workload": "nodes: 100,000 vars / 400,000 propagators (bounds scale 1e6) at its fixpoint, 4,096 nodes, k ~ U[1,64] bisections of unfixed vars",
                    "nodes_ok": int((status == 0).sum()), "nodes_failed": int((status == 1).sum()),
-                   "max_rounds": int(rounds.max()), "mean_rounds": float(rounds.mean())},
+                   "max_rounds": int(rounds.max()), "mean_rounds": float(rounds.mean()),
+                   "schedule": args.node_sched, "executions_per_step": execs // args.steps,
+                   "batched_ac1_ms": st_ac1["device_ms"], "batched_ac1_executions": st_ac1["executions"]},
         "plain_sequential": {"nodes_per_s_device": seq_dev_rate, "nodes_per_s_wall": seq_wall_rate,
                              "sample_nodes": sample,
                              "batched_over_sequential_device": value / seq_dev_rate,
@@ -609,6 +614,7 @@ def main():
     ap.add_argument("--cpu-nodes", type=int, default=256)
     ap.add_argument("--cpu-instances", type=int, default=128)
     ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--node-sched", default="events", choices=["events", "ac1"])
     ap.add_argument("--wake-fraction", type=float, default=1 / 32)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

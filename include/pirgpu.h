@@ -57,7 +57,9 @@ enum pir_mode {
 /* Propagator schedules. */
 enum pir_sched {
   PIR_SCHED_AC1 = 0,      /* every propagator every round (plain AC-1 sweeps) */
-  PIR_SCHED_LEARNED = 1   /* wake set chosen by the trained scorer, certified by a full sweep */
+  PIR_SCHED_LEARNED = 1,  /* wake set chosen by the trained scorer, certified by a full sweep */
+  PIR_SCHED_EVENTS = 2    /* pir_fixpoint_nodes only, base store at its fixpoint: each round runs the
+                             propagators of the variables that changed in the previous round */
 };
 
 typedef struct pir_opts {

@@ -50,12 +50,21 @@ struct BatchState {
   size_t cap_nout = 0;
   int *d_nio = nullptr;  // per-node output staging
   size_t cap_nio = 0;
+  // event-driven nodes: AoS bytecode, variable -> propagator adjacency, per-CTA scratch
+  long long ev_version = -1;
+  int4 *d_bc4 = nullptr;
+  int *d_adj_ptr = nullptr, *d_adj = nullptr;
+  int ev_grid = 0, ev_nvars = 0;
+  long long ev_n = 0;
+  void *d_ev = nullptr;  // per-CTA scratch block
+  size_t cap_ev = 0;
 };
 
 void destroy_batch_state(pirgpu_ctx *ctx) {
   BatchState *b = ctx->batch;
   if (!b) return;
-  void *ptrs[] = {b->d_bc, b->d_off, b->d_store, b->d_aux, b->d_iout, b->d_nstore, b->d_tight, b->d_nout, b->d_nio};
+  void *ptrs[] = {b->d_bc, b->d_off,    b->d_store, b->d_aux,     b->d_iout, b->d_nstore, b->d_tight,
+                  b->d_nout, b->d_nio, b->d_bc4, b->d_adj_ptr, b->d_adj, b->d_ev};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete b;
@@ -318,6 +327,180 @@ __global__ void __launch_bounds__(512) k_nodes(NodeArgs a) {
   }
 }
 
+// ------------------------------------------------- event-driven nodes -----
+//
+// One CTA per node, nodes stolen from a counter.  The base store is a fixpoint
+// of the bytecode, so after the node's tightenings only propagators of a
+// variable that changed in the previous round can change anything: round r
+// runs exactly the propagators adjacent (variable -> propagator adjacency) to
+// the variables that narrowed in round r - 1 (first round: the tightened
+// variables).  A propagator none of whose variables changed since its last
+// run is at its fixpoint, so when a round leaves no variable changed the
+// store is the node's fixpoint, the one AC-1 rounds reach.
+//
+// Each CTA keeps one working store (equal to the base between nodes: after a
+// node only the variables it touched are put back), and dedups candidate
+// propagators and changed variables with epoch stamps (a per-CTA counter that
+// only grows, so the stamp arrays are never cleared).
+
+struct EvArgs {
+  const int4 *bc;  // (op, x, y, z) per propagator, engine order
+  long long n;
+  int nvars;
+  const int *adj_ptr, *adj;
+  const int2 *base;
+  int2 *out_store;  // node-major nnodes x nvars, or nullptr
+  const int *off, *var, *lb, *ub;
+  int nnodes;
+  int *next;
+  int2 *ws;          // grid x nvars
+  unsigned *vmark;   // grid x nvars: epoch a variable last entered a changed list
+  unsigned *tmark;   // grid x nvars: node tag a variable last entered the touched list
+  int *lists;        // grid x 3 x nvars: changed lists (2) and the touched list
+  unsigned *pstamp;  // grid x n: epoch a propagator last became a candidate
+  int *cand;         // grid x n
+  unsigned *epochs;  // grid
+  NodeOut *out;
+  unsigned long long *execs, *narrowed;
+  long long max_rounds;
+};
+
+struct EvStore {
+  int2 *ws;
+  unsigned *vmark, *tmark;
+  int *dnext, *touched;
+  int *nd, *nt;  // shared-memory counters
+  unsigned epoch, tag;
+  __device__ __forceinline__ Itv load(int v) const {
+    const int2 t = __ldcg(ws + v);
+    return mk(t.x, t.y);
+  }
+  __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
+    int n = 0;
+    if (r.l > seen.l) {
+      asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(&ws[v].x), "r"(r.l) : "memory");
+      ++n;
+    }
+    if (r.u < seen.u) {
+      asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(&ws[v].y), "r"(r.u) : "memory");
+      ++n;
+    }
+    if (n) {
+      if (atomicMax(vmark + v, epoch) < epoch) dnext[atomicAdd(nd, 1)] = v;
+      if (atomicExch(tmark + v, tag) != tag) touched[atomicAdd(nt, 1)] = v;
+      if (is_bot(mk(max(seen.l, r.l), min(seen.u, r.u)))) failed = 1;
+    }
+    return n;
+  }
+};
+
+__global__ void __launch_bounds__(512) k_nodes_events(EvArgs a) {
+  __shared__ int s_node, s_ncand, s_nd[2], s_nt;
+  const size_t nv = (size_t)a.nvars;
+  int2 *ws = a.ws + blockIdx.x * nv;
+  unsigned *vmark = a.vmark + blockIdx.x * nv, *tmark = a.tmark + blockIdx.x * nv;
+  int *dl[2] = {a.lists + blockIdx.x * 3 * nv, a.lists + blockIdx.x * 3 * nv + nv};
+  int *touched = a.lists + blockIdx.x * 3 * nv + 2 * nv;
+  unsigned *pstamp = a.pstamp + blockIdx.x * (size_t)a.n;
+  int *cand = a.cand + blockIdx.x * (size_t)a.n;
+  unsigned epoch = a.epochs[blockIdx.x];
+  for (size_t v = threadIdx.x; v < nv; v += blockDim.x) ws[v] = a.base[v];
+  unsigned long long execs = 0, narrowed = 0;
+  __syncthreads();
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_node = atomicAdd(a.next, 1);
+      s_nd[0] = s_nd[1] = 0;
+      s_nt = 0;
+    }
+    __syncthreads();
+    const int node = s_node;
+    if (node >= a.nnodes) break;
+    ++epoch;
+    const unsigned tag = epoch;
+    // tightenings: meets, the changed ones start the first changed list
+    int f = 0;
+    const int k0 = a.off[node], k1 = a.off[node + 1];
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+      const int v = a.var[k];
+      const int ol = atomicMax(&ws[v].x, a.lb[k]), ou = atomicMin(&ws[v].y, a.ub[k]);
+      if (ol < a.lb[k] || ou > a.ub[k]) {
+        if (atomicMax(vmark + v, epoch) < epoch) dl[0][atomicAdd(&s_nd[0], 1)] = v;
+        if (atomicExch(tmark + v, tag) != tag) touched[atomicAdd(&s_nt, 1)] = v;
+      }
+    }
+    __syncthreads();
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+      const int2 t = __ldcg(ws + a.var[k]);
+      f |= is_bot(mk(t.x, t.y));
+    }
+    int failed = __syncthreads_or(f);
+    int cur = 0;
+    long long round = 0;
+    int status = PIR_OK;
+    while (!failed) {
+      if (s_nd[cur] == 0) break;
+      if (a.max_rounds > 0 && round >= a.max_rounds) {
+        status = PIR_TIMEOUT;
+        break;
+      }
+      ++round;
+      ++epoch;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        s_ncand = 0;
+        s_nd[cur ^ 1] = 0;
+      }
+      __syncthreads();
+      // candidates: propagators adjacent to the variables changed last round
+      const int nd = s_nd[cur];
+      for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+        const int v = dl[cur][i];
+        for (int q = __ldg(a.adj_ptr + v), qe = __ldg(a.adj_ptr + v + 1); q < qe; ++q) {
+          const int p = __ldg(a.adj + q);
+          if (atomicMax(pstamp + p, epoch) < epoch) cand[atomicAdd(&s_ncand, 1)] = p;
+        }
+      }
+      __syncthreads();
+      EvStore st{ws, vmark, tmark, dl[cur ^ 1], touched, &s_nd[cur ^ 1], &s_nt, epoch, tag};
+      const int nc = s_ncand;
+      int f2 = 0;
+      for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+        const int4 b = __ldg(a.bc + cand[i]);
+        const Itv ia = st.load(b.y), ib = st.load(b.z), ic = st.load(b.w);
+        narrowed += deduce_loaded(b.x, b.y, b.z, b.w, ia, ib, ic, st, f2);
+        ++execs;
+      }
+      failed = __syncthreads_or(f2);
+      cur ^= 1;
+    }
+    if (failed) status = PIR_FAILED;
+    if (threadIdx.x == 0) {
+      a.out[node].status = status;
+      a.out[node].rounds = (int)round;
+    }
+    if (a.out_store) {
+      int2 *dst = a.out_store + (size_t)node * nv;
+      for (size_t v = threadIdx.x; v < nv; v += blockDim.x) dst[v] = __ldcg(ws + v);
+    }
+    __syncthreads();
+    // put the touched variables back to the base store
+    const int nt = s_nt;
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+      const int v = touched[i];
+      ws[v] = a.base[v];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) a.epochs[blockIdx.x] = epoch;
+  execs = warp_sum64(execs);
+  narrowed = warp_sum64(narrowed);
+  if ((threadIdx.x & 31) == 0) {
+    if (execs) atomicAdd(a.execs, execs);
+    if (narrowed) atomicAdd(a.narrowed, narrowed);
+  }
+}
+
 // Node-major output: out[node][v] = group store[v][lane].
 __global__ void k_nodes_unpack(const int2 *nstore, int nvars, int nnodes, int *out_lb, int *out_ub) {
   const long long total = (long long)nnodes * nvars;
@@ -346,6 +529,170 @@ __global__ void k_unpack_int2(const int2 *in, long long n, int *lb, int *ub) {
 BatchState *batch(pirgpu_ctx *ctx) {
   if (!ctx->batch) ctx->batch = new BatchState();
   return ctx->batch;
+}
+
+// AoS bytecode and the variable -> propagator adjacency of the context's
+// bytecode (engine order), rebuilt when the bytecode changes.
+int ensure_events_graph(pirgpu_ctx *ctx, BatchState *b) {
+  if (b->ev_version == ctx->bytecode_version && b->d_bc4) return PIR_OK;
+  const long long n = ctx->n;
+  const int nv = ctx->nvars;
+  std::vector<int4> bc4((size_t)n);
+  std::vector<int> ptr((size_t)nv + 1, 0), adj((size_t)n * 3);
+  for (long long p = 0; p < n; ++p) {
+    bc4[p] = make_int4(ctx->h_op[p], ctx->h_x[p], ctx->h_y[p], ctx->h_z[p]);
+    ++ptr[ctx->h_x[p] + 1];
+    ++ptr[ctx->h_y[p] + 1];
+    ++ptr[ctx->h_z[p] + 1];
+  }
+  for (int v = 0; v < nv; ++v) ptr[v + 1] += ptr[v];
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (long long p = 0; p < n; ++p) {
+    adj[fill[ctx->h_x[p]]++] = (int)p;
+    adj[fill[ctx->h_y[p]]++] = (int)p;
+    adj[fill[ctx->h_z[p]]++] = (int)p;
+  }
+  void *ptrs[] = {b->d_bc4, b->d_adj_ptr, b->d_adj};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+  b->d_bc4 = nullptr;
+  b->d_adj_ptr = b->d_adj = nullptr;
+  if (cudaMalloc(&b->d_bc4, std::max<size_t>(1, (size_t)n) * sizeof(int4)) != cudaSuccess ||
+      cudaMalloc(&b->d_adj_ptr, ((size_t)nv + 1) * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&b->d_adj, std::max<size_t>(1, (size_t)n * 3) * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, PIR_ENOMEM, "event graph");
+  }
+  PIR_CK(cudaMemcpyAsync(b->d_bc4, bc4.data(), (size_t)n * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaMemcpyAsync(b->d_adj_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaMemcpyAsync(b->d_adj, adj.data(), adj.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaStreamSynchronize(ctx->stream));
+  b->ev_version = ctx->bytecode_version;
+  return PIR_OK;
+}
+
+int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const int32_t *off, const int32_t *var,
+                          const int32_t *lb, const int32_t *ub, const pir_opts &opts, int32_t *out_lb,
+                          int32_t *out_ub, int32_t *out_status, int32_t *out_rounds, pir_stats *stats) {
+  int r;
+  if ((r = ensure_events_graph(ctx, b))) return r;
+  const int block = 512;
+  int occ = 0;
+  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nodes_events, block, 0));
+  occ = std::max(occ, 1);
+  const int grid = std::max(1, std::min(nnodes, ctx->num_sms * (opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ)));
+  const size_t nv = (size_t)ctx->nvars, n = (size_t)std::max<long long>(ctx->n, 1);
+  // per-CTA scratch: ws | vmark | tmark | lists(3) | pstamp | cand | epochs
+  const size_t per_cta = nv * 8 + nv * 4 * 2 + nv * 4 * 3 + n * 4 * 2;
+  const size_t need = per_cta * (size_t)grid + 64 * (size_t)grid + 256;
+  if (b->cap_ev < need || b->ev_grid != grid || b->ev_nvars != ctx->nvars || b->ev_n != ctx->n) {
+    if (b->d_ev) cudaFree(b->d_ev);
+    b->d_ev = nullptr;
+    b->cap_ev = 0;
+    if (cudaMalloc(&b->d_ev, need) != cudaSuccess) {
+      cudaGetLastError();
+      return set_err(ctx, PIR_ENOMEM, "event scratch (%zu bytes)", need);
+    }
+    b->cap_ev = need;
+    b->ev_grid = grid;
+    b->ev_nvars = ctx->nvars;
+    b->ev_n = ctx->n;
+    PIR_CK(cudaMemsetAsync(b->d_ev, 0, need, ctx->stream));  // stamps and epochs start at 0
+  }
+  char *base = (char *)b->d_ev;
+  EvArgs a;
+  a.bc = b->d_bc4;
+  a.n = ctx->n;
+  a.nvars = ctx->nvars;
+  a.adj_ptr = b->d_adj_ptr;
+  a.adj = b->d_adj;
+  a.base = ctx->d_store;
+  a.ws = (int2 *)base;
+  base += (size_t)grid * nv * 8;
+  a.vmark = (unsigned *)base;
+  base += (size_t)grid * nv * 4;
+  a.tmark = (unsigned *)base;
+  base += (size_t)grid * nv * 4;
+  a.lists = (int *)base;
+  base += (size_t)grid * nv * 12;
+  a.pstamp = (unsigned *)base;
+  base += (size_t)grid * n * 4;
+  a.cand = (int *)base;
+  base += (size_t)grid * n * 4;
+  a.epochs = (unsigned *)base;
+  // tightenings, counters, outputs
+  const int ntight = off[nnodes];
+  if ((r = ensure(ctx, (void **)&b->d_tight, &b->cap_tight, ((size_t)nnodes + 1 + 3 * (size_t)ntight + 8) * sizeof(int))))
+    return r;
+  if ((r = ensure(ctx, (void **)&b->d_nout, &b->cap_nout, (size_t)nnodes * sizeof(NodeOut) + 64))) return r;
+  int *d_off = b->d_tight, *d_var = d_off + nnodes + 1, *d_lb = d_var + ntight, *d_ub = d_lb + ntight;
+  int *d_next = d_ub + ntight;
+  unsigned long long *d_cnt =
+      reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(b->d_nout) + (size_t)nnodes * sizeof(NodeOut));
+  PIR_CK(cudaMemcpyAsync(d_off, off, (nnodes + 1) * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  if (ntight) {
+    PIR_CK(cudaMemcpyAsync(d_var, var, ntight * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    PIR_CK(cudaMemcpyAsync(d_lb, lb, ntight * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    PIR_CK(cudaMemcpyAsync(d_ub, ub, ntight * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  PIR_CK(cudaMemsetAsync(d_next, 0, 4 * sizeof(int), ctx->stream));
+  PIR_CK(cudaMemsetAsync(d_cnt, 0, 2 * sizeof(unsigned long long), ctx->stream));
+  int2 *d_out_store = nullptr;
+  if (out_lb) {
+    if ((r = ensure(ctx, (void **)&b->d_nstore, &b->cap_nstore, (size_t)nnodes * nv * sizeof(int2)))) return r;
+    d_out_store = b->d_nstore;
+  }
+  a.out_store = d_out_store;
+  a.off = d_off;
+  a.var = d_var;
+  a.lb = d_lb;
+  a.ub = d_ub;
+  a.nnodes = nnodes;
+  a.next = d_next;
+  a.out = b->d_nout;
+  a.execs = d_cnt;
+  a.narrowed = d_cnt + 1;
+  a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
+  PIR_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  k_nodes_events<<<grid, block, 0, ctx->stream>>>(a);
+  PIR_CK(cudaGetLastError());
+  PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  std::vector<NodeOut> hout(nnodes);
+  unsigned long long hcnt[2] = {0, 0};
+  PIR_CK(cudaMemcpyAsync(hout.data(), b->d_nout, nnodes * sizeof(NodeOut), cudaMemcpyDeviceToHost, ctx->stream));
+  PIR_CK(cudaMemcpyAsync(hcnt, d_cnt, sizeof(hcnt), cudaMemcpyDeviceToHost, ctx->stream));
+  if (out_lb) {
+    int per = (int)std::min<long long>(nnodes, (256ll << 20) / std::max<long long>(8ll * ctx->nvars, 1));
+    per = std::max(per, 1);
+    if ((r = ensure(ctx, (void **)&b->d_nio, &b->cap_nio, (size_t)per * nv * 2 * sizeof(int)))) return r;
+    for (int j0 = 0; j0 < nnodes; j0 += per) {
+      const int cnt = std::min(per, nnodes - j0);
+      const long long items = (long long)cnt * (long long)nv;
+      k_unpack_int2<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(b->d_nstore + (size_t)j0 * nv, items, b->d_nio,
+                                                              b->d_nio + (size_t)cnt * nv);
+      PIR_CK(cudaGetLastError());
+      PIR_CK(cudaMemcpyAsync(out_lb + (size_t)j0 * nv, b->d_nio, (size_t)items * sizeof(int), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+      PIR_CK(cudaMemcpyAsync(out_ub + (size_t)j0 * nv, b->d_nio + (size_t)cnt * nv, (size_t)items * sizeof(int),
+                             cudaMemcpyDeviceToHost, ctx->stream));
+    }
+  }
+  PIR_CK(cudaStreamSynchronize(ctx->stream));
+  pir_stats st;
+  std::memset(&st, 0, sizeof(st));
+  PIR_CK(cudaEventElapsedTime(&st.device_ms, ctx->ev0, ctx->ev1));
+  int worst = PIR_OK;
+  for (int j = 0; j < nnodes; ++j) {
+    out_status[j] = hout[j].status;
+    if (out_rounds) out_rounds[j] = hout[j].rounds;
+    st.rounds = std::max<int64_t>(st.rounds, hout[j].rounds);
+    if (hout[j].status == PIR_TIMEOUT) worst = PIR_TIMEOUT;
+  }
+  st.executions = (int64_t)hcnt[0];
+  st.narrowed = (int64_t)hcnt[1];
+  st.status = worst;
+  if (stats) *stats = st;
+  return PIR_OK;
 }
 
 }  // namespace pirgpu
@@ -541,6 +888,9 @@ extern "C" int pir_fixpoint_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t
     return PIR_OK;
   }
   BatchState *b = batch(ctx);
+  if (opts.sched == PIR_SCHED_EVENTS && ctx->at_fixpoint)
+    return fixpoint_nodes_events(ctx, b, nnodes, off, var, lb, ub, opts, out_lb, out_ub, out_status, out_rounds,
+                                 stats);
   const int ngroups = (nnodes + 31) / 32;
   const size_t group_bytes = (size_t)ctx->nvars * 32 * sizeof(int2);
   int r;

@@ -321,6 +321,7 @@ int apply_meets(pirgpu_ctx *ctx, const std::vector<int> &var, const std::vector<
   Control h;
   if ((r = read_control(ctx, &h))) return r;
   if (h.failed) ctx->failed = true;
+  if (h.changed[0]) ctx->at_fixpoint = false;
   if (changed) *changed = h.changed[0];
   return PIR_OK;
 }
@@ -383,6 +384,7 @@ int pir_load_store(pirgpu_ctx *ctx, int32_t nvars, const int32_t *lb, const int3
   if ((r = ensure(ctx, (void **)&ctx->d_io, &ctx->cap_io, (size_t)nvars * 2 * sizeof(int)))) return r;
   ctx->nvars = nvars;
   ctx->failed = false;
+  ctx->at_fixpoint = false;
   if (nvars == 0) return PIR_OK;
   if ((r = reset_control(ctx))) return r;
   CK(cudaMemcpyAsync(ctx->d_io, lb, (size_t)nvars * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
@@ -501,6 +503,7 @@ int pir_tell(pirgpu_ctx *ctx, int32_t n, const int32_t *op, const int32_t *x, co
   ctx->n = (long long)tot;
   ctx->max_var_used = maxv;
   ctx->bytecode_version++;
+  ctx->at_fixpoint = false;
   if ((r = upload_bytecode(ctx))) return r;
   if (changed) *changed = 1;
   return PIR_OK;
@@ -616,6 +619,7 @@ int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
   else if (mode == PIR_MODE_HOSTLOOP ? (h.changed[(rounds - 1) & 1] != 0) : (h.changed[0] != 0)) status = PIR_TIMEOUT;
   else status = PIR_OK;
   if (status == PIR_FAILED) ctx->failed = true;
+  ctx->at_fixpoint = status == PIR_OK;
   st.status = status;
   ctx->last_mode = mode;
   if (stats) *stats = st;
@@ -637,7 +641,7 @@ int pir_autotune(pirgpu_ctx *ctx, int32_t rounds, int32_t *out_variant, float *o
   }
   const size_t bytes = (size_t)ctx->nvars * sizeof(int2);
   CK(cudaMemcpyAsync(saved, ctx->d_store, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-  const bool failed0 = ctx->failed;
+  const bool failed0 = ctx->failed, fix0 = ctx->at_fixpoint;
   int best = -1;
   float best_us = 0.f;
   int rc = PIR_OK;
@@ -672,6 +676,7 @@ int pir_autotune(pirgpu_ctx *ctx, int32_t rounds, int32_t *out_variant, float *o
   cudaStreamSynchronize(ctx->stream);
   cudaFree(saved);
   ctx->failed = failed0;
+  ctx->at_fixpoint = fix0;
   if (rc != PIR_OK) return rc;
   ctx->tuned_variant = best;
   ctx->tuned_version = ctx->bytecode_version;
@@ -691,6 +696,7 @@ int pir_deduce_one(pirgpu_ctx *ctx, int64_t i, int *changed) {
   Control h;
   if ((r = read_control(ctx, &h))) return r;
   if (h.failed) ctx->failed = true;
+  if (h.changed[0]) ctx->at_fixpoint = false;
   if (changed) *changed = h.changed[0];
   return PIR_OK;
 }
@@ -785,6 +791,7 @@ struct pirgpu_snapshot {
   long long n;
   int nvars;
   bool failed;
+  bool at_fixpoint;
   int2 *d_store;
 };
 
@@ -796,6 +803,7 @@ int pir_snapshot(pirgpu_ctx *ctx, pirgpu_snapshot **out) {
   s->n = ctx->n;
   s->nvars = ctx->nvars;
   s->failed = ctx->failed;
+  s->at_fixpoint = ctx->at_fixpoint;
   s->d_store = nullptr;
   if (ctx->nvars > 0) {
     if (cudaMalloc(&s->d_store, (size_t)ctx->nvars * sizeof(int2)) != cudaSuccess) {
@@ -832,6 +840,7 @@ int pir_restore(pirgpu_ctx *ctx, const pirgpu_snapshot *snap) {
   }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->failed = snap->failed;
+  ctx->at_fixpoint = snap->at_fixpoint && snap->n == ctx->n;
   return PIR_OK;
 }
 

@@ -29,6 +29,7 @@ struct pirgpu_ctx {
   int *d_io = nullptr;  // 2 * nvars int32 staging for pack / unpack
   size_t cap_io = 0;
   bool failed = false;  // is_bot()
+  bool at_fixpoint = false;  // the store is a fixpoint of the bytecode (last pir_fixpoint returned OK)
 
   // Bytecode in engine order (sorted by op, y, x, z), host copy and device SoA.
   long long n = 0;

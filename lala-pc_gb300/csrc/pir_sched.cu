@@ -602,6 +602,7 @@ int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   int status = h.status ? h.status : (h.failed ? PIR_FAILED : (h.changed[0] ? PIR_TIMEOUT : PIR_OK));
   st.status = status;
   if (status == PIR_FAILED) ctx->failed = true;
+  ctx->at_fixpoint = status == PIR_OK;
   if (stats) *stats = st;
   return status;
 }
@@ -644,6 +645,7 @@ extern "C" int pir_sched_collect(pirgpu_ctx *ctx, int32_t nnodes, const int32_t 
     return set_err(ctx, PIR_ENOMEM, "trace base store");
   }
   PIR_CK(cudaMemcpyAsync(base, ctx->d_store, sb, cudaMemcpyDeviceToDevice, ctx->stream));
+  const bool fix0 = ctx->at_fixpoint;
   PIR_CK(cudaMemsetAsync(s->d_counts, 0, 4 * sizeof(unsigned long long), ctx->stream));
   const int grid = std::max(1, (int)std::min<long long>(ctx->num_sms * 8, (ctx->n + 255) / 256));
   unsigned long long tcount = 0;
@@ -674,6 +676,7 @@ extern "C" int pir_sched_collect(pirgpu_ctx *ctx, int32_t nnodes, const int32_t 
   PIR_CK(cudaStreamSynchronize(ctx->stream));
   cudaFree(base);
   ctx->failed = false;
+  ctx->at_fixpoint = fix0;
   if (r) return r;
   s->tcount = std::min<long long>((long long)tcount, s->tcap);
   if (s->tcount > 0) {

@@ -18,7 +18,7 @@ ADD, MUL, TDIV, FDIV, CDIV, EDIV, MIN, MAX, EQ, LEQ = range(10)
 OK, FAILED, TIMEOUT, BARRIER_TIMEOUT, EINVAL, ECUDA, ENOMEM = range(7)
 STATUS = ["OK", "FAILED", "TIMEOUT", "BARRIER_TIMEOUT", "EINVAL", "ECUDA", "ENOMEM"]
 MODE_AUTO, MODE_PERSISTENT, MODE_HOSTLOOP, MODE_SMEM = range(4)
-SCHED_AC1, SCHED_LEARNED = range(2)
+SCHED_AC1, SCHED_LEARNED, SCHED_EVENTS = range(3)
 INF = 2**31 - 1
 MINF = -2**31
 

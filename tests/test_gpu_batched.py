@@ -117,3 +117,44 @@ def test_nodes_partial_group_and_cap(P, oracle):
     np.testing.assert_array_equal(olb[ok], ostore[ok, :, 0])
     capped, _, _, r2, _ = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, max_rounds=1)
     assert np.all((capped != P.OK) | (r2 <= 1))
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_nodes_events_parity(seed, P, oracle):
+    """Event-driven nodes (base at its fixpoint): same statuses and stores as
+    the oracle's Gauss-Seidel per node."""
+    ctx, (blb, bub), off, var, lb, ub = _nodes_setup(P, seed=seed)
+    status, olb, oub, rounds, st = ctx.fixpoint_nodes(off, var, lb, ub, sched=P.SCHED_EVENTS)
+    op, x, y, z = ctx.bytecode()
+    base = np.ascontiguousarray(np.stack([blb, bub], 1))
+    ostatus, ostore, ostats = oracle.fixpoint_nodes(op, x, y, z, base, off, var, lb, ub)
+    np.testing.assert_array_equal(status, ostatus)
+    ok = ostatus == oracle.OK
+    assert ok.sum() > 0 and (~ok).sum() > 0
+    np.testing.assert_array_equal(olb[ok], ostore[ok, :, 0])
+    np.testing.assert_array_equal(oub[ok], ostore[ok, :, 1])
+    # far fewer executions than AC-1 rounds over the whole bytecode
+    assert st["executions"] < 0.5 * (ostats[:, 1].sum())
+    # a second launch reuses the scratch (stamps, working stores) correctly
+    s2, l2, u2, _, _ = ctx.fixpoint_nodes(off, var, lb, ub, sched=P.SCHED_EVENTS)
+    np.testing.assert_array_equal(s2, status)
+    np.testing.assert_array_equal(l2[ok], olb[ok])
+
+
+def test_nodes_events_need_a_fixpoint_base(P, oracle):
+    """When the base store is not a fixpoint the event schedule is not exact;
+    the call then runs AC-1 rounds and still matches the oracle."""
+    import workloads as W
+    base = W.plain(5000, 20_000, 10**6, 7)
+    ctx = P.Context(0)
+    ctx.load_store(base.lb, base.ub)
+    ctx.tell(base.op, base.x, base.y, base.z)
+    blb, bub = ctx.read_store()
+    _, off, var, lb, ub = W.nodes(5000, 20_000, 64, 7, 16, base_store=(blb, bub))
+    status, olb, oub, _, _ = ctx.fixpoint_nodes(off, var, lb, ub, sched=P.SCHED_EVENTS)
+    op, x, y, z = ctx.bytecode()
+    bs = np.ascontiguousarray(np.stack([blb, bub], 1))
+    ostatus, ostore, _ = oracle.fixpoint_nodes(op, x, y, z, bs, off, var, lb, ub)
+    np.testing.assert_array_equal(status, ostatus)
+    ok = ostatus == oracle.OK
+    np.testing.assert_array_equal(olb[ok], ostore[ok, :, 0])
