@@ -15,7 +15,11 @@
 #include <numeric>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "pir_engine.h"
+
+namespace cg = cooperative_groups;
 
 namespace pirgpu {
 
@@ -190,6 +194,137 @@ __global__ void __launch_bounds__(512) k_instances(InstArgs a) {
       a.out[j].ns = globaltimer() - t0;
     }
     __syncthreads();
+  }
+}
+
+// ------------------------------------------------ cluster instance kernel ---
+//
+// Instances whose store does not fit one CTA's shared memory run on a
+// cluster of CLU CTAs: variable v lives in the shared memory of CTA
+// (v % CLU) at slot v / CLU, and every CTA reads and joins remote slots
+// through distributed shared memory.  The cluster's threads split the
+// propagators; rounds end with a hardware cluster barrier, and the round's
+// change / failure bits are OR-ed into rank 0's shared memory.  All CTAs of a
+// cluster take the same branches, so every one runs the same barriers, and
+// they leave together after a barrier that follows the last remote read.
+constexpr int CLU = 8;
+
+struct DsmStore {
+  int2 *base[CLU];  // the slot array of each CTA of the cluster (generic addresses)
+  __device__ __forceinline__ int2 *slot(int v) const { return base[v & (CLU - 1)] + (v >> 3); }
+  __device__ __forceinline__ Itv load(int v) const {
+    const volatile int2 *p = slot(v);
+    return mk(p->x, p->y);
+  }
+  __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
+    int n = 0;
+    int2 *p = slot(v);
+    int nl = seen.l, nu = seen.u;
+    if (r.l > seen.l) {
+      const int old = atomicMax(&p->x, r.l);
+      n += old < r.l;
+      nl = max(old, r.l);
+    }
+    if (r.u < seen.u) {
+      const int old = atomicMin(&p->y, r.u);
+      n += old > r.u;
+      nu = min(old, r.u);
+    }
+    if (n && is_bot(mk(nl, nu))) failed = 1;
+    return n;
+  }
+};
+
+struct CluArgs {
+  const int4 *op, *x, *y, *z;
+  const long long *coff, *voff;
+  int2 *store;
+  const int *order;  // the instances this kernel runs, largest first
+  int ninst;
+  int *next;
+  InstOut *out;
+  long long max_rounds;
+};
+
+__global__ void __launch_bounds__(512, 1) k_instances_cluster(CluArgs a) {
+  extern __shared__ int4 sm[];
+  __shared__ int s_inst;
+  __shared__ unsigned s_flags[3][2];  // rank 0's: [round % 3][changed, failed]
+  __shared__ unsigned long long s_t0;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  int2 *mine = reinterpret_cast<int2 *>(sm);
+  DsmStore st;
+#pragma unroll
+  for (int k = 0; k < CLU; ++k) st.base[k] = cluster.map_shared_rank(mine, k);
+  unsigned *flags0 = cluster.map_shared_rank(&s_flags[0][0], 0);
+  int *inst0 = cluster.map_shared_rank(&s_inst, 0);
+  const int ctid = rank * blockDim.x + threadIdx.x, cstride = CLU * blockDim.x;
+  for (;;) {
+    cluster.sync();
+    if (rank == 0 && threadIdx.x == 0) {
+      s_inst = atomicAdd(a.next, 1);
+      for (int q = 0; q < 3; ++q) s_flags[q][0] = s_flags[q][1] = 0;
+    }
+    cluster.sync();
+    const int k = *inst0;
+    // Every CTA has read rank 0's slot before any CTA may leave: a CTA must
+    // not exit while another can still access its shared memory.
+    cluster.sync();
+    if (k >= a.ninst) break;
+    const int j = a.order[k];
+    const long long c0 = a.coff[j];
+    const int nch = (int)(a.coff[j + 1] - c0);
+    const long long v0 = a.voff[j];
+    const int nv = (int)(a.voff[j + 1] - v0);
+    int2 *gs = a.store + v0;
+    if (rank == 0 && threadIdx.x == 0) s_t0 = globaltimer();
+    // this CTA's slots: variables v = CLU * i + rank
+    for (int i = threadIdx.x; CLU * i + rank < nv; i += blockDim.x) mine[i] = gs[CLU * i + rank];
+    Bytecode bc;
+    bc.op = a.op + c0;
+    bc.x = a.x + c0;
+    bc.y = a.y + c0;
+    bc.z = a.z + c0;
+    bc.nchunks = nch;
+    cluster.sync();
+    int dummy = 0;
+    for (int c = ctid; c < nch; c += cstride) {  // install: reified targets met with [0, 1]
+      const int4 o = bc.op[c], X = bc.x[c];
+      const int ops[4] = {o.x, o.y, o.z, o.w}, xs[4] = {X.x, X.y, X.z, X.w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (ops[q] == OP_EQ || ops[q] == OP_LEQ) st.embed(xs[q], st.load(xs[q]), mk(0, 1), dummy);
+    }
+    cluster.sync();
+    long long round = 0;
+    unsigned changed_any = 0, failed_any = 0;
+    unsigned long long narrowed = 0;
+    for (;;) {
+      const int par = (int)(round % 3);
+      if (rank == 0 && threadIdx.x == 0) s_flags[(round + 1) % 3][0] = s_flags[(round + 1) % 3][1] = 0;
+      int ch = 0, f = 0;
+      for (int c = ctid; c < nch; c += cstride) ch += sweep_chunk(bc, c, st, f);
+      narrowed += ch;
+      const int any_ch = __syncthreads_or(ch), any_f = __syncthreads_or(f);
+      if (threadIdx.x == 0) {
+        if (any_ch) atomicOr(flags0 + 2 * par, 1u);
+        if (any_f) atomicOr(flags0 + 2 * par + 1, 1u);
+      }
+      cluster.sync();
+      changed_any = *(volatile unsigned *)(flags0 + 2 * par);
+      failed_any = *(volatile unsigned *)(flags0 + 2 * par + 1);
+      ++round;
+      if (failed_any || !changed_any || (a.max_rounds > 0 && round >= a.max_rounds)) break;
+    }
+    for (int i = threadIdx.x; CLU * i + rank < nv; i += blockDim.x) gs[CLU * i + rank] = mine[i];
+    narrowed = warp_sum64(narrowed);
+    if ((threadIdx.x & 31) == 0 && narrowed) atomicAdd(&a.out[j].narrowed, narrowed);
+    if (rank == 0 && threadIdx.x == 0) {
+      a.out[j].status = failed_any ? PIR_FAILED : (changed_any ? PIR_TIMEOUT : PIR_OK);
+      a.out[j].rounds = (int)round;
+      a.out[j].ns = globaltimer() - s_t0;
+    }
   }
 }
 
@@ -765,6 +900,24 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
     return prop_off[p + 1] - prop_off[p] > prop_off[q + 1] - prop_off[q];
   });
+  // Instances whose store does not fit one CTA's shared memory (at two CTAs
+  // per SM) but fits a cluster's go to the cluster kernel, the rest to the
+  // one-CTA-per-instance kernel; `order` lists the cluster ones first.
+  const int small_cap = (std::min(ctx->smem_optin, (int)((228 * 1024) / 2) - 2048) / 16) * 16;
+  const int clu_cap = (ctx->smem_optin / 16) * 16 - 1024;
+  int nbig = 0;
+  if (opts.mode != PIR_MODE_SMEM) {
+    std::vector<int> big, rest;
+    for (int j : order) {
+      const long long nv = var_off[j + 1] - var_off[j];
+      const long long slot_bytes = ((nv + CLU - 1) / CLU) * 8;
+      if (nv * 8 > small_cap && slot_bytes <= clu_cap) big.push_back(j);
+      else rest.push_back(j);
+    }
+    nbig = (int)big.size();
+    order = big;
+    order.insert(order.end(), rest.begin(), rest.end());
+  }
   int r;
   if ((r = ensure(ctx, (void **)&b->d_bc, &b->cap_bc, (size_t)std::max<long long>(nchunks, 1) * 64))) return r;
   if ((r = ensure(ctx, (void **)&b->d_off, &b->cap_off, off.size() * sizeof(long long)))) return r;
@@ -815,7 +968,45 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   a.smem_cap = smem;
   const int grid = std::max(1, std::min(ninst, ctx->num_sms * per_sm));
   PIR_CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  k_instances<<<grid, block, smem, ctx->stream>>>(a);
+  if (nbig > 0) {
+    // phase 1: the large instances on clusters of CLU CTAs (whole GPU)
+    CluArgs ca;
+    ca.op = a.op;
+    ca.x = a.x;
+    ca.y = a.y;
+    ca.z = a.z;
+    ca.coff = a.coff;
+    ca.voff = a.voff;
+    ca.store = a.store;
+    ca.order = d_order;
+    ca.ninst = nbig;
+    ca.next = d_next + 1;
+    ca.out = b->d_iout;
+    ca.max_rounds = a.max_rounds;
+    PIR_CK(cudaFuncSetAttribute(k_instances_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, clu_cap));
+    cudaLaunchConfig_t cfg;
+    std::memset(&cfg, 0, sizeof(cfg));
+    const int nclusters = std::max(1, std::min(nbig, ctx->num_sms / CLU));
+    cfg.gridDim = dim3(nclusters * CLU);
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = clu_cap;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CLU;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PIR_CK(cudaLaunchKernelEx(&cfg, k_instances_cluster, ca));
+  }
+  if (nbig < ninst) {
+    // phase 2: the rest, one CTA per instance
+    a.order = d_order + nbig;
+    a.ninst = ninst - nbig;
+    const int grid2 = std::max(1, std::min(ninst - nbig, ctx->num_sms * per_sm));
+    k_instances<<<grid2, block, smem, ctx->stream>>>(a);
+  }
   PIR_CK(cudaGetLastError());
   PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   if (nvars) {

@@ -58,22 +58,42 @@ static __device__ __forceinline__ int cl(long long v) {
 static __device__ __forceinline__ long long mn(long long a, long long b) { return a < b ? a : b; }
 static __device__ __forceinline__ long long mx(long long a, long long b) { return a > b ? a : b; }
 
+// Truncating quotient and remainder, b != 0: 32-bit division when both
+// operands fit in int32 (and the quotient does), the 64-bit routine otherwise.
+static __device__ __forceinline__ void d_qr(long long a, long long b, long long &q, long long &r) {
+  if (a >= INT_MIN && a <= INT_MAX && b >= INT_MIN && b <= INT_MAX && !(a == INT_MIN && b == -1)) {
+    const int qi = (int)a / (int)b;
+    q = qi;
+    r = a - (long long)qi * b;
+  } else {
+    q = a / b;
+    r = a - q * b;
+  }
+}
 // Integer divisions by their definitions (cuda-battery tdiv/fdiv/cdiv/ediv), b != 0.
 static __device__ __forceinline__ long long d_fdiv(long long a, long long b) {
-  long long q = a / b, r = a - q * b;
+  long long q, r;
+  d_qr(a, b, q, r);
   return (r != 0 && ((r ^ b) < 0)) ? q - 1 : q;
 }
 static __device__ __forceinline__ long long d_cdiv(long long a, long long b) {
-  long long q = a / b, r = a - q * b;
+  long long q, r;
+  d_qr(a, b, q, r);
   return (r != 0 && ((r ^ b) >= 0)) ? q + 1 : q;
 }
 static __device__ __forceinline__ long long d_ediv(long long a, long long b) {
-  long long q = a / b, r = a - q * b;
+  long long q, r;
+  d_qr(a, b, q, r);
   return r < 0 ? (b > 0 ? q - 1 : q + 1) : q;
+}
+static __device__ __forceinline__ long long d_tdiv(long long a, long long b) {
+  long long q, r;
+  d_qr(a, b, q, r);
+  return q;
 }
 static __device__ __forceinline__ long long d_div(int op, long long a, long long b) {
   switch (op) {
-    case OP_TDIV: return a / b;
+    case OP_TDIV: return d_tdiv(a, b);
     case OP_CDIV: return d_cdiv(a, b);
     case OP_FDIV: return d_fdiv(a, b);
     default: return d_ediv(a, b);

@@ -158,3 +158,24 @@ def test_nodes_events_need_a_fixpoint_base(P, oracle):
     np.testing.assert_array_equal(status, ostatus)
     ok = ostatus == oracle.OK
     np.testing.assert_array_equal(olb[ok], ostore[ok, :, 0])
+
+
+def test_instances_cluster_path(P, oracle):
+    """More large instances than clusters (work stealing across clusters of 8
+    CTAs sharing the store through distributed shared memory) plus small ones
+    in the same call: every store bit-exact."""
+    import workloads as W
+    insts = [W.plain(30_000 + 997 * j, 120_000 + 3000 * j, 1000, 40 + j, mix=W.MIX_UNEVEN) for j in range(24)]
+    insts += [W.plain(400 + 10 * j, 1600 + 40 * j, 1000, 90 + j, mix=W.MIX_UNEVEN) for j in range(8)]
+    prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
+    ctx = P.Context(0)
+    status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
+    for j, inst in enumerate(insts):
+        s = inst.store()
+        oracle.install(inst.op, inst.x, inst.y, inst.z, s)
+        orc, _ = oracle.fixpoint(inst.op, inst.x, inst.y, inst.z, s)
+        assert status[j] == orc == oracle.OK, j
+        np.testing.assert_array_equal(lb[var_off[j]:var_off[j + 1]], s[:, 0])
+        np.testing.assert_array_equal(ub[var_off[j]:var_off[j + 1]], s[:, 1])
+    capped, r2, _, _ = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb.copy(), ub.copy(), max_rounds=1)
+    assert np.all(r2 <= 1)
