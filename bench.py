@@ -381,29 +381,36 @@ def run_nodes(args):
         cr.flush_l2()
     clocks = clk.stop()
     # the batched AC-1 kernel, for reference
-    _, _, _, _, st_ac1 = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=pirgpu.SCHED_AC1)
+    st_ac1 = {"device_ms": None, "executions": None}
+    if not args.no_cpu:
+        _, _, _, _, st_ac1 = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=pirgpu.SCHED_AC1)
     dev_s = sum(r["device_ms"] for r in runs) / 1e3
     value = nn * args.steps / dev_s
     execs = sum(r["executions"] for r in runs)
     joins = sum(r["narrowed"] for r in runs)
     # the plain single-instance GPU loop, node after node (sample)
     snap = ctx.snapshot()
-    ctx.autotune(8)
     sample = min(nn, args.seq_nodes)
-    seq_dev, t0 = 0.0, time.perf_counter()
-    for j in range(sample):
+    seq_dev_rate = seq_wall_rate = None
+    if sample:
+        ctx.autotune(8)
         ctx.restore(snap)
-        ctx.embed_many(var[off[j]:off[j + 1]], lb[off[j]:off[j + 1]], ub[off[j]:off[j + 1]])
-        rc, st = ctx.fixpoint()
-        seq_dev += st["device_ms"] / 1e3
-    seq_wall = time.perf_counter() - t0
-    ctx.restore(snap)
-    seq_dev_rate = sample / seq_dev
-    seq_wall_rate = sample / seq_wall
+        seq_dev, t0 = 0.0, time.perf_counter()
+        for j in range(sample):
+            ctx.restore(snap)
+            ctx.embed_many(var[off[j]:off[j + 1]], lb[off[j]:off[j + 1]], ub[off[j]:off[j + 1]])
+            rc, st = ctx.fixpoint()
+            seq_dev += st["device_ms"] / 1e3
+        seq_wall = time.perf_counter() - t0
+        ctx.restore(snap)
+        seq_dev_rate = sample / seq_dev
+        seq_wall_rate = sample / seq_wall
     # end to end: host tightenings in, node stores out
-    t0 = time.perf_counter()
-    status, olb, oub, rounds2, st = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=True, sched=sched)
-    e2e_t = time.perf_counter() - t0
+    e2e_t = None
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        ctx.fixpoint_nodes(off, var, lb, ub, want_stores=True, sched=sched)
+        e2e_t = time.perf_counter() - t0
     hbm, hbm_src = peaks()
     achieved = (execs * ALG_BYTES_PER_EXEC + joins * ALG_BYTES_PER_JOIN) / dev_s / 1e9
     cpu = None
@@ -430,13 +437,15 @@ def run_nodes(args):
                    "batched_ac1_ms": st_ac1["device_ms"], "batched_ac1_executions": st_ac1["executions"]},
         "plain_sequential": {"nodes_per_s_device": seq_dev_rate, "nodes_per_s_wall": seq_wall_rate,
                              "sample_nodes": sample,
-                             "batched_over_sequential_device": value / seq_dev_rate,
-                             "batched_over_sequential_wall": (nn / e2e_t) / seq_wall_rate},
+                             "batched_over_sequential_device": value / seq_dev_rate if seq_dev_rate else None,
+                             "batched_over_sequential_wall": (nn / e2e_t) / seq_wall_rate
+                             if (seq_wall_rate and e2e_t) else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": ncu_traffic("nodes_fixpoint"),
                      "peak_source": hbm_src},
         "cpu_baseline": cpu,
-        "e2e": {"value": nn / e2e_t, "unit": "nodes/s", "h2d_bytes_per_step": int(len(var) * 12 + len(off) * 4),
+        "e2e": {"value": nn / e2e_t if e2e_t else None, "unit": "nodes/s",
+                "h2d_bytes_per_step": int(len(var) * 12 + len(off) * 4),
                 "d2h_bytes_per_step": int(nn * len(blb) * 8)},
         "gpu_launches": args.steps, "clocks": clocks,
     }
