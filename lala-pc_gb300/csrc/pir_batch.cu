@@ -529,7 +529,7 @@ struct EvStore {
   }
 };
 
-__global__ void __launch_bounds__(512) k_nodes_events(EvArgs a) {
+__global__ void __launch_bounds__(1024) k_nodes_events(EvArgs a) {
   __shared__ int s_node, s_ncand, s_nd[2], s_nt;
   const size_t nv = (size_t)a.nvars;
   int2 *ws = a.ws + blockIdx.x * nv;
@@ -711,7 +711,7 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
                           int32_t *out_ub, int32_t *out_status, int32_t *out_rounds, pir_stats *stats) {
   int r;
   if ((r = ensure_events_graph(ctx, b))) return r;
-  const int block = 512;
+  const int block = opts.block > 0 ? std::min(std::max(opts.block / 32 * 32, 32), 1024) : 256;
   int occ = 0;
   PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nodes_events, block, 0));
   occ = std::max(occ, 1);
