@@ -154,7 +154,7 @@ static __device__ __forceinline__ void meet(Itv &a, Itv b) {
 }
 
 // r1 = r2 / r3 forward (pir.hpp:449-467)
-static __device__ __noinline__ void itv_div(int op, Itv &r1, Itv &r2, Itv &r3) {
+static __device__ __forceinline__ void itv_div(int op, Itv &r1, Itv &r2, Itv &r3) {
   if (r3.l < 0 && r3.u > 0) {
     r1.l = max(r1.l, min(r2.l, r2.u == MINF ? INF : sneg(r2.u)));
     r1.u = min(r1.u, max(r2.l == INF ? MINF : sneg(r2.l), r2.u));
@@ -341,9 +341,17 @@ static __device__ Itv den_ediv(Itv r1, Itv r2, Itv r3) {
   return top();
 }
 
+// The three intervals of one propagator, passed to and returned from the out
+// of line division code by value: a reference would take the caller's
+// intervals' address and put them in local memory for every opcode.
+struct Itv3 {
+  Itv a, b, c;
+};
+
 // The four division opcodes (pir.hpp:780-792), out of line so that the common
 // opcodes keep a small register footprint.
-static __device__ __noinline__ void deduce_div(int op, Itv &r1, Itv &r2, Itv &r3) {
+static __device__ __noinline__ Itv3 deduce_div(int op, Itv3 t) {
+  Itv r1 = t.a, r2 = t.b, r3 = t.c;
   itv_div(op, r1, r2, r3);
   if (!is_bot(r1) && !is_bot(r3)) {
     switch (op) {
@@ -361,6 +369,11 @@ static __device__ __noinline__ void deduce_div(int op, Itv &r1, Itv &r2, Itv &r3
       }
     }
   }
+  Itv3 out;
+  out.a = r1;
+  out.b = r2;
+  out.c = r3;
+  return out;
 }
 
 // ---------------------------------------------------------------- deduce ----
@@ -445,9 +458,17 @@ static __device__ __forceinline__ int deduce_loaded(int op, int X, int Y, int Z,
     case OP_TDIV:
     case OP_FDIV:
     case OP_CDIV:
-    case OP_EDIV:
-      deduce_div(op, r1, r2, r3);
+    case OP_EDIV: {
+      Itv3 t;
+      t.a = r1;
+      t.b = r2;
+      t.c = r3;
+      t = deduce_div(op, t);
+      r1 = t.a;
+      r2 = t.b;
+      r3 = t.c;
       break;
+    }
     default:
       return 0;
   }

@@ -17,9 +17,10 @@ using namespace pirgpu;
 
 // Persistent AC-1 fixpoint: one cooperative launch, rounds separated by the
 // bounded grid barrier.  PPI propagators per thread and step; MINB CTAs of 256
-// threads per SM bound the register budget.  Thread 0 of CTA 0 writes the
-// round count.
-template <int PPI, int MINB>
+// threads per SM bound the register budget; PIPE selects the software-pipelined
+// sweep (next step's gathers in flight while this step computes).  Thread 0 of
+// CTA 0 writes the round count.
+template <int PPI, int MINB, bool PIPE = false>
 __global__ void __launch_bounds__(256, MINB) k_fixpoint_persistent(Bytecode bc, int2 *store, Control *ctl,
                                                                    long long max_rounds, long long timeout_ns) {
   __shared__ unsigned s_word;
@@ -31,7 +32,10 @@ __global__ void __launch_bounds__(256, MINB) k_fixpoint_persistent(Bytecode bc, 
   long long round = 0;
   for (;;) {
     int changed = 0, failed = 0;
-    for (int c = gtid; c < nsteps; c += gstride) changed += sweep_step<PPI>(bc, c, st, failed);
+    if (PIPE)
+      changed = sweep_pipelined<PPI>(bc, gtid, gstride, nsteps, st, failed);
+    else
+      for (int c = gtid; c < nsteps; c += gstride) changed += sweep_step<PPI>(bc, c, st, failed);
     narrowed += changed;
     const int any_changed = __syncthreads_or(changed);
     const int any_failed = __syncthreads_or(failed);
@@ -64,6 +68,7 @@ static const PersistentVariant kPersistent[] = {
     {2, 3, (const void *)k_fixpoint_persistent<2, 3>}, {2, 4, (const void *)k_fixpoint_persistent<2, 4>},
     {1, 4, (const void *)k_fixpoint_persistent<1, 4>}, {1, 6, (const void *)k_fixpoint_persistent<1, 6>},
     {4, 1, (const void *)k_fixpoint_persistent<4, 1>}, {2, 2, (const void *)k_fixpoint_persistent<2, 2>},
+    {1, 3, (const void *)k_fixpoint_persistent<1, 3, true>}, {2, 2, (const void *)k_fixpoint_persistent<2, 2, true>},
 };
 static const int kNumPersistent = sizeof(kPersistent) / sizeof(kPersistent[0]);
 

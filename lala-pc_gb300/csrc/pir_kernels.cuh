@@ -172,6 +172,73 @@ __device__ __forceinline__ int sweep_step(const Bytecode &bc, int c, S &st, int 
   return ch;
 }
 
+template <int PPI>
+__device__ __forceinline__ void bc_fetch(const Bytecode &bc, int c, typename Vec<PPI>::T (&v)[4]) {
+  using V = typename Vec<PPI>::T;
+  v[0] = __ldg(reinterpret_cast<const V *>(bc.op) + c);
+  v[1] = __ldg(reinterpret_cast<const V *>(bc.x) + c);
+  v[2] = __ldg(reinterpret_cast<const V *>(bc.y) + c);
+  v[3] = __ldg(reinterpret_cast<const V *>(bc.z) + c);
+}
+
+template <int PPI, class S>
+__device__ __forceinline__ void gather(const typename Vec<PPI>::T (&v)[4], const S &st, Itv (&a)[PPI], Itv (&b)[PPI],
+                                       Itv (&d)[PPI]) {
+#pragma unroll
+  for (int k = 0; k < PPI; ++k) {
+    a[k] = st.load(Vec<PPI>::get(v[1], k));
+    b[k] = st.load(Vec<PPI>::get(v[2], k));
+    d[k] = st.load(Vec<PPI>::get(v[3], k));
+  }
+}
+
+// Grid-strided sweep over the steps c, c + stride, ... below nsteps, software
+// pipelined: before step i is computed, the intervals of step i+1 and the
+// bytecode of step i+2 are already requested, so two L2 round trips overlap
+// the arithmetic instead of following it.  Reads may therefore be up to two
+// steps older than this thread's own joins; within a round every read may be
+// stale anyway, and a round in which nothing changed anywhere read the store of
+// its start, so the end-of-round change test stays exact.
+template <int PPI, class S>
+__device__ __forceinline__ int sweep_pipelined(const Bytecode &bc, int c, const int stride, const int nsteps, S &st,
+                                               int &failed) {
+  using V = typename Vec<PPI>::T;
+  if (c >= nsteps) return 0;
+  V cur[4], nxt[4];
+  Itv a[PPI], b[PPI], d[PPI];
+  bc_fetch<PPI>(bc, c, cur);
+  gather<PPI>(cur, st, a, b, d);
+  int c1 = c + stride;
+  if (c1 < nsteps) bc_fetch<PPI>(bc, c1, nxt);
+  int ch = 0;
+  for (;;) {
+    const bool has1 = c1 < nsteps;
+    Itv a1[PPI], b1[PPI], d1[PPI];
+    if (has1) gather<PPI>(nxt, st, a1, b1, d1);
+    const int c2 = c1 + stride;
+    V nn[4];
+    if (c2 < nsteps) bc_fetch<PPI>(bc, c2, nn);
+#pragma unroll
+    for (int k = 0; k < PPI; ++k)
+      ch += deduce_loaded(Vec<PPI>::get(cur[0], k), Vec<PPI>::get(cur[1], k), Vec<PPI>::get(cur[2], k),
+                          Vec<PPI>::get(cur[3], k), a[k], b[k], d[k], st, failed);
+    if (!has1) break;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      cur[j] = nxt[j];
+      nxt[j] = nn[j];
+    }
+#pragma unroll
+    for (int k = 0; k < PPI; ++k) {
+      a[k] = a1[k];
+      b[k] = b1[k];
+      d[k] = d1[k];
+    }
+    c1 = c2;
+  }
+  return ch;
+}
+
 // Number of PPI-wide steps covering the (4-padded) bytecode.
 template <int PPI>
 __device__ __forceinline__ int steps_of(const Bytecode &bc) {

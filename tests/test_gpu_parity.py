@@ -216,7 +216,7 @@ def test_engine_order_is_reference_sort(P, oracle):
         np.testing.assert_array_equal(a, b[perm])
 
 
-@pytest.mark.parametrize("variant", range(1, 9))
+@pytest.mark.parametrize("variant", range(1, 11))
 def test_persistent_variants(variant, P, oracle):
     """Every autotuner candidate computes the same fixpoint."""
     import workloads as W
