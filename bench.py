@@ -247,7 +247,7 @@ def run_ours(args):
     kw = dict(mode=args.mode, max_rounds=args.max_rounds, variant=args.variant)
     tuned = None
     if args.mode in (0, 1) and args.variant == 0:
-        tuned = ctx.autotune(16)
+        tuned = ctx.autotune(64)
         ctx.restore(snap)
     ok = (pirgpu.OK, pirgpu.TIMEOUT) if args.max_rounds else (pirgpu.OK,)
 
@@ -363,15 +363,25 @@ def run_nodes(args):
     """Batched search nodes: 4,096 nodes over a 100,000-var / 400,000-propagator
     base at its fixpoint, each bisecting k ~ U[1, 64] variables."""
     import pirgpu
+    import shard
     ws, rank, local = dist_env()
+    dist = dist_init(ws)
     cr = Cudart()
     cr.set_device(local)
     ctx, base, (blb, bub), off, var, lb, ub = _nodes_workload()
+    nn_all = len(off) - 1
+    if ws > 1:
+        # this rank's nodes (cost-balanced partition, no collective on the data path)
+        parts = shard.lpt_partition(shard.node_costs(off), ws)
+        off, var, lb, ub = shard.select_nodes(off, var, lb, ub, parts[rank])
     nn = len(off) - 1
     sched = pirgpu.SCHED_EVENTS if args.node_sched == "events" else pirgpu.SCHED_AC1
     for _ in range(args.warmup):
         ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=sched)
         cr.flush_l2()
+    if dist:
+        dist.barrier()
+    cr.sync()
     clk = ClockSampler(local)
     clk.start()
     runs = []
@@ -380,17 +390,24 @@ def run_nodes(args):
         runs.append(st)
         cr.flush_l2()
     clocks = clk.stop()
+    dev_s = sum(r["device_ms"] for r in runs) / 1e3
+    t_max = dist_max(dist, dev_s)
+    value = nn_all * args.steps / t_max
+    n_ok = int(dist_sum(dist, int((status == 0).sum())))
+    n_failed = int(dist_sum(dist, int((status == 1).sum())))
+    max_rounds = int(dist_max(dist, int(rounds.max()) if nn else 0))
+    if rank != 0:
+        return
+    extras = ws == 1  # comparison runs and the CPU baseline: rank 0 at N=1 only
     # the batched AC-1 kernel, for reference
     st_ac1 = {"device_ms": None, "executions": None}
-    if not args.no_cpu:
+    if extras and not args.no_cpu:
         _, _, _, _, st_ac1 = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=pirgpu.SCHED_AC1)
-    dev_s = sum(r["device_ms"] for r in runs) / 1e3
-    value = nn * args.steps / dev_s
     execs = sum(r["executions"] for r in runs)
     joins = sum(r["narrowed"] for r in runs)
     # the plain single-instance GPU loop, node after node (sample)
     snap = ctx.snapshot()
-    sample = min(nn, args.seq_nodes)
+    sample = min(nn, args.seq_nodes) if extras else 0
     seq_dev_rate = seq_wall_rate = None
     if sample:
         ctx.autotune(8)
@@ -407,14 +424,14 @@ def run_nodes(args):
         seq_wall_rate = sample / seq_wall
     # end to end: host tightenings in, node stores out
     e2e_t = None
-    if not args.no_e2e:
+    if extras and not args.no_e2e:
         t0 = time.perf_counter()
         ctx.fixpoint_nodes(off, var, lb, ub, want_stores=True, sched=sched)
         e2e_t = time.perf_counter() - t0
     hbm, hbm_src = peaks()
     achieved = (execs * ALG_BYTES_PER_EXEC + joins * ALG_BYTES_PER_JOIN) / dev_s / 1e9
     cpu = None
-    if not args.no_cpu:
+    if extras and not args.no_cpu:
         from oracle import oracle as O
         op, x, y, z = ctx.bytecode()
         bs = np.ascontiguousarray(np.stack([blb, bub], 1))
@@ -426,25 +443,27 @@ def run_nodes(args):
         cpu = {"value": m / ct, "unit": "nodes/s", "cores": th, "kind": "port",
                "sample": "%d nodes, Gauss-Seidel per node, %d host threads, %.1f s" % (m, th, ct)}
     out = {
-        "metric": "batched nodes/sec", "value": value, "unit": "nodes/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+        "metric": "batched nodes/sec", "value": value, "unit": "nodes/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic: planted-solution base instance at its fixpoint, bisected nodes",
         "config": {"workload": "nodes: 100,000 vars / 400,000 propagators (bounds scale 1e6) at its fixpoint, 4,096 nodes, k ~ U[1,64] bisections of unfixed vars",
-                   "nodes_ok": int((status == 0).sum()), "nodes_failed": int((status == 1).sum()),
-                   "max_rounds": int(rounds.max()), "mean_rounds": float(rounds.mean()),
+                   "parallelism": "nodes sharded over %d ranks (cost-balanced, no collective)" % ws
+                   if ws > 1 else "single",
+                   "nodes_ok": n_ok, "nodes_failed": n_failed,
+                   "max_rounds": max_rounds, "mean_rounds_rank0": float(rounds.mean()) if nn else 0.0,
                    "schedule": args.node_sched, "executions_per_step": execs // args.steps,
                    "batched_ac1_ms": st_ac1["device_ms"], "batched_ac1_executions": st_ac1["executions"]},
         "plain_sequential": {"nodes_per_s_device": seq_dev_rate, "nodes_per_s_wall": seq_wall_rate,
                              "sample_nodes": sample,
                              "batched_over_sequential_device": value / seq_dev_rate if seq_dev_rate else None,
-                             "batched_over_sequential_wall": (nn / e2e_t) / seq_wall_rate
+                             "batched_over_sequential_wall": (nn_all / e2e_t) / seq_wall_rate
                              if (seq_wall_rate and e2e_t) else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": ncu_traffic("nodes_fixpoint"),
+                     "frac": achieved / hbm, "traffic": ncu_traffic("nodes_events_4096_nodes"),
                      "peak_source": hbm_src},
         "cpu_baseline": cpu,
-        "e2e": {"value": nn / e2e_t if e2e_t else None, "unit": "nodes/s",
+        "e2e": {"value": nn_all / e2e_t if e2e_t else None, "unit": "nodes/s",
                 "h2d_bytes_per_step": int(len(var) * 12 + len(off) * 4),
                 "d2h_bytes_per_step": int(nn * len(blb) * 8)},
         "gpu_launches": args.steps, "clocks": clocks,
@@ -507,16 +526,30 @@ def run_learned(args):
 def run_uneven(args):
     """512 independent instances, propagators log-uniform in [1e3, 2e5]."""
     import pirgpu
+    import shard
     import workloads as W
     ws, rank, local = dist_env()
+    dist = dist_init(ws)
     cr = Cudart()
     cr.set_device(local)
-    insts = W.uneven(512, 1000, 200_000, 0)
-    prop_off, var_off, op, x, y, z, lb0, ub0 = W.pack(insts)
+    insts_all = W.uneven(512, 1000, 200_000, 0)
+    n_all = len(insts_all)
+    prop_off, var_off, op, x, y, z, lb0, ub0 = W.pack(insts_all)
+    total_props = int(prop_off[-1])
+    insts = insts_all
+    if ws > 1:
+        # this rank's instances (cost-balanced partition, no collective on the data path)
+        parts = shard.lpt_partition(shard.instance_costs(prop_off), ws)
+        prop_off, var_off, op, x, y, z, lb0, ub0 = shard.select_instances(prop_off, var_off, op, x, y, z,
+                                                                          lb0, ub0, parts[rank])
+        insts = [insts_all[i] for i in parts[rank]]
     ctx = pirgpu.Context(local)
     for _ in range(args.warmup):
         lb, ub = lb0.copy(), ub0.copy()
         ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
+    if dist:
+        dist.barrier()
+    cr.sync()
     clk = ClockSampler(local)
     clk.start()
     runs, walls, per = [], [], []
@@ -529,13 +562,20 @@ def run_uneven(args):
         per.append(ms)
     clocks = clk.stop()
     dev_s = sum(r["device_ms"] for r in runs) / 1e3
-    n = len(insts)
+    t_max = dist_max(dist, dev_s)
+    wall_max = dist_max(dist, sum(walls))
+    n_failed = int(dist_sum(dist, int((status == 1).sum())))
     per = np.concatenate(per)
+    per_all = shard.gather_to_root(dist, per)
+    if rank != 0:
+        return
+    per_all = np.concatenate(per_all)
+    n = len(insts)
     execs = sum(r["executions"] for r in runs)
     hbm, hbm_src = peaks()
     achieved = execs * ALG_BYTES_PER_EXEC / dev_s / 1e9
     cpu = None
-    if not args.no_cpu:
+    if ws == 1 and not args.no_cpu:
         from oracle import oracle as O
         m = n
         sub = insts
@@ -548,18 +588,21 @@ def run_uneven(args):
         cpu = {"value": m / ct, "unit": "instances/s", "cores": th, "kind": "port",
                "sample": "all %d instances (install + Gauss-Seidel each), %d host threads, %.1f s" % (m, th, ct)}
     out = {
-        "metric": "batched instances/sec", "value": n * args.steps / dev_s, "unit": "instances/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+        "metric": "batched instances/sec", "value": n_all * args.steps / t_max, "unit": "instances/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic: planted-solution instances",
         "config": {"workload": "uneven: 512 instances, propagators log-uniform [1e3, 2e5], vars = props/4, "
-                               "5% tdiv + 5% tmod", "propagators": int(prop_off[-1]),
-                   "instance_ms_p50": float(np.percentile(per, 50)), "instance_ms_p99": float(np.percentile(per, 99)),
-                   "failed": int((status == 1).sum())},
+                               "5% tdiv + 5% tmod", "propagators": total_props,
+                   "parallelism": "instances sharded over %d ranks (cost-balanced, no collective)" % ws
+                   if ws > 1 else "single",
+                   "instance_ms_p50": float(np.percentile(per_all, 50)),
+                   "instance_ms_p99": float(np.percentile(per_all, 99)),
+                   "failed": n_failed},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": ncu_traffic("instances_fixpoint"), "peak_source": hbm_src},
+                     "traffic": ncu_traffic("instances_cluster_uneven_512"), "peak_source": hbm_src},
         "cpu_baseline": cpu,
-        "e2e": {"value": n * args.steps / sum(walls), "unit": "instances/s",
+        "e2e": {"value": n_all * args.steps / wall_max, "unit": "instances/s",
                 "h2d_bytes_per_step": int(prop_off[-1] * 16 + var_off[-1] * 8),
                 "d2h_bytes_per_step": int(var_off[-1] * 8)},
         "gpu_launches": args.steps, "clocks": clocks,

@@ -62,6 +62,10 @@ enum pir_sched {
                              propagators of the variables that changed in the previous round */
 };
 
+/* Number of persistent-kernel variants (propagators per thread and step x CTAs
+ * per SM x pipelined sweep) that pir_autotune chooses from. */
+#define PIR_PERSISTENT_VARIANTS 10
+
 typedef struct pir_opts {
   int64_t max_rounds;         /* 0: no cap */
   int64_t barrier_timeout_ns; /* 0: 2 s; bound on every grid-barrier wait */
@@ -70,7 +74,7 @@ typedef struct pir_opts {
   int32_t ctas_per_sm;        /* persistent grid = SMs * ctas_per_sm, 0: occupancy limit */
   int32_t sched;              /* enum pir_sched */
   float wake_fraction;        /* learned schedule: fraction of propagators woken per round (0: 1/16) */
-  int32_t variant;            /* persistent kernel variant 1..N (0: autotuned, else the default) */
+  int32_t variant;            /* persistent kernel variant 1..PIR_PERSISTENT_VARIANTS (0: autotuned, else the default) */
   int32_t reserved[6];
 } pir_opts;
 
@@ -123,7 +127,9 @@ int pir_get_bytecode(pirgpu_ctx *ctx, int32_t *op, int32_t *x, int32_t *y, int32
  * error.  opts may be NULL (defaults); stats may be NULL. */
 int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts, pir_stats *stats);
 /* Autotuner: times every persistent-kernel variant (propagators per thread
- * and step, CTAs per SM) for `rounds` rounds (0: 16) from the current store,
+ * and step, CTAs per SM, pipelining) for `rounds` rounds (0: 64; the first
+ * rounds of a fixpoint narrow far more than the later ones, so short windows
+ * favour the wrong variant) from the current store,
  * keeps the fastest for this context's later pir_fixpoint calls
  * (opts.variant = 0) and puts the store back.  out_variant (1-based) and
  * out_us_per_round may be NULL. */

@@ -23,25 +23,35 @@ using namespace pirgpu;
 template <int PPI, int MINB, bool PIPE = false>
 __global__ void __launch_bounds__(256, MINB) k_fixpoint_persistent(Bytecode bc, int2 *store, Control *ctl,
                                                                    long long max_rounds, long long timeout_ns) {
-  __shared__ unsigned s_word;
+  // per round parity: the CTA's OR of changed (bit 0) / failed (bit 1), and the
+  // barrier's decision word; two block barriers per round
+  __shared__ unsigned s_bits[2], s_word[2];
   RedStore st{store};
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gstride = gridDim.x * blockDim.x;
   const int nsteps = steps_of<PPI>(bc);
   unsigned long long narrowed = 0;
   long long round = 0;
+  if (threadIdx.x == 0) s_bits[0] = s_bits[1] = 0u;
+  __syncthreads();
   for (;;) {
+    const int p = (int)(round & 1);
     int changed = 0, failed = 0;
     if (PIPE)
       changed = sweep_pipelined<PPI>(bc, gtid, gstride, nsteps, st, failed);
     else
       for (int c = gtid; c < nsteps; c += gstride) changed += sweep_step<PPI>(bc, c, st, failed);
     narrowed += changed;
-    const int any_changed = __syncthreads_or(changed);
-    const int any_failed = __syncthreads_or(failed);
-    if (threadIdx.x == 0) s_word = grid_sync_or(ctl, gridDim.x, any_changed, any_failed, timeout_ns);
+    const unsigned bits = __reduce_or_sync(0xFFFFFFFFu, (changed ? 1u : 0u) | (failed ? 2u : 0u));
+    if ((threadIdx.x & 31) == 0 && bits) atomicOr(&s_bits[p], bits);
     __syncthreads();
-    const unsigned w = s_word;
+    if (threadIdx.x == 0) {
+      const unsigned b = s_bits[p];
+      s_bits[p ^ 1] = 0u;
+      s_word[p] = grid_sync_rot(ctl, gridDim.x, round, b & 1u, b & 2u, timeout_ns);
+    }
+    __syncthreads();
+    const unsigned w = s_word[p];
     ++round;
     if ((w & BIT_ERROR) || (w & BIT_FAILED) || !(w & BIT_CHANGED) || (max_rounds > 0 && round >= max_rounds)) {
       if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -51,7 +61,6 @@ __global__ void __launch_bounds__(256, MINB) k_fixpoint_persistent(Bytecode bc, 
       }
       break;
     }
-    __syncthreads();
   }
   narrowed = warp_sum64(narrowed);
   if ((threadIdx.x & 31) == 0 && narrowed) atomicAdd(&ctl->narrowed, narrowed);
@@ -71,6 +80,7 @@ static const PersistentVariant kPersistent[] = {
     {1, 3, (const void *)k_fixpoint_persistent<1, 3, true>}, {2, 2, (const void *)k_fixpoint_persistent<2, 2, true>},
 };
 static const int kNumPersistent = sizeof(kPersistent) / sizeof(kPersistent[0]);
+static_assert(sizeof(kPersistent) / sizeof(kPersistent[0]) == PIR_PERSISTENT_VARIANTS, "variant count");
 
 // One AC-1 round per launch (host-driven loop).  Change flag per round parity.
 __global__ void __launch_bounds__(256) k_sweep_round(Bytecode bc, int2 *store, Control *ctl, int parity) {
@@ -637,7 +647,7 @@ int pir_autotune(pirgpu_ctx *ctx, int32_t rounds, int32_t *out_variant, float *o
   if (out_variant) *out_variant = 0;
   if (out_us_per_round) *out_us_per_round = 0.f;
   if (ctx->n == 0 || ctx->failed || ctx->nvars == 0) return PIR_OK;
-  if (rounds <= 0) rounds = 16;
+  if (rounds <= 0) rounds = 64;
   CK(cudaSetDevice(ctx->device));
   int2 *saved = nullptr;
   if (cudaMalloc(&saved, (size_t)ctx->nvars * sizeof(int2)) != cudaSuccess) {

@@ -4,9 +4,9 @@
 // PIR::deduce(int), tests/pir_test.cpp:60-62, and of the per-block copies with
 // shared bytecode of pir.hpp:182-195): every round applies every propagator
 // once; bound joins are atomic and visible to later reads of the same round;
-// the round's "changed" and "failed" bits are OR-reduced (CTA: __syncthreads_or,
-// grid: the barrier word) and the loop stops after a round with no change, a
-// round that saw an empty interval, or the round cap.
+// the round's "changed" and "failed" bits are OR-reduced (CTA: a warp reduction
+// and a shared-memory OR, grid: the barrier word) and the loop stops after a
+// round with no change, a round that saw an empty interval, or the round cap.
 #pragma once
 #include "pir_device.cuh"
 
@@ -14,33 +14,24 @@ namespace pirgpu {
 
 // Device-side control block of one fixpoint run (scratch memory).
 struct Control {
-  unsigned long long arrive;  // barrier: arrivals | changed-count << 20 | failed-count << 40
-  unsigned long long pad0[7];
-  unsigned int gen;           // barrier generation | decision bits
-  unsigned int pad1[15];
+  // grid barrier words (grid_sync_rot): arrivals | changed-count << 20 |
+  // failed-count << 40, three in rotation, one 128-byte line each
+  unsigned long long rot[3][16];
   int status;                 // 0, or the pir_status error a CTA raised
   int failed;                 // sticky failure flag (host loop / single-thread kernels)
   int changed[4];             // host-loop change flags, one per round parity
   long long rounds;           // rounds executed (written by CTA 0)
   unsigned long long narrowed;
   unsigned long long executions;
+  unsigned long long pad[10];
 };
 
-constexpr unsigned GEN_MASK = 0x1FFFFFFFu;
 constexpr unsigned BIT_CHANGED = 1u << 29;
 constexpr unsigned BIT_FAILED = 1u << 30;
 constexpr unsigned BIT_ERROR = 1u << 31;
 
 constexpr int ERR_BARRIER_TIMEOUT = 3;  // = PIR_BARRIER_TIMEOUT
 
-static __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-static __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 static __device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
   return v;
@@ -52,39 +43,56 @@ static __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
-// Grid barrier with an OR-reduction of two bits, called by thread 0 of every
-// CTA.  Every wait is bounded by timeout_ns; on expiry the CTA records
-// PIR_BARRIER_TIMEOUT in ctl->status and the returned word carries BIT_ERROR.
-static __device__ __noinline__ unsigned grid_sync_or(Control *ctl, unsigned nblocks, int changed, int failed,
-                                              long long timeout_ns) {
-  const unsigned g0 = ld_acquire(&ctl->gen);
-  __threadfence();
+static __device__ __forceinline__ unsigned long long atom_add_release(unsigned long long *p, unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.add.release.gpu.global.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+  return old;
+}
+static __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid barrier of round `round` (0, 1, 2, ...) with an OR-reduction of the
+// changed / failed bits, called by thread 0 of every CTA.  Round r uses word
+// rot[r % 3]: each CTA adds 1 | changed << 20 | failed << 40 with one release
+// RMW and polls the same word with acquire loads until all nblocks arrived, so
+// the last arrival releases everyone directly (no generation word, no second
+// store).  CTA 0 zeroes the word of round r + 2 as soon as it has passed round
+// r: that word was last read at barrier r - 1, which every CTA left before
+// arriving at barrier r, and CTA 0's own arrival at barrier r + 1 (a release
+// after the zeroing) is seen by every CTA before it can arrive at r + 2.  The
+// three words start at zero (the host clears the control block).  Every wait is
+// bounded by timeout_ns; on expiry the CTA records PIR_BARRIER_TIMEOUT in
+// ctl->status and the result carries BIT_ERROR.
+static __device__ __noinline__ unsigned grid_sync_rot(Control *ctl, unsigned nblocks, long long round, int changed,
+                                                      int failed, long long timeout_ns) {
+  unsigned long long *w = &ctl->rot[round % 3][0];
   const unsigned long long add =
       1ull | ((unsigned long long)(changed != 0) << 20) | ((unsigned long long)(failed != 0) << 40);
-  const unsigned long long old = atomicAdd(&ctl->arrive, add);
-  if ((unsigned)(old & 0xFFFFFull) + 1u == nblocks) {
-    const unsigned long long tot = old + add;
-    const unsigned ch = (unsigned)((tot >> 20) & 0xFFFFFull), fl = (unsigned)((tot >> 40) & 0xFFFFFull);
-    ctl->arrive = 0ull;
-    unsigned next = ((g0 + 1u) & GEN_MASK) | (ch ? BIT_CHANGED : 0u) | (fl ? BIT_FAILED : 0u);
-    if (*(volatile int *)&ctl->status) next |= BIT_ERROR;
-    __threadfence();
-    st_release(&ctl->gen, next);
-    return next;
-  }
-  const unsigned long long t0 = globaltimer();
-  for (unsigned it = 0;; ++it) {
-    const unsigned g = ld_acquire(&ctl->gen);
-    if ((g & GEN_MASK) != (g0 & GEN_MASK)) return g;
-    if (it >= 32) __nanosleep(it < 256 ? 32 : 200);
-    if ((it & 7u) == 0u) {
-      if (*(volatile int *)&ctl->status) return BIT_ERROR;
-      if ((long long)(globaltimer() - t0) > timeout_ns) {
-        atomicCAS(&ctl->status, 0, ERR_BARRIER_TIMEOUT);
-        return BIT_ERROR;
+  unsigned long long v = atom_add_release(w, add) + add;
+  if ((unsigned)(v & 0xFFFFFull) != nblocks) {
+    const unsigned long long t0 = globaltimer();
+    for (unsigned it = 0;; ++it) {
+      v = ld_acquire64(w);
+      if ((unsigned)(v & 0xFFFFFull) == nblocks) break;
+      if (it >= 64) __nanosleep(it < 512 ? 20 : 200);
+      if ((it & 7u) == 0u) {
+        if (*(volatile int *)&ctl->status) return BIT_ERROR;
+        if ((long long)(globaltimer() - t0) > timeout_ns) {
+          atomicCAS(&ctl->status, 0, ERR_BARRIER_TIMEOUT);
+          return BIT_ERROR;
+        }
       }
     }
   }
+  if (blockIdx.x == 0) ctl->rot[(round + 2) % 3][0] = 0ull;
+  unsigned r = 0;
+  if ((v >> 20) & 0xFFFFFull) r |= BIT_CHANGED;
+  if ((v >> 40) & 0xFFFFFull) r |= BIT_FAILED;
+  if (*(volatile int *)&ctl->status) r |= BIT_ERROR;
+  return r;
 }
 
 // The bytecode as a structure of arrays, padded with OP_NOP to a multiple of 4

@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
   const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long gstride = (long long)gridDim.x * blockDim.x;
   unsigned long long woken = 0, narrowed = 0;
-  long long round = 0;
+  long long round = 0, nbar = 0;  // nbar: grid barriers passed (thread 0)
   bool certify = false;
   int par = 0;
   for (;;) {
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
       for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x)
         if (sh[i]) atomicAdd(gh + i, sh[i]);
       __syncthreads();
-      if (threadIdx.x == 0) s_word = grid_sync_or(a.ctl, gridDim.x, 0, 0, a.timeout_ns);
+      if (threadIdx.x == 0) s_word = grid_sync_rot(a.ctl, gridDim.x, nbar++, 0, 0, a.timeout_ns);
       __syncthreads();
       if (s_word & BIT_ERROR) break;
       // (B) threshold; CTA 0 clears the other histogram for the next round
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
     narrowed += changed;
     const int any_changed = __syncthreads_or(changed);
     const int any_failed = __syncthreads_or(failed);
-    if (threadIdx.x == 0) s_word = grid_sync_or(a.ctl, gridDim.x, any_changed, any_failed, a.timeout_ns);
+    if (threadIdx.x == 0) s_word = grid_sync_rot(a.ctl, gridDim.x, nbar++, any_changed, any_failed, a.timeout_ns);
     __syncthreads();
     const unsigned w = s_word;
     if (w & BIT_ERROR) break;

@@ -84,13 +84,16 @@ __global__ void k_static_validate(const int *op, const int *x, const int *y, con
 // The persistent AC-1 kernel with its control block in the static scratch:
 // one propagator per thread and step, scalar loads of the caller's unpadded
 // bytecode, rounds separated by the bounded grid barrier.
-__global__ void __launch_bounds__(256, 4) k_fixpoint_static(const int *op, const int *x, const int *y,
+__global__ void __launch_bounds__(256, 3) k_fixpoint_static(const int *op, const int *x, const int *y,
                                                             const int *z, long long n, int2 *store,
                                                             StaticScratch *sc, long long max_rounds,
                                                             long long timeout_ns) {
-  __shared__ unsigned s_word;
+  __shared__ unsigned s_bits[2], s_word[2];
   __shared__ unsigned long long s_narrowed;
-  if (threadIdx.x == 0) s_narrowed = 0ull;
+  if (threadIdx.x == 0) {
+    s_narrowed = 0ull;
+    s_bits[0] = s_bits[1] = 0u;
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) sc->t_start = globaltimer();
   __syncthreads();
   RedStore st{store};
@@ -106,11 +109,17 @@ __global__ void __launch_bounds__(256, 4) k_fixpoint_static(const int *op, const
       changed += deduce_loaded(o, a, b, c, ia, ib, ic, st, failed);
     }
     narrowed += changed;
-    const int any_changed = __syncthreads_or(changed);
-    const int any_failed = __syncthreads_or(failed);
-    if (threadIdx.x == 0) s_word = grid_sync_or(&sc->ctl, gridDim.x, any_changed, any_failed, timeout_ns);
+    const int p = (int)(round & 1);
+    const unsigned bits = __reduce_or_sync(0xFFFFFFFFu, (changed ? 1u : 0u) | (failed ? 2u : 0u));
+    if ((threadIdx.x & 31) == 0 && bits) atomicOr(&s_bits[p], bits);
     __syncthreads();
-    const unsigned w = s_word;
+    if (threadIdx.x == 0) {
+      const unsigned b = s_bits[p];
+      s_bits[p ^ 1] = 0u;
+      s_word[p] = grid_sync_rot(&sc->ctl, gridDim.x, round, b & 1u, b & 2u, timeout_ns);
+    }
+    __syncthreads();
+    const unsigned w = s_word[p];
     ++round;
     if ((w & BIT_ERROR) || (w & BIT_FAILED) || !(w & BIT_CHANGED) || (max_rounds > 0 && round >= max_rounds)) {
       if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -120,7 +129,6 @@ __global__ void __launch_bounds__(256, 4) k_fixpoint_static(const int *op, const
       }
       break;
     }
-    __syncthreads();
   }
   narrowed = warp_sum64(narrowed);
   if ((threadIdx.x & 31) == 0 && narrowed) atomicAdd(&s_narrowed, narrowed);

@@ -19,6 +19,7 @@ OK, FAILED, TIMEOUT, BARRIER_TIMEOUT, EINVAL, ECUDA, ENOMEM = range(7)
 STATUS = ["OK", "FAILED", "TIMEOUT", "BARRIER_TIMEOUT", "EINVAL", "ECUDA", "ENOMEM"]
 MODE_AUTO, MODE_PERSISTENT, MODE_HOSTLOOP, MODE_SMEM = range(4)
 SCHED_AC1, SCHED_LEARNED, SCHED_EVENTS = range(3)
+PERSISTENT_VARIANTS = 10  # PIR_PERSISTENT_VARIANTS
 INF = 2**31 - 1
 MINF = -2**31
 
@@ -226,7 +227,7 @@ class Context:
         self._check(rc, (OK, FAILED, TIMEOUT, BARRIER_TIMEOUT))
         return rc, s.asdict()
 
-    def autotune(self, rounds=16):
+    def autotune(self, rounds=64):
         """Times the persistent-kernel variants; returns (variant, us per round)."""
         v = ctypes.c_int32(0)
         us = ctypes.c_float(0)

@@ -55,3 +55,11 @@ def test_context_create_fails_cleanly_without_gpu():
     h = ctypes.c_void_p()
     rc = pirgpu.lib().pir_ctx_create(ctypes.byref(h), 0)
     assert rc == pirgpu.ECUDA and not h.value
+
+
+def test_python_constants_match_header():
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "lala-pc_gb300"))
+    import pirgpu
+    src = open(os.path.join(ROOT, "include", "pirgpu.h")).read()
+    assert int(re.search(r"#define PIR_PERSISTENT_VARIANTS (\d+)", src).group(1)) == pirgpu.PERSISTENT_VARIANTS
