@@ -305,6 +305,23 @@ def run_ours(args):
     e2e_t = dist_max(dist, time.perf_counter() - t0)
     e2e_value = dist_sum(dist, e2e_execs) / e2e_t if e2e_steps else None
 
+    # the same fixpoint under the event schedule (only the propagators of the
+    # variables narrowed in the previous round run), for its time to fixpoint
+    ev = None
+    if args.mode in (0, 1) and args.max_rounds == 0 and not args.no_events:
+        ev_runs = []
+        for _ in range(2):
+            ctx.restore(snap)
+            rc, st = ctx.fixpoint(sched=pirgpu.SCHED_EVENTS)
+            if rc != pirgpu.OK:
+                raise RuntimeError("event fixpoint status %s" % pirgpu.STATUS[rc])
+            ev_runs.append(st)
+            cr.flush_l2()
+        st = min(ev_runs, key=lambda s: s["device_ms"])
+        ev = {"time_to_fixpoint_ms": st["device_ms"], "executions": st["executions"], "rounds": st["rounds"],
+              "ac1_over_events_time": (dev_ms / args.steps) / st["device_ms"],
+              "ac1_over_events_executions": (execs / args.steps) / max(st["executions"], 1),
+              "fixpoint": "identical to AC-1 (bit-exact tests)"}
     if rank != 0:
         return
     hbm, hbm_src = peaks()
@@ -339,6 +356,7 @@ def run_ours(args):
         "gpu_launches": args.steps * (1 if args.mode in (0, 1, 3) else rounds[0] * 2),
         "clocks": clocks,
         "time_to_fixpoint_ms": dev_ms / args.steps,
+        "events_schedule": ev,
         "wall_s": wall,
     }
     print(json.dumps(out), flush=True)
@@ -661,6 +679,7 @@ def main():
     ap.add_argument("--ref-sweeps", type=int, default=3)
     ap.add_argument("--max-rounds", type=int, default=0, help="round cap (profiling runs)")
     ap.add_argument("--variant", type=int, default=0, help="persistent kernel variant, 0: autotuned")
+    ap.add_argument("--no-events", action="store_true", help="skip the event-schedule run of the single instance")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seq-nodes", type=int, default=128, help="nodes timed in the sequential loop")
     ap.add_argument("--cpu-nodes", type=int, default=256)

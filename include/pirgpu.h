@@ -58,8 +58,11 @@ enum pir_mode {
 enum pir_sched {
   PIR_SCHED_AC1 = 0,      /* every propagator every round (plain AC-1 sweeps) */
   PIR_SCHED_LEARNED = 1,  /* wake set chosen by the trained scorer, certified by a full sweep */
-  PIR_SCHED_EVENTS = 2    /* pir_fixpoint_nodes only, base store at its fixpoint: each round runs the
-                             propagators of the variables that changed in the previous round */
+  PIR_SCHED_EVENTS = 2    /* each round runs the propagators of the variables narrowed in the previous
+                             round (the first round runs all).  pir_fixpoint: one instance, rounds
+                             with at most opts.local_frontier propagators on one CTA;
+                             pir_fixpoint_nodes: one CTA per node, when the base store is at its
+                             fixpoint (else AC-1 rounds) */
 };
 
 /* Number of persistent-kernel variants (propagators per thread and step x CTAs
@@ -75,7 +78,8 @@ typedef struct pir_opts {
   int32_t sched;              /* enum pir_sched */
   float wake_fraction;        /* learned schedule: fraction of propagators woken per round (0: 1/16) */
   int32_t variant;            /* persistent kernel variant 1..PIR_PERSISTENT_VARIANTS (0: autotuned, else the default) */
-  int32_t reserved[6];
+  int32_t local_frontier;     /* event schedule: rounds of at most this many propagators run on one CTA (0: 256) */
+  int32_t reserved[5];
 } pir_opts;
 
 typedef struct pir_stats {

@@ -706,6 +706,16 @@ int ensure_events_graph(pirgpu_ctx *ctx, BatchState *b) {
   return PIR_OK;
 }
 
+int events_graph(pirgpu_ctx *ctx, const int4 **bc, const int **adj_ptr, const int **adj) {
+  BatchState *b = batch(ctx);
+  const int r = ensure_events_graph(ctx, b);
+  if (r) return r;
+  *bc = b->d_bc4;
+  *adj_ptr = b->d_adj_ptr;
+  *adj = b->d_adj;
+  return PIR_OK;
+}
+
 int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const int32_t *off, const int32_t *var,
                           const int32_t *lb, const int32_t *ub, const pir_opts &opts, int32_t *out_lb,
                           int32_t *out_ub, int32_t *out_status, int32_t *out_rounds, pir_stats *stats) {

@@ -558,6 +558,7 @@ int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
     return PIR_OK;
   }
   if (opts.sched == PIR_SCHED_LEARNED) return fixpoint_learned(ctx, opts, stats);
+  if (opts.sched == PIR_SCHED_EVENTS) return fixpoint_events(ctx, opts, stats);
   const long long max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
   const long long timeout = opts.barrier_timeout_ns > 0 ? opts.barrier_timeout_ns : 2000000000ll;
   Bytecode bc = bytecode_view(ctx);

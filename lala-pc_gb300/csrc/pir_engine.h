@@ -64,6 +64,7 @@ Bytecode bytecode_view(const pirgpu_ctx *ctx);
 void destroy_batch_state(pirgpu_ctx *ctx);
 void destroy_sched_state(pirgpu_ctx *ctx);
 int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);
+int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);
 // Records variables embedded since the last learned fixpoint (its "just
 // changed" feature).
 void note_embedded(pirgpu_ctx *ctx, const int32_t *var, int count);

@@ -23,7 +23,13 @@ struct Control {
   long long rounds;           // rounds executed (written by CTA 0)
   unsigned long long narrowed;
   unsigned long long executions;
-  unsigned long long pad[10];
+  // event-driven fixpoint: the CTA that runs small rounds alone publishes a
+  // heartbeat (rounds done), the round it stopped at and why (EV_*)
+  unsigned long long hb;
+  long long ev_round;
+  int ev_state;
+  int pad_i;
+  unsigned long long pad[7];
 };
 
 constexpr unsigned BIT_CHANGED = 1u << 29;
@@ -65,21 +71,31 @@ static __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned
 // after the zeroing) is seen by every CTA before it can arrive at r + 2.  The
 // three words start at zero (the host clears the control block).  Every wait is
 // bounded by timeout_ns; on expiry the CTA records PIR_BARRIER_TIMEOUT in
-// ctl->status and the result carries BIT_ERROR.
+// ctl->status and the result carries BIT_ERROR.  With a heartbeat word `hb`
+// (a CTA working alone while the others wait), the limit runs from the last
+// change of *hb, and the waiters poll less often.
 static __device__ __noinline__ unsigned grid_sync_rot(Control *ctl, unsigned nblocks, long long round, int changed,
-                                                      int failed, long long timeout_ns) {
+                                                      int failed, long long timeout_ns,
+                                                      const unsigned long long *hb = nullptr) {
   unsigned long long *w = &ctl->rot[round % 3][0];
   const unsigned long long add =
       1ull | ((unsigned long long)(changed != 0) << 20) | ((unsigned long long)(failed != 0) << 40);
   unsigned long long v = atom_add_release(w, add) + add;
   if ((unsigned)(v & 0xFFFFFull) != nblocks) {
-    const unsigned long long t0 = globaltimer();
+    unsigned long long t0 = globaltimer(), beat = hb ? *(const volatile unsigned long long *)hb : 0ull;
     for (unsigned it = 0;; ++it) {
       v = ld_acquire64(w);
       if ((unsigned)(v & 0xFFFFFull) == nblocks) break;
-      if (it >= 64) __nanosleep(it < 512 ? 20 : 200);
+      if (it >= 64) __nanosleep(hb ? 1000 : (it < 512 ? 20 : 200));
       if ((it & 7u) == 0u) {
         if (*(volatile int *)&ctl->status) return BIT_ERROR;
+        if (hb) {
+          const unsigned long long b = *(const volatile unsigned long long *)hb;
+          if (b != beat) {
+            beat = b;
+            t0 = globaltimer();
+          }
+        }
         if ((long long)(globaltimer() - t0) > timeout_ns) {
           atomicCAS(&ctl->status, 0, ERR_BARRIER_TIMEOUT);
           return BIT_ERROR;

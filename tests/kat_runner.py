@@ -102,6 +102,7 @@ class GpuEngine:
     """The CUDA engine through the C ABI behind the engine interface."""
 
     mode = 0  # pirgpu.MODE_AUTO; set per test
+    sched = 0  # pirgpu.SCHED_AC1; set per test
 
     def __init__(self, lb, ub):
         import pirgpu
@@ -121,7 +122,7 @@ class GpuEngine:
         return self.ctx.num_deductions()
 
     def fixpoint(self):
-        rc, _ = self.ctx.fixpoint(mode=self.mode)
+        rc, _ = self.ctx.fixpoint(mode=self.mode, sched=self.sched)
         return rc == self.P.FAILED
 
     def read(self):
