@@ -88,7 +88,9 @@ class Cudart:
 
 # ------------------------------------------------------------------ clocks --
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms.  start() returns
+    once the first sample is in (nvidia-smi takes a while to start); a timed
+    region shorter than the interval gets the sample taken right after it."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -102,12 +104,17 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t0 = time.time()
+        while not self.lines and time.time() - t0 < 3.0 and self.proc.poll() is None:
+            time.sleep(0.005)
+        self.n0 = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -116,6 +123,11 @@ class ClockSampler:
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        t0 = time.time()
+        while len(self.lines) <= self.n0 and time.time() - t0 < 1.0 and self.proc.poll() is None:
+            time.sleep(0.005)
+        in_region = max(0, len(self.lines) - self.n0)
+        self.lines = self.lines[max(0, self.n0 - 1):]  # the last sample before the region and the ones after
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -137,7 +149,8 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "interval_ms": 50,
+                "samples_after_start": in_region}
 
 
 def peaks():
@@ -440,12 +453,20 @@ def run_nodes(args):
         ctx.restore(snap)
         seq_dev_rate = sample / seq_dev
         seq_wall_rate = sample / seq_wall
-    # end to end: host tightenings in, node stores out
-    e2e_t = None
+    # end to end through the C ABI: host tightenings in, per-node status and
+    # rounds out (what a search driver reads; the sequential loop reads the
+    # same), and separately with every node's store downloaded as well
+    e2e_t = e2e_stores_t = None
     if extras and not args.no_e2e:
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=sched)
+            ts.append(time.perf_counter() - t0)
+        e2e_t = min(ts)
         t0 = time.perf_counter()
         ctx.fixpoint_nodes(off, var, lb, ub, want_stores=True, sched=sched)
-        e2e_t = time.perf_counter() - t0
+        e2e_stores_t = time.perf_counter() - t0
     hbm, hbm_src = peaks()
     achieved = (execs * ALG_BYTES_PER_EXEC + joins * ALG_BYTES_PER_JOIN) / dev_s / 1e9
     cpu = None
@@ -483,7 +504,9 @@ def run_nodes(args):
         "cpu_baseline": cpu,
         "e2e": {"value": nn_all / e2e_t if e2e_t else None, "unit": "nodes/s",
                 "h2d_bytes_per_step": int(len(var) * 12 + len(off) * 4),
-                "d2h_bytes_per_step": int(nn * len(blb) * 8)},
+                "d2h_bytes_per_step": int(nn * 8),
+                "with_stores": {"value": nn_all / e2e_stores_t if e2e_stores_t else None,
+                                "d2h_bytes_per_step": int(nn * len(blb) * 8)}},
         "gpu_launches": args.steps, "clocks": clocks,
     }
     print(json.dumps(out), flush=True)
