@@ -58,17 +58,22 @@ struct BatchState {
   long long ev_version = -1;
   int4 *d_bc4 = nullptr;
   int *d_adj_ptr = nullptr, *d_adj = nullptr;
-  int ev_grid = 0, ev_nvars = 0;
+  int ev_slots = 0, ev_nvars = 0;  // per-CTA scratch slots allocated (grid <= slots)
   long long ev_n = 0;
   void *d_ev = nullptr;  // per-CTA scratch block
   size_t cap_ev = 0;
+  long long ev_base_version = -1;  // store version the first ev_valid_slots working stores equal
+  int ev_valid_slots = 0;
+  unsigned char *d_ent = nullptr;  // entailed-at-base flags per propagator
+  size_t cap_ent = 0;
+  long long ent_store_version = -1, ent_bc_version = -1;
 };
 
 void destroy_batch_state(pirgpu_ctx *ctx) {
   BatchState *b = ctx->batch;
   if (!b) return;
   void *ptrs[] = {b->d_bc, b->d_off,    b->d_store, b->d_aux,     b->d_iout, b->d_nstore, b->d_tight,
-                  b->d_nout, b->d_nio, b->d_bc4, b->d_adj_ptr, b->d_adj, b->d_ev};
+                  b->d_nout, b->d_nio, b->d_bc4, b->d_adj_ptr, b->d_adj, b->d_ev, b->d_ent};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete b;
@@ -473,26 +478,40 @@ __global__ void __launch_bounds__(512) k_nodes(NodeArgs a) {
 // run is at its fixpoint, so when a round leaves no variable changed the
 // store is the node's fixpoint, the one AC-1 rounds reach.
 //
-// Each CTA keeps one working store (equal to the base between nodes: after a
-// node only the variables it touched are put back), and dedups candidate
-// propagators and changed variables with epoch stamps (a per-CTA counter that
-// only grows, so the stamp arrays are never cleared).
+// Propagators entailed at the base store (ask, pir.hpp:417-438) are skipped:
+// entailment survives narrowing and an entailed propagator narrows nothing
+// (both checked exhaustively against the oracle), so they cannot change a
+// node's fixpoint -- lala-pc's FixpointSubset idea (pir.hpp:874-884).
+//
+// Each CTA keeps one working store, equal to the base between nodes (after a
+// node only the variables it touched are put back) and between launches while
+// the base store does not change, so it is copied only when it did.  Within a
+// round, the expansion of the changed variables' adjacency is spread over the
+// whole CTA (block scan of the degrees), and candidates, changed variables and
+// touched variables are deduplicated in shared-memory hash sets; a set whose
+// probe window is full falls back to epoch stamps in global memory for that
+// key (a key takes the same path for as long as its set is not cleared).
+
+constexpr int NODE_BLOCK = 256;
+constexpr int CAND_LOG = 11, CHG_LOG = 10, TOUCH_LOG = 11, MAX_PROBE = 16;
 
 struct EvArgs {
   const int4 *bc;  // (op, x, y, z) per propagator, engine order
   long long n;
   int nvars;
   const int *adj_ptr, *adj;
+  const unsigned char *ent;  // per propagator: entailed at the base store (skipped)
   const int2 *base;
+  int copy_base;    // the working stores must be (re)loaded from the base
   int2 *out_store;  // node-major nnodes x nvars, or nullptr
   const int *off, *var, *lb, *ub;
   int nnodes;
   int *next;
   int2 *ws;          // grid x nvars
-  unsigned *vmark;   // grid x nvars: epoch a variable last entered a changed list
-  unsigned *tmark;   // grid x nvars: node tag a variable last entered the touched list
+  unsigned *vmark;   // grid x nvars: epoch a variable last entered a changed list (fallback)
+  unsigned *tmark;   // grid x nvars: node tag a variable last entered the touched list (fallback)
   int *lists;        // grid x 3 x nvars: changed lists (2) and the touched list
-  unsigned *pstamp;  // grid x n: epoch a propagator last became a candidate
+  unsigned *pstamp;  // grid x n: epoch a propagator last became a candidate (fallback)
   int *cand;         // grid x n
   unsigned *epochs;  // grid
   NodeOut *out;
@@ -500,15 +519,48 @@ struct EvArgs {
   long long max_rounds;
 };
 
-struct EvStore {
+// Insert `key` into the shared-memory set tab[1 << LOG] (-1 = free): 1 newly
+// inserted, 0 already there, -1 no free slot within MAX_PROBE (Fibonacci
+// hashing, linear probing).
+template <int LOG>
+__device__ __forceinline__ int set_insert(int *tab, int key) {
+  unsigned h = ((unsigned)key * 2654435761u) >> (32 - LOG);
+  for (int i = 0; i < MAX_PROBE; ++i) {
+    const int prev = atomicCAS(tab + h, -1, key);
+    if (prev == -1) return 1;
+    if (prev == key) return 0;
+    h = (h + 1) & ((1u << LOG) - 1u);
+  }
+  return -1;
+}
+
+template <int LOG>
+__device__ __forceinline__ void set_clear(int *tab) {
+  for (int i = threadIdx.x; i < (1 << LOG); i += blockDim.x) tab[i] = -1;
+}
+
+struct NodeEvStore {
   int2 *ws;
   unsigned *vmark, *tmark;
   int *dnext, *touched;
-  int *nd, *nt;  // shared-memory counters
+  int *nd, *nt;              // shared-memory counters
+  int *chg_set, *touch_set;  // shared-memory sets
   unsigned epoch, tag;
   __device__ __forceinline__ Itv load(int v) const {
     const int2 t = __ldcg(ws + v);
     return mk(t.x, t.y);
+  }
+  // v narrowed: first time this round -> next changed list; first time this
+  // node -> touched list
+  __device__ __forceinline__ void note(int v) const {
+    int c = set_insert<CHG_LOG>(chg_set, v);
+    if (c < 0) c = atomicMax(vmark + v, epoch) < epoch ? 1 : 0;
+    if (c > 0) {
+      dnext[atomicAdd(nd, 1)] = v;
+      int t = set_insert<TOUCH_LOG>(touch_set, v);
+      if (t < 0) t = atomicExch(tmark + v, tag) != tag ? 1 : 0;
+      if (t > 0) touched[atomicAdd(nt, 1)] = v;
+    }
   }
   __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
     int n = 0;
@@ -521,51 +573,84 @@ struct EvStore {
       ++n;
     }
     if (n) {
-      if (atomicMax(vmark + v, epoch) < epoch) dnext[atomicAdd(nd, 1)] = v;
-      if (atomicExch(tmark + v, tag) != tag) touched[atomicAdd(nt, 1)] = v;
+      note(v);
       if (is_bot(mk(max(seen.l, r.l), min(seen.u, r.u)))) failed = 1;
     }
     return n;
   }
 };
 
-__global__ void __launch_bounds__(1024) k_nodes_events(EvArgs a) {
+// Inclusive prefix sum of `x` over the CTA (blockDim.x a multiple of 32,
+// at most NODE_BLOCK); s_warp holds 32 ints.
+__device__ __forceinline__ int block_scan_incl(int x, int *s_warp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    int w = lane < nw ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nw) s_warp[lane] = w;
+  }
+  __syncthreads();
+  const int r = x + (warp ? s_warp[warp - 1] : 0);
+  __syncthreads();
+  return r;
+}
+
+// MINB: resident CTAs per SM the register budget is sized for (more nodes in
+// flight against fewer registers per thread).
+template <int MINB>
+__global__ void __launch_bounds__(NODE_BLOCK, MINB) k_nodes_events(EvArgs a) {
   __shared__ int s_node, s_ncand, s_nd[2], s_nt;
+  __shared__ int s_cand_set[1 << CAND_LOG], s_chg_set[1 << CHG_LOG], s_touch_set[1 << TOUCH_LOG];
+  __shared__ int s_beg[NODE_BLOCK], s_end[NODE_BLOCK], s_warp[32];
   const size_t nv = (size_t)a.nvars;
+  const int tid = threadIdx.x;
   int2 *ws = a.ws + blockIdx.x * nv;
   unsigned *vmark = a.vmark + blockIdx.x * nv, *tmark = a.tmark + blockIdx.x * nv;
-  int *dl[2] = {a.lists + blockIdx.x * 3 * nv, a.lists + blockIdx.x * 3 * nv + nv};
+  int *const dl0 = a.lists + blockIdx.x * 3 * nv, *const dl1 = dl0 + nv;  // changed lists
   int *touched = a.lists + blockIdx.x * 3 * nv + 2 * nv;
   unsigned *pstamp = a.pstamp + blockIdx.x * (size_t)a.n;
   int *cand = a.cand + blockIdx.x * (size_t)a.n;
   unsigned epoch = a.epochs[blockIdx.x];
-  for (size_t v = threadIdx.x; v < nv; v += blockDim.x) ws[v] = a.base[v];
+  if (a.copy_base)
+    for (size_t v = tid; v < nv; v += blockDim.x) ws[v] = a.base[v];
   unsigned long long execs = 0, narrowed = 0;
   __syncthreads();
   for (;;) {
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
       s_node = atomicAdd(a.next, 1);
       s_nd[0] = s_nd[1] = 0;
       s_nt = 0;
     }
+    set_clear<CHG_LOG>(s_chg_set);
+    set_clear<TOUCH_LOG>(s_touch_set);
     __syncthreads();
     const int node = s_node;
     if (node >= a.nnodes) break;
     ++epoch;
     const unsigned tag = epoch;
+    NodeEvStore st{ws, vmark, tmark, dl0, touched, &s_nd[0], &s_nt, s_chg_set, s_touch_set, epoch, tag};
     // tightenings: meets, the changed ones start the first changed list
     int f = 0;
     const int k0 = a.off[node], k1 = a.off[node + 1];
-    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+    for (int k = k0 + tid; k < k1; k += blockDim.x) {
       const int v = a.var[k];
       const int ol = atomicMax(&ws[v].x, a.lb[k]), ou = atomicMin(&ws[v].y, a.ub[k]);
-      if (ol < a.lb[k] || ou > a.ub[k]) {
-        if (atomicMax(vmark + v, epoch) < epoch) dl[0][atomicAdd(&s_nd[0], 1)] = v;
-        if (atomicExch(tmark + v, tag) != tag) touched[atomicAdd(&s_nt, 1)] = v;
-      }
+      if (ol < a.lb[k] || ou > a.ub[k]) st.note(v);
     }
     __syncthreads();
-    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+    for (int k = k0 + tid; k < k1; k += blockDim.x) {
       const int2 t = __ldcg(ws + a.var[k]);
       f |= is_bot(mk(t.x, t.y));
     }
@@ -581,58 +666,91 @@ __global__ void __launch_bounds__(1024) k_nodes_events(EvArgs a) {
       }
       ++round;
       ++epoch;
-      __syncthreads();
-      if (threadIdx.x == 0) {
+      if (tid == 0) {
         s_ncand = 0;
         s_nd[cur ^ 1] = 0;
       }
+      set_clear<CAND_LOG>(s_cand_set);
+      set_clear<CHG_LOG>(s_chg_set);
       __syncthreads();
-      // candidates: propagators adjacent to the variables changed last round
+      // candidates: the non-entailed propagators adjacent to the variables
+      // changed last round, the adjacency spread over the CTA
       const int nd = s_nd[cur];
-      for (int i = threadIdx.x; i < nd; i += blockDim.x) {
-        const int v = dl[cur][i];
-        for (int q = __ldg(a.adj_ptr + v), qe = __ldg(a.adj_ptr + v + 1); q < qe; ++q) {
-          const int p = __ldg(a.adj + q);
-          if (atomicMax(pstamp + p, epoch) < epoch) cand[atomicAdd(&s_ncand, 1)] = p;
+      for (int c0 = 0; c0 < nd; c0 += blockDim.x) {
+        const int i = c0 + tid;
+        int beg = 0, deg = 0;
+        if (i < nd) {
+          const int v = (cur ? dl1 : dl0)[i];
+          beg = __ldg(a.adj_ptr + v);
+          deg = __ldg(a.adj_ptr + v + 1) - beg;
         }
+        const int incl = block_scan_incl(deg, s_warp);
+        s_beg[tid] = beg;
+        s_end[tid] = incl;
+        __syncthreads();
+        const int total = s_end[blockDim.x - 1];
+        for (int j = tid; j < total; j += blockDim.x) {
+          int lo = 0, hi = (int)blockDim.x - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (s_end[mid] > j) hi = mid;
+            else lo = mid + 1;
+          }
+          const int first = lo ? s_end[lo - 1] : 0;
+          const int p = __ldg(a.adj + s_beg[lo] + (j - first));
+          if (a.ent && a.ent[p]) continue;
+          int c = set_insert<CAND_LOG>(s_cand_set, p);
+          if (c < 0) c = atomicMax(pstamp + p, epoch) < epoch ? 1 : 0;
+          if (c > 0) cand[atomicAdd(&s_ncand, 1)] = p;
+        }
+        __syncthreads();
       }
-      __syncthreads();
-      EvStore st{ws, vmark, tmark, dl[cur ^ 1], touched, &s_nd[cur ^ 1], &s_nt, epoch, tag};
+      NodeEvStore rs{ws, vmark, tmark, cur ? dl0 : dl1, touched, &s_nd[cur ^ 1], &s_nt, s_chg_set, s_touch_set,
+                     epoch, tag};
       const int nc = s_ncand;
       int f2 = 0;
-      for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+      for (int i = tid; i < nc; i += blockDim.x) {
         const int4 b = __ldg(a.bc + cand[i]);
-        const Itv ia = st.load(b.y), ib = st.load(b.z), ic = st.load(b.w);
-        narrowed += deduce_loaded(b.x, b.y, b.z, b.w, ia, ib, ic, st, f2);
+        const Itv ia = rs.load(b.y), ib = rs.load(b.z), ic = rs.load(b.w);
+        narrowed += deduce_loaded(b.x, b.y, b.z, b.w, ia, ib, ic, rs, f2);
         ++execs;
       }
       failed = __syncthreads_or(f2);
       cur ^= 1;
     }
     if (failed) status = PIR_FAILED;
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
       a.out[node].status = status;
       a.out[node].rounds = (int)round;
     }
     if (a.out_store) {
       int2 *dst = a.out_store + (size_t)node * nv;
-      for (size_t v = threadIdx.x; v < nv; v += blockDim.x) dst[v] = __ldcg(ws + v);
+      for (size_t v = tid; v < nv; v += blockDim.x) dst[v] = __ldcg(ws + v);
     }
     __syncthreads();
     // put the touched variables back to the base store
     const int nt = s_nt;
-    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+    for (int i = tid; i < nt; i += blockDim.x) {
       const int v = touched[i];
       ws[v] = a.base[v];
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) a.epochs[blockIdx.x] = epoch;
+  if (tid == 0) a.epochs[blockIdx.x] = epoch;
   execs = warp_sum64(execs);
   narrowed = warp_sum64(narrowed);
-  if ((threadIdx.x & 31) == 0) {
+  if ((tid & 31) == 0) {
     if (execs) atomicAdd(a.execs, execs);
     if (narrowed) atomicAdd(a.narrowed, narrowed);
+  }
+}
+
+// Entailment of every propagator at the base store (engine-order AoS bytecode).
+__global__ void k_entailed(const int4 *bc, long long n, const int2 *store, unsigned char *ent) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const int4 b = __ldg(bc + p);
+    const int2 x = store[b.y], y = store[b.z], z = store[b.w];
+    ent[p] = b.x != OP_NOP && ask(b.x, mk(x.x, x.y), mk(y.x, y.y), mk(z.x, z.y)) ? 1 : 0;
   }
 }
 
@@ -721,29 +839,40 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
                           int32_t *out_ub, int32_t *out_status, int32_t *out_rounds, pir_stats *stats) {
   int r;
   if ((r = ensure_events_graph(ctx, b))) return r;
-  const int block = opts.block > 0 ? std::min(std::max(opts.block / 32 * 32, 32), 1024) : 256;
+  const int block = NODE_BLOCK;
+  // variant 1..5: the kernel sized for 2, 3, 4, 6, 8 resident CTAs per SM
+  static const void *const kNodeVariants[] = {(const void *)k_nodes_events<2>, (const void *)k_nodes_events<3>,
+                                              (const void *)k_nodes_events<4>, (const void *)k_nodes_events<6>,
+                                              (const void *)k_nodes_events<8>};
+  const int nvar = opts.variant >= 1 && opts.variant <= 5 ? opts.variant : 5;
+  const void *kfn = kNodeVariants[nvar - 1];
   int occ = 0;
-  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nodes_events, block, 0));
+  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, block, 0));
   occ = std::max(occ, 1);
   const int grid = std::max(1, std::min(nnodes, ctx->num_sms * (opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ)));
   const size_t nv = (size_t)ctx->nvars, n = (size_t)std::max<long long>(ctx->n, 1);
-  // per-CTA scratch: ws | vmark | tmark | lists(3) | pstamp | cand | epochs
+  // per-CTA scratch slots: ws | vmark | tmark | lists(3) | pstamp | cand | epochs
   const size_t per_cta = nv * 8 + nv * 4 * 2 + nv * 4 * 3 + n * 4 * 2;
-  const size_t need = per_cta * (size_t)grid + 64 * (size_t)grid + 256;
-  if (b->cap_ev < need || b->ev_grid != grid || b->ev_nvars != ctx->nvars || b->ev_n != ctx->n) {
+  if (b->ev_slots < grid || b->ev_nvars != ctx->nvars || b->ev_n != ctx->n) {
+    const int slots = std::max(grid, ctx->num_sms * occ);
+    const size_t need = per_cta * (size_t)slots + 64 * (size_t)slots + 256;
     if (b->d_ev) cudaFree(b->d_ev);
     b->d_ev = nullptr;
     b->cap_ev = 0;
+    b->ev_slots = 0;
+    b->ev_valid_slots = 0;
+    b->ev_base_version = -1;
     if (cudaMalloc(&b->d_ev, need) != cudaSuccess) {
       cudaGetLastError();
       return set_err(ctx, PIR_ENOMEM, "event scratch (%zu bytes)", need);
     }
     b->cap_ev = need;
-    b->ev_grid = grid;
+    b->ev_slots = slots;
     b->ev_nvars = ctx->nvars;
     b->ev_n = ctx->n;
     PIR_CK(cudaMemsetAsync(b->d_ev, 0, need, ctx->stream));  // stamps and epochs start at 0
   }
+  const size_t slots = (size_t)b->ev_slots;
   char *base = (char *)b->d_ev;
   EvArgs a;
   a.bc = b->d_bc4;
@@ -752,19 +881,25 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
   a.adj_ptr = b->d_adj_ptr;
   a.adj = b->d_adj;
   a.base = ctx->d_store;
+  // the working stores equal the base unless the store changed since they were loaded
+  a.copy_base = (b->ev_base_version != ctx->store_version || b->ev_valid_slots < grid) ? 1 : 0;
   a.ws = (int2 *)base;
-  base += (size_t)grid * nv * 8;
+  base += slots * nv * 8;
   a.vmark = (unsigned *)base;
-  base += (size_t)grid * nv * 4;
+  base += slots * nv * 4;
   a.tmark = (unsigned *)base;
-  base += (size_t)grid * nv * 4;
+  base += slots * nv * 4;
   a.lists = (int *)base;
-  base += (size_t)grid * nv * 12;
+  base += slots * nv * 12;
   a.pstamp = (unsigned *)base;
-  base += (size_t)grid * n * 4;
+  base += slots * n * 4;
   a.cand = (int *)base;
-  base += (size_t)grid * n * 4;
+  base += slots * n * 4;
   a.epochs = (unsigned *)base;
+  // propagators entailed at the base store
+  if ((r = ensure(ctx, (void **)&b->d_ent, &b->cap_ent, n))) return r;
+  const bool need_ent = b->ent_store_version != ctx->store_version || b->ent_bc_version != ctx->bytecode_version;
+  a.ent = b->d_ent;
   // tightenings, counters, outputs
   const int ntight = off[nnodes];
   if ((r = ensure(ctx, (void **)&b->d_tight, &b->cap_tight, ((size_t)nnodes + 1 + 3 * (size_t)ntight + 8) * sizeof(int))))
@@ -799,7 +934,14 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
   a.narrowed = d_cnt + 1;
   a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
   PIR_CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  k_nodes_events<<<grid, block, 0, ctx->stream>>>(a);
+  if (need_ent) {
+    k_entailed<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(b->d_bc4, ctx->n, ctx->d_store, b->d_ent);
+    PIR_CK(cudaGetLastError());
+  }
+  {
+    void *kargs[] = {&a};
+    PIR_CK(cudaLaunchKernel(kfn, dim3(grid), dim3(block), kargs, 0, ctx->stream));
+  }
   PIR_CK(cudaGetLastError());
   PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   std::vector<NodeOut> hout(nnodes);
@@ -823,6 +965,14 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
     }
   }
   PIR_CK(cudaStreamSynchronize(ctx->stream));
+  // every node put its touched variables back: the first `grid` working stores
+  // (all of them when this launch loaded them) equal the base store
+  if (a.copy_base) {
+    b->ev_base_version = ctx->store_version;
+    b->ev_valid_slots = grid;
+  }
+  b->ent_store_version = ctx->store_version;
+  b->ent_bc_version = ctx->bytecode_version;
   pir_stats st;
   std::memset(&st, 0, sizeof(st));
   PIR_CK(cudaEventElapsedTime(&st.device_ms, ctx->ev0, ctx->ev1));

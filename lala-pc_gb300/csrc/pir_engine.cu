@@ -320,6 +320,7 @@ int upload_bytecode(pirgpu_ctx *ctx) {
 int apply_meets(pirgpu_ctx *ctx, const std::vector<int> &var, const std::vector<int> &lb,
                 const std::vector<int> &ub, int *changed) {
   const int count = (int)var.size();
+  ++ctx->store_version;
   if (changed) *changed = 0;
   if (count == 0) return PIR_OK;
   int r;
@@ -390,6 +391,7 @@ void pir_ctx_destroy(pirgpu_ctx *ctx) {
 const char *pir_last_error(const pirgpu_ctx *ctx) { return ctx ? ctx->err : "no context"; }
 
 int pir_load_store(pirgpu_ctx *ctx, int32_t nvars, const int32_t *lb, const int32_t *ub) {
+  if (ctx) ++ctx->store_version;
   if (!ctx) return PIR_EINVAL;
   if (nvars < 0 || (nvars > 0 && (!lb || !ub))) return set_err(ctx, PIR_EINVAL, "bad store arguments");
   if (nvars < ctx->max_var_used + 1) return set_err(ctx, PIR_EINVAL, "store smaller than the variables used by the bytecode");
@@ -557,6 +559,7 @@ int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
     if (stats) *stats = st;
     return PIR_OK;
   }
+  ++ctx->store_version;
   if (opts.sched == PIR_SCHED_LEARNED) return fixpoint_learned(ctx, opts, stats);
   if (opts.sched == PIR_SCHED_EVENTS) return fixpoint_events(ctx, opts, stats);
   const long long max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
@@ -644,6 +647,7 @@ int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
 }
 
 int pir_autotune(pirgpu_ctx *ctx, int32_t rounds, int32_t *out_variant, float *out_us_per_round) {
+  if (ctx) ++ctx->store_version;
   if (!ctx) return PIR_EINVAL;
   if (out_variant) *out_variant = 0;
   if (out_us_per_round) *out_us_per_round = 0.f;
@@ -702,6 +706,7 @@ int pir_autotune(pirgpu_ctx *ctx, int32_t rounds, int32_t *out_variant, float *o
 }
 
 int pir_deduce_one(pirgpu_ctx *ctx, int64_t i, int *changed) {
+  if (ctx) ++ctx->store_version;
   if (!ctx) return PIR_EINVAL;
   if (i < 0 || i >= ctx->n) return set_err(ctx, PIR_EINVAL, "deduce(%lld) out of range", (long long)i);
   CK(cudaSetDevice(ctx->device));
@@ -836,6 +841,7 @@ int pir_snapshot(pirgpu_ctx *ctx, pirgpu_snapshot **out) {
 }
 
 int pir_restore(pirgpu_ctx *ctx, const pirgpu_snapshot *snap) {
+  if (ctx) ++ctx->store_version;
   if (!ctx || !snap) return PIR_EINVAL;
   if (snap->nvars != ctx->nvars) return set_err(ctx, PIR_EINVAL, "snapshot has %d vars, store has %d", snap->nvars, ctx->nvars);
   if (snap->n > ctx->n) return set_err(ctx, PIR_EINVAL, "snapshot has more propagators than the context");

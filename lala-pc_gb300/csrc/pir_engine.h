@@ -35,6 +35,7 @@ struct pirgpu_ctx {
   long long n = 0;
   int max_var_used = -1;
   long long bytecode_version = 0;
+  long long store_version = 0;  // bumped by every call that may change d_store (caches key on it)
   std::vector<int> h_op, h_x, h_y, h_z;
   int *d_op = nullptr, *d_x = nullptr, *d_y = nullptr, *d_z = nullptr;
   size_t cap_op = 0, cap_x = 0, cap_y = 0, cap_z = 0;

@@ -58,7 +58,11 @@ __device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
 // Store policy: joins as RedStore does; the first narrowing of a variable in
 // round r lists its propagators for round r + 1 (the round stamps keep every
 // variable expanded, and every propagator listed, at most once per round).
-// List slots are taken with one atomic per group of converged lanes.
+// The adjacency is walked EXPAND entries at a time: their loads and stamp
+// atomics are independent (one memory round trip each per batch, not per
+// entry), and the batch takes its list slots with one atomic.
+constexpr int EXPAND = 8;
+
 struct EvStore {
   int2 *s;
   const int *adj_ptr, *adj;
@@ -73,19 +77,19 @@ struct EvStore {
   __device__ __forceinline__ void schedule(int v) const {
     if (atomicMax(vstamp + v, next_round) >= next_round) return;
     const int b = __ldg(adj_ptr + v), e = __ldg(adj_ptr + v + 1);
-    const int lane = threadIdx.x & 31;
-    for (int k = b; k < e; ++k) {
-      const int q = __ldg(adj + k);
-      const bool take = atomicMax(pstamp + q, next_round) < next_round;
-      const unsigned active = __activemask();
-      const unsigned m = __ballot_sync(active, take);
-      if (m) {
-        const int leader = __ffs(m) - 1;
-        unsigned base = 0;
-        if (lane == leader) base = atomicAdd(next_cnt, (unsigned)__popc(m));
-        base = __shfl_sync(active, base, leader);
-        if (take) next[base + __popc(m & ((1u << lane) - 1u))] = q;
-      }
+    for (int k0 = b; k0 < e; k0 += EXPAND) {
+      int q[EXPAND];
+#pragma unroll
+      for (int j = 0; j < EXPAND; ++j) q[j] = k0 + j < e ? __ldg(adj + k0 + j) : -1;
+      unsigned take = 0;
+#pragma unroll
+      for (int j = 0; j < EXPAND; ++j)
+        if (q[j] >= 0 && atomicMax(pstamp + q[j], next_round) < next_round) take |= 1u << j;
+      if (!take) continue;
+      unsigned slot = atomicAdd(next_cnt, (unsigned)__popc(take));
+#pragma unroll
+      for (int j = 0; j < EXPAND; ++j)
+        if (take & (1u << j)) next[slot++] = q[j];
     }
   }
   __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {

@@ -616,6 +616,7 @@ extern "C" int pir_sched_collect(pirgpu_ctx *ctx, int32_t nnodes, const int32_t 
                                  int64_t *out_samples, int64_t *out_positives) {
   if (!ctx || nnodes < 0 || max_samples <= 0 || (nnodes > 0 && (!off || !var || !lb || !ub)))
     return PIR_EINVAL;
+  ++ctx->store_version;  // the store is used as scratch and put back
   for (int j = 0; j < nnodes; ++j)
     if (off[j + 1] < off[j]) return set_err(ctx, PIR_EINVAL, "node offsets decrease");
   for (int k = 0; k < (nnodes ? off[nnodes] : 0); ++k)

@@ -36,6 +36,8 @@ def lib():
         L.orc_deduce.argtypes = [i32, i32, i32, i32, _I32P, ctypes.POINTER(ctypes.c_int)]
         L.orc_ask.argtypes = [i32, i32, i32, i32, _I32P]
         _U8P = ctypes.POINTER(ctypes.c_uint8)
+        L.orc_ask_batch.argtypes = [i64, _I32P, _I32P, _I32P, _U8P]
+        L.orc_ask_batch.restype = None
         L.orc_deduce_batch.argtypes = [i64, _I32P, _I32P, _I32P, _I32P, _I32P, _U8P, _U8P, _I64P]
         L.orc_deduce_batch.restype = None
         L.orc_store_is_bot.argtypes = [i32, _I32P]
@@ -175,6 +177,16 @@ def deduce_batch(op, in_lb, in_ub):
 
 def ask(op, x, y, z, store):
     return bool(lib().orc_ask(op, x, y, z, _p32(store)))
+
+
+def ask_batch(op, in_lb, in_ub):
+    """ask(bytecode) of op[k] over private intervals in_lb/in_ub[k, 0:3]."""
+    op = _c32(op)
+    in_lb, in_ub = _c32(in_lb).reshape(-1, 3), _c32(in_ub).reshape(-1, 3)
+    out = np.empty(len(op), np.uint8)
+    lib().orc_ask_batch(len(op), _p32(op), _p32(in_lb), _p32(in_ub),
+                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    return out.astype(bool)
 
 
 def ask_all(op, x, y, z, store):

@@ -678,6 +678,21 @@ int orc_ask(int32_t op, int32_t x, int32_t y, int32_t z, const int32_t *store) {
   return ask(op, x, y, z, store);
 }
 
+// ask(bytecode) (pir.hpp:417-438) of op[k] over the private intervals in_lb/in_ub[k][0..2].
+void orc_ask_batch(int64_t count, const int32_t *op, const int32_t *in_lb, const int32_t *in_ub, uint8_t *out) {
+  const i64 chunk = 1 << 16;
+  parallel_for((count + chunk - 1) / chunk, resolve_threads(0), [&](i64 c) {
+    for (i64 k = c * chunk; k < std::min(count, (c + 1) * chunk); ++k) {
+      i32 s[6];
+      for (int j = 0; j < 3; ++j) {
+        s[2 * j] = in_lb[3 * k + j];
+        s[2 * j + 1] = in_ub[3 * k + j];
+      }
+      out[k] = orc_ask(op[k], 0, 1, 2, s) ? 1 : 0;
+    }
+  });
+}
+
 void orc_deduce_batch(int64_t count, const int32_t *op, const int32_t *in_lb, const int32_t *in_ub,
                       int32_t *out_lb, int32_t *out_ub, uint8_t *out_changed, uint8_t *out_failed,
                       int64_t *overflows) {

@@ -141,6 +141,56 @@ def test_nodes_events_parity(seed, P, oracle):
     np.testing.assert_array_equal(l2[ok], olb[ok])
 
 
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5])
+def test_nodes_events_variants(variant, P, oracle):
+    """The event node kernel sized for 2, 3, 4, 6 and 8 resident CTAs per SM."""
+    ctx, (blb, bub), off, var, lb, ub = _nodes_setup(P, seed=4, nnodes=300)
+    status, olb, oub, _, _ = ctx.fixpoint_nodes(off, var, lb, ub, sched=P.SCHED_EVENTS, variant=variant)
+    op, x, y, z = ctx.bytecode()
+    base = np.ascontiguousarray(np.stack([blb, bub], 1))
+    ostatus, ostore, _ = oracle.fixpoint_nodes(op, x, y, z, base, off, var, lb, ub)
+    np.testing.assert_array_equal(status, ostatus)
+    ok = ostatus == oracle.OK
+    np.testing.assert_array_equal(olb[ok], ostore[ok, :, 0])
+    np.testing.assert_array_equal(oub[ok], ostore[ok, :, 1])
+
+
+def test_nodes_events_follow_a_changed_base(P, oracle):
+    """The working stores are reused while the base store is unchanged and
+    reloaded when it changes (embed + fixpoint, restore, a smaller batch):
+    every launch matches the oracle run on the base of that moment."""
+    import workloads as W
+    ctx, (blb, bub), off, var, lb, ub = _nodes_setup(P, seed=5, nnodes=256)
+    op, x, y, z = ctx.bytecode()
+    snap = ctx.snapshot()
+
+    def check(o, v, l, u):
+        cl, cu = ctx.read_store()
+        base = np.ascontiguousarray(np.stack([cl, cu], 1))
+        status, olb, oub, _, _ = ctx.fixpoint_nodes(o, v, l, u, sched=P.SCHED_EVENTS)
+        ostatus, ostore, _ = oracle.fixpoint_nodes(op, x, y, z, base, o, v, l, u)
+        np.testing.assert_array_equal(status, ostatus)
+        ok = ostatus == oracle.OK
+        np.testing.assert_array_equal(olb[ok], ostore[ok, :, 0])
+        np.testing.assert_array_equal(oub[ok], ostore[ok, :, 1])
+
+    check(off, var, lb, ub)
+    check(off, var, lb, ub)  # same base: working stores reused
+    # a new base: one unfixed variable bisected, then propagated
+    free = np.where(blb < bub)[0]
+    v0 = int(free[0])
+    ctx.embed(v0, int(blb[v0]), int(blb[v0] + (bub[v0] - blb[v0]) // 2))
+    rc, _ = ctx.fixpoint()
+    assert rc == P.OK
+    nl, nu = ctx.read_store()
+    _, off2, var2, lb2, ub2 = W.nodes(5000, 20_000, 256, 6, 48, base_store=(nl, nu))
+    check(off2, var2, lb2, ub2)
+    # back to the first base, then a smaller batch on the same base
+    ctx.restore(snap)
+    check(off, var, lb, ub)
+    check(off[:41], var, lb, ub)
+
+
 def test_nodes_events_need_a_fixpoint_base(P, oracle):
     """When the base store is not a fixpoint the event schedule is not exact;
     the call then runs AC-1 rounds and still matches the oracle."""

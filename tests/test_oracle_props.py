@@ -93,3 +93,66 @@ def test_spec_variant_fails_at_install(oracle):
     s = inst.store()
     st, _ = oracle.install_and_fixpoint(inst.op, inst.x, inst.y, inst.z, s)
     assert st == oracle.FAILED
+
+
+def _triples(lo, hi):
+    itv = np.array([(l, u) for l in range(lo, hi + 1) for u in range(l, hi + 1)], np.int32)
+    k = len(itv)
+    idx = np.stack(np.meshgrid(np.arange(k), np.arange(k), np.arange(k), indexing="ij"), -1).reshape(-1, 3)
+    return itv[idx, 0], itv[idx, 1]
+
+
+def _install_invariant(op, lb, ub):
+    """Reified targets live in [0, 1] after install (pir.hpp:333-335): keep
+    the triples whose x meets [0, 1], with x narrowed to it."""
+    if op not in (8, 9):
+        return lb, ub
+    lb, ub = lb.copy(), ub.copy()
+    lb[:, 0] = np.maximum(lb[:, 0], 0)
+    ub[:, 0] = np.minimum(ub[:, 0], 1)
+    keep = lb[:, 0] <= ub[:, 0]
+    return lb[keep], ub[keep]
+
+
+@pytest.mark.parametrize("op", range(10))
+def test_entailed_propagator_narrows_nothing(op, oracle):
+    """The premise of dropping propagators entailed at a search node's base
+    store: where ask(bytecode) holds (pir.hpp:417-438), deduce(bytecode)
+    (pir.hpp:721-817) changes no bound.  Every interval triple of [-5, 5]^3 and
+    random wide ones, reified targets within [0, 1] as install leaves them
+    (outside it the reified ask reads x <= 0 as false)."""
+    lb, ub = _triples(-5, 5)
+    rng = np.random.default_rng(100 + op)
+    m = 300_000
+    a = rng.integers(-10**6, 10**6, (m, 3))
+    b = a + rng.integers(0, 3, (m, 3)) * rng.integers(0, 10**3, (m, 3))
+    # many singletons so that entailment happens
+    b = np.where(rng.random((m, 3)) < .6, a, b)
+    a = np.where(rng.random((m, 3)) < .3, rng.integers(-3, 4, (m, 3)), a)
+    b = np.maximum(a, np.where(rng.random((m, 3)) < .3, a, b))
+    lb = np.concatenate([lb, a.astype(np.int32)])
+    ub = np.concatenate([ub, b.astype(np.int32)])
+    lb, ub = _install_invariant(op, lb, ub)
+    ops = np.full(len(lb), op, np.int32)
+    ent = oracle.ask_batch(ops, lb, ub)
+    assert ent.sum() > 100
+    out_lb, out_ub, changed, failed, _ = oracle.deduce_batch(ops[ent], lb[ent], ub[ent])
+    assert not changed.any() and not failed.any()
+    np.testing.assert_array_equal(out_lb, lb[ent].reshape(-1, 3))
+    np.testing.assert_array_equal(out_ub, ub[ent].reshape(-1, 3))
+
+
+@pytest.mark.parametrize("op", range(10))
+def test_entailment_is_monotone(op, oracle):
+    """ask(bytecode) stays true when any of its intervals narrows: a
+    propagator entailed at a base store is entailed at every node below it."""
+    lb, ub = _install_invariant(op, *_triples(-4, 4))
+    ops = np.full(len(lb), op, np.int32)
+    ent = oracle.ask_batch(ops, lb, ub)
+    lb, ub = lb[ent], ub[ent]
+    rng = np.random.default_rng(op)
+    for _ in range(4):
+        # a random non-empty sub-interval of each interval
+        nl = lb + (rng.random(lb.shape) * (ub - lb + 1)).astype(np.int32)
+        nu = nl + (rng.random(lb.shape) * (ub - nl + 1)).astype(np.int32)
+        assert oracle.ask_batch(ops[:len(nl)], nl, nu).all()
