@@ -185,6 +185,55 @@ int pir_fixpoint_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, cons
                        int32_t *out_lb, int32_t *out_ub, int32_t *out_status,
                        int32_t *out_rounds, pir_stats *stats);
 
+/* pir_fixpoint_nodes for a search driver: instead of whole stores, every node
+ * reports the final bounds of the `nwatch` variables `watch` (out_wlb/out_wub,
+ * nnodes x nwatch, node-major).  Runs the event schedule; the context's store
+ * is first brought to its fixpoint when it is not known to be one (node
+ * results do not depend on it: a node's fixpoint is that of base + its
+ * tightenings).  Replaces reading the decision variables of each child node
+ * (pir.hpp:840-851) after its propagation. */
+int pir_fixpoint_nodes_watch(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, const int32_t *var,
+                             const int32_t *lb, const int32_t *ub, const pir_opts *opts, int32_t nwatch,
+                             const int32_t *watch, int32_t *out_wlb, int32_t *out_wub, int32_t *out_status,
+                             int32_t *out_rounds, pir_stats *stats);
+
+/* Branching order of pir_search. */
+enum pir_order {
+  PIR_ORDER_INPUT = 0,     /* the first decision variable that is not fixed */
+  PIR_ORDER_MIN_DOMAIN = 1 /* the unfixed decision variable with the smallest domain (first on ties) */
+};
+
+typedef struct pir_search_opts {
+  int64_t max_nodes;     /* nodes to propagate, 0: no limit */
+  int64_t max_solutions; /* stop after this many solutions (rows of out_solutions); 0: count them all */
+  int32_t batch;         /* nodes per launch, 0: 4096 */
+  int32_t order;         /* enum pir_order */
+  int32_t reserved[6];
+} pir_search_opts;
+
+typedef struct pir_search_stats {
+  int64_t nodes;      /* nodes propagated, the root included */
+  int64_t failures;   /* nodes whose store became empty */
+  int64_t solutions;  /* nodes with every decision variable fixed */
+  int64_t launches;   /* batched node launches */
+  int64_t max_depth;  /* deepest node */
+  float device_ms;    /* summed device time of the node launches */
+  int32_t status;     /* PIR_OK: space exhausted or max_solutions reached; PIR_TIMEOUT: max_nodes reached */
+} pir_search_stats;
+
+/* Depth-first search over the decision variables `dec` (ndec of them) from the
+ * context's store: a node whose decision variables are all fixed is a solution
+ * (its values go to row k of out_solutions, max_solutions x ndec); otherwise
+ * the branching variable's interval [l, u] is bisected into [l, m] (explored
+ * first) and [m + 1, u], m = l + (u - l) / 2.  Up to opts->batch open nodes
+ * are propagated per launch (pir_fixpoint_nodes_watch), so with batch > 1 the
+ * solutions come in the order of the batches.  The decision variables must
+ * determine the others (typically: all variables).  The loop a solver runs
+ * around lala-pc's PIR with snapshot / restore (pir.hpp:857-870); the context
+ * keeps its store (brought to its fixpoint). */
+int pir_search(pirgpu_ctx *ctx, int32_t ndec, const int32_t *dec, const pir_search_opts *opts,
+               int32_t *out_solutions, pir_search_stats *stats);
+
 /* Batched independent instances of uneven size, one launch: instance j owns
  * propagators prop_off[j] .. prop_off[j+1]-1 (var indices local to the
  * instance) and variables var_off[j] .. var_off[j+1]-1 of lb/ub, which are

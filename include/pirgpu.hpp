@@ -22,6 +22,7 @@
 #ifndef PIRGPU_HPP
 #define PIRGPU_HPP
 
+#include <algorithm>
 #include <climits>
 #include <cstdint>
 #include <memory>
@@ -236,6 +237,27 @@ class PIR {
     check(pir_read_store(ctx(), lb.data(), ub.data()));
     ua.resize((size_t)n);
     for (int32_t i = 0; i < n; ++i) ua[(size_t)i] = Itv(lb[(size_t)i], ub[(size_t)i]);
+  }
+
+  // Depth-first search over the decision variables `dec` (pir_search): the
+  // branch / propagate / restore loop a solver runs around PIR
+  // (pir.hpp:857-870), children propagated in batches on the GPU.  Keeps at
+  // most opts.max_solutions solutions (0: counts them only).
+  struct search_result {
+    pir_status status;
+    std::vector<std::vector<int32_t>> solutions;
+    pir_search_stats stats;
+  };
+  search_result search(const std::vector<int32_t> &dec, const pir_search_opts &opts) {
+    search_result res;
+    std::vector<int32_t> buf((size_t)std::max<int64_t>(opts.max_solutions, 1) * dec.size());
+    const int rc = pir_search(ctx(), (int32_t)dec.size(), dec.data(), &opts, buf.data(), &res.stats);
+    if (rc != PIR_OK && rc != PIR_TIMEOUT) fail(rc);
+    res.status = (pir_status)res.stats.status;
+    const int64_t kept = opts.max_solutions > 0 ? res.stats.solutions : 0;
+    for (int64_t k = 0; k < kept; ++k)
+      res.solutions.emplace_back(buf.begin() + (size_t)k * dec.size(), buf.begin() + (size_t)(k + 1) * dec.size());
+    return res;
   }
 
   pirgpu_ctx *ctx() const { return ctx_.get(); }

@@ -64,6 +64,8 @@ struct BatchState {
   size_t cap_ev = 0;
   long long ev_base_version = -1;  // store version the first ev_valid_slots working stores equal
   int ev_valid_slots = 0;
+  int *d_watch = nullptr;  // watched variables | their bounds per node
+  size_t cap_watch = 0;
   unsigned char *d_ent = nullptr;  // entailed-at-base flags per propagator
   size_t cap_ent = 0;
   long long ent_store_version = -1, ent_bc_version = -1;
@@ -73,7 +75,7 @@ void destroy_batch_state(pirgpu_ctx *ctx) {
   BatchState *b = ctx->batch;
   if (!b) return;
   void *ptrs[] = {b->d_bc, b->d_off,    b->d_store, b->d_aux,     b->d_iout, b->d_nstore, b->d_tight,
-                  b->d_nout, b->d_nio, b->d_bc4, b->d_adj_ptr, b->d_adj, b->d_ev, b->d_ent};
+                  b->d_nout, b->d_nio, b->d_bc4, b->d_adj_ptr, b->d_adj, b->d_ev, b->d_ent, b->d_watch};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete b;
@@ -504,6 +506,9 @@ struct EvArgs {
   const int2 *base;
   int copy_base;    // the working stores must be (re)loaded from the base
   int2 *out_store;  // node-major nnodes x nvars, or nullptr
+  const int *watch;  // nwatch variables whose final bounds every node reports
+  int nwatch;
+  int2 *out_watch;   // nnodes x nwatch
   const int *off, *var, *lb, *ub;
   int nnodes;
   int *next;
@@ -727,6 +732,8 @@ __global__ void __launch_bounds__(NODE_BLOCK, MINB) k_nodes_events(EvArgs a) {
       int2 *dst = a.out_store + (size_t)node * nv;
       for (size_t v = tid; v < nv; v += blockDim.x) dst[v] = __ldcg(ws + v);
     }
+    for (int k = tid; k < a.nwatch; k += blockDim.x)
+      a.out_watch[(size_t)node * a.nwatch + k] = __ldcg(ws + a.watch[k]);
     __syncthreads();
     // put the touched variables back to the base store
     const int nt = s_nt;
@@ -836,7 +843,9 @@ int events_graph(pirgpu_ctx *ctx, const int4 **bc, const int **adj_ptr, const in
 
 int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const int32_t *off, const int32_t *var,
                           const int32_t *lb, const int32_t *ub, const pir_opts &opts, int32_t *out_lb,
-                          int32_t *out_ub, int32_t *out_status, int32_t *out_rounds, pir_stats *stats) {
+                          int32_t *out_ub, int32_t *out_status, int32_t *out_rounds, pir_stats *stats,
+                          int32_t nwatch = 0, const int32_t *watch = nullptr, int32_t *out_wlb = nullptr,
+                          int32_t *out_wub = nullptr) {
   int r;
   if ((r = ensure_events_graph(ctx, b))) return r;
   const int block = NODE_BLOCK;
@@ -923,6 +932,18 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
     d_out_store = b->d_nstore;
   }
   a.out_store = d_out_store;
+  a.nwatch = nwatch;
+  a.watch = nullptr;
+  a.out_watch = nullptr;
+  if (nwatch > 0) {
+    const size_t wbytes = (size_t)nwatch * sizeof(int) + 16 + (size_t)nnodes * nwatch * sizeof(int2);
+    if ((r = ensure(ctx, (void **)&b->d_watch, &b->cap_watch, wbytes))) return r;
+    int *dw = b->d_watch;
+    int2 *dwo = reinterpret_cast<int2 *>(reinterpret_cast<char *>(dw) + (((size_t)nwatch * sizeof(int) + 15) & ~(size_t)15));
+    PIR_CK(cudaMemcpyAsync(dw, watch, (size_t)nwatch * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    a.watch = dw;
+    a.out_watch = dwo;
+  }
   a.off = d_off;
   a.var = d_var;
   a.lb = d_lb;
@@ -948,6 +969,11 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
   unsigned long long hcnt[2] = {0, 0};
   PIR_CK(cudaMemcpyAsync(hout.data(), b->d_nout, nnodes * sizeof(NodeOut), cudaMemcpyDeviceToHost, ctx->stream));
   PIR_CK(cudaMemcpyAsync(hcnt, d_cnt, sizeof(hcnt), cudaMemcpyDeviceToHost, ctx->stream));
+  std::vector<int2> hw;
+  if (nwatch > 0) {
+    hw.resize((size_t)nnodes * nwatch);
+    PIR_CK(cudaMemcpyAsync(hw.data(), a.out_watch, hw.size() * sizeof(int2), cudaMemcpyDeviceToHost, ctx->stream));
+  }
   if (out_lb) {
     int per = (int)std::min<long long>(nnodes, (256ll << 20) / std::max<long long>(8ll * ctx->nvars, 1));
     per = std::max(per, 1);
@@ -982,6 +1008,10 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
     if (out_rounds) out_rounds[j] = hout[j].rounds;
     st.rounds = std::max<int64_t>(st.rounds, hout[j].rounds);
     if (hout[j].status == PIR_TIMEOUT) worst = PIR_TIMEOUT;
+  }
+  for (size_t k = 0; k < hw.size(); ++k) {
+    out_wlb[k] = hw[k].x;
+    out_wub[k] = hw[k].y;
   }
   st.executions = (int64_t)hcnt[0];
   st.narrowed = (int64_t)hcnt[1];

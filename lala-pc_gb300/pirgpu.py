@@ -38,6 +38,23 @@ class Opts(ctypes.Structure):
                 ("local_frontier", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
 
 
+class SearchOpts(ctypes.Structure):
+    _fields_ = [("max_nodes", ctypes.c_int64), ("max_solutions", ctypes.c_int64),
+                ("batch", ctypes.c_int32), ("order", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+
+
+class SearchStats(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_int64), ("failures", ctypes.c_int64), ("solutions", ctypes.c_int64),
+                ("launches", ctypes.c_int64), ("max_depth", ctypes.c_int64), ("device_ms", ctypes.c_float),
+                ("status", ctypes.c_int32)]
+
+    def asdict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+ORDER_INPUT, ORDER_MIN_DOMAIN = range(2)
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("rounds", ctypes.c_int64), ("executions", ctypes.c_int64),
                 ("narrowed", ctypes.c_int64), ("device_ms", ctypes.c_float),
@@ -89,6 +106,11 @@ SIGNATURES = [
     ("pir_fixpoint_nodes", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P, _I32P,
                                           ctypes.POINTER(Opts), _I32P, _I32P, _I32P, _I32P,
                                           ctypes.POINTER(Stats)]),
+    ("pir_fixpoint_nodes_watch", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P, _I32P,
+                                                ctypes.POINTER(Opts), ctypes.c_int32, _I32P, _I32P, _I32P,
+                                                _I32P, _I32P, ctypes.POINTER(Stats)]),
+    ("pir_search", ctypes.c_int, [_P, ctypes.c_int32, _I32P, ctypes.POINTER(SearchOpts), _I32P,
+                                  ctypes.POINTER(SearchStats)]),
     ("pir_fixpoint_instances", ctypes.c_int, [_P, ctypes.c_int32, _I64P, _I64P, _I32P, _I32P,
                                               _I32P, _I32P, _I32P, _I32P, ctypes.POINTER(Opts),
                                               _I32P, _I32P, _F32P, ctypes.POINTER(Stats)]),
@@ -312,6 +334,36 @@ class Context:
                                         _p32(status), _p32(rounds), ctypes.byref(s))
         self._check(rc)
         return status, out_lb, out_ub, rounds, s.asdict()
+
+    def fixpoint_nodes_watch(self, off, var, lb, ub, watch, **kw):
+        """Per node: status, rounds and the final bounds of the `watch` variables
+        (nnodes x nwatch arrays)."""
+        off, var, lb, ub, watch = map(_c32, (off, var, lb, ub, watch))
+        nn, nw = len(off) - 1, len(watch)
+        wl = np.empty((nn, nw), np.int32)
+        wu = np.empty((nn, nw), np.int32)
+        status = np.empty(nn, np.int32)
+        rounds = np.empty(nn, np.int32)
+        o = make_opts(**kw)
+        s = Stats()
+        self._check(self._L.pir_fixpoint_nodes_watch(self.h, nn, _p32(off), _p32(var), _p32(lb), _p32(ub),
+                                                     ctypes.byref(o), nw, _p32(watch), _p32(wl), _p32(wu),
+                                                     _p32(status), _p32(rounds), ctypes.byref(s)))
+        return status, wl, wu, rounds, s.asdict()
+
+    def search(self, dec, max_solutions=0, max_nodes=0, batch=0, order=ORDER_INPUT):
+        """Depth-first search over the decision variables `dec`: (status, the
+        solutions found (rows of decision values; none kept when max_solutions
+        is 0), stats)."""
+        dec = _c32(dec)
+        o = SearchOpts()
+        o.max_nodes, o.max_solutions, o.batch, o.order = max_nodes, max_solutions, batch, order
+        out = np.empty((max(max_solutions, 1), len(dec)), np.int32)
+        s = SearchStats()
+        rc = self._L.pir_search(self.h, len(dec), _p32(dec), ctypes.byref(o), _p32(out), ctypes.byref(s))
+        self._check(rc, (OK, TIMEOUT))
+        st = s.asdict()
+        return st["status"], out[:st["solutions"] if max_solutions else 0], st
 
     def fixpoint_instances(self, prop_off, var_off, op, x, y, z, lb, ub, **kw):
         """lb/ub are updated in place (int32 contiguous arrays)."""

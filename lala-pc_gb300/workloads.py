@@ -358,3 +358,31 @@ def pack(instances):
         var_off[j + 1] = var_off[j] + inst.nvars
     cat = lambda f: np.concatenate([getattr(i, f) for i in instances]).astype(np.int32)
     return prop_off, var_off, cat("op"), cat("x"), cat("y"), cat("z"), cat("lb"), cat("ub")
+
+
+def queens(n):
+    """n queens as PIR propagators: q_i in [0, n-1] is the row of the queen in
+    column i; for i < j, d_ij = q_i - q_j (ADD q_i = d_ij + q_j) and
+    d_ij != 0, d_ij != j - i, d_ij != i - j, each written as the reified
+    EQ false = (d_ij == c) with c a singleton.  Variables: q_0..q_{n-1}, then
+    the d_ij, the constants -(n-1)..n-1 and false = [0, 0].  Solutions: 1, 0,
+    0, 2, 10, 4, 40, 92 for n = 1..8."""
+    pairs = [(i, j) for i in range(n) for j in range(i + 1, n)]
+    nq, nd = n, len(pairs)
+    c0 = nq + nd                      # constant k lives at c0 + k + (n - 1)
+    false = c0 + 2 * n - 1
+    nvars = false + 1
+    lb = np.zeros(nvars, np.int64)
+    ub = np.zeros(nvars, np.int64)
+    ub[:nq] = n - 1
+    lb[nq:c0] = -(n - 1)
+    ub[nq:c0] = n - 1
+    for k in range(-(n - 1), n):
+        lb[c0 + k + n - 1] = ub[c0 + k + n - 1] = k
+    op, x, y, z = [], [], [], []
+    for t, (i, j) in enumerate(pairs):
+        d = nq + t
+        op.append(ADD); x.append(i); y.append(d); z.append(j)
+        for k in (0, j - i, i - j):
+            op.append(EQ); x.append(false); y.append(d); z.append(c0 + k + n - 1)
+    return Instance(lb, ub, op, x, y, z, queens=n)

@@ -140,6 +140,35 @@ static void interpretation_error() {
   EXPECT(t.bytecodes.empty());
 }
 
+// 6 queens through the facade: 4 solutions (the search driver around PIR).
+static void queens6() {
+  const int n = 6;
+  std::vector<Itv> dom;
+  for (int i = 0; i < n; ++i) dom.push_back(Itv(0, n - 1));
+  std::vector<std::pair<int, int>> pairs;
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j) pairs.emplace_back(i, j);
+  for (size_t t = 0; t < pairs.size(); ++t) dom.push_back(Itv(-(n - 1), n - 1));  // d_ij
+  const int c0 = (int)dom.size();
+  for (int k = -(n - 1); k < n; ++k) dom.push_back(Itv(k, k));
+  const int f = (int)dom.size();
+  dom.push_back(Itv(0, 0));
+  PIR pir(dom);
+  for (size_t t = 0; t < pairs.size(); ++t) {
+    const int i = pairs[t].first, j = pairs[t].second, d = n + (int)t;
+    tell(pir, Formula::ternary(i, Sig::ADD, d, j));
+    for (int k : {0, j - i, i - j}) tell(pir, Formula::ternary(f, Sig::EQ, d, c0 + k + n - 1));
+  }
+  std::vector<int32_t> dec;
+  for (int i = 0; i < n; ++i) dec.push_back(i);
+  pir_search_opts o{};
+  o.max_solutions = 10;
+  PIR::search_result r = pir.search(dec, o);
+  EXPECT(r.status == PIR_OK);
+  EXPECT(r.stats.solutions == 4);
+  EXPECT(r.solutions.size() == 4);
+}
+
 int main() {
   ternary_problem();
   top_prop();
@@ -149,6 +178,7 @@ int main() {
   snapshot_loop();
   gauss_seidel_drop_in();
   interpretation_error();
+  queens6();
   std::printf("%d failures\n", failures);
   return failures ? 1 : 0;
 }

@@ -156,3 +156,18 @@ def test_entailment_is_monotone(op, oracle):
         nl = lb + (rng.random(lb.shape) * (ub - lb + 1)).astype(np.int32)
         nu = nl + (rng.random(lb.shape) * (ub - nl + 1)).astype(np.int32)
         assert oracle.ask_batch(ops[:len(nl)], nl, nu).all()
+
+
+def test_queens_model_counts(oracle):
+    """The n-queens PIR model (reified EQ with a false target as !=, ADD for
+    differences) has the known solution counts under the CPU reference search."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(__file__))
+    import workloads as W
+    from search_ref import cpu_search
+    for n, want in [(1, 1), (2, 0), (3, 0), (4, 2), (5, 10), (6, 4), (7, 40), (8, 92)]:
+        inst = W.queens(n)
+        s = inst.store()
+        st, perm = oracle.install(inst.op, inst.x, inst.y, inst.z, s)
+        sols, _, _ = cpu_search(oracle, inst.op[perm], inst.x[perm], inst.y[perm], inst.z[perm], s, np.arange(n))
+        assert len(sols) == want
