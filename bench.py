@@ -436,8 +436,16 @@ def run_nodes(args):
         _, _, _, _, st_ac1 = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=pirgpu.SCHED_AC1)
     execs = sum(r["executions"] for r in runs)
     joins = sum(r["narrowed"] for r in runs)
-    # the plain single-instance GPU loop, node after node (sample)
     snap = ctx.snapshot()
+    # the first batch after the base store changed (working stores reloaded,
+    # entailment at the base recomputed); restore() marks the store changed
+    first_ms = None
+    if extras:
+        ctx.restore(snap)
+        cr.flush_l2()
+        _, _, _, _, st_first = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=sched)
+        first_ms = st_first["device_ms"]
+    # the plain single-instance GPU loop, node after node (sample)
     sample = min(nn, args.seq_nodes) if extras else 0
     seq_dev_rate = seq_wall_rate = None
     if sample:
@@ -492,7 +500,8 @@ def run_nodes(args):
                    "nodes_ok": n_ok, "nodes_failed": n_failed,
                    "max_rounds": max_rounds, "mean_rounds_rank0": float(rounds.mean()) if nn else 0.0,
                    "schedule": args.node_sched, "executions_per_step": execs // args.steps,
-                   "batched_ac1_ms": st_ac1["device_ms"], "batched_ac1_executions": st_ac1["executions"]},
+                   "batched_ac1_ms": st_ac1["device_ms"], "batched_ac1_executions": st_ac1["executions"],
+                   "first_batch_on_new_base_ms": first_ms},
         "plain_sequential": {"nodes_per_s_device": seq_dev_rate, "nodes_per_s_wall": seq_wall_rate,
                              "sample_nodes": sample,
                              "batched_over_sequential_device": value / seq_dev_rate if seq_dev_rate else None,
@@ -651,6 +660,68 @@ def run_uneven(args):
     print(json.dumps(out), flush=True)
 
 
+def run_search(args):
+    """The search driver on n-queens (all solutions, bisection of the first
+    unfixed queen): nodes propagated per second; the CPU oracle's depth-first
+    search of the same tree beside it."""
+    import pirgpu
+    import workloads as W
+    ws, rank, local = dist_env()
+    cr = Cudart()
+    cr.set_device(local)
+    n = args.queens
+    inst = W.queens(n)
+    dec = np.arange(n, dtype=np.int32)
+    ctx = pirgpu.Context(local)
+    ctx.load_store(inst.lb, inst.ub)
+    ctx.tell(inst.op, inst.x, inst.y, inst.z)
+    for _ in range(args.warmup):
+        ctx.search(dec)
+    clk = ClockSampler(local)
+    clk.start()
+    runs, walls = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        status, _, st = ctx.search(dec)
+        walls.append(time.perf_counter() - t0)
+        runs.append(st)
+    clocks = clk.stop()
+    st = runs[0]
+    dev_s = sum(r["device_ms"] for r in runs) / 1e3
+    nodes = sum(r["nodes"] for r in runs)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        s = inst.store()
+        _, perm = O.install(inst.op, inst.x, inst.y, inst.z, s)
+        cap = args.cpu_search_nodes
+        t0 = time.perf_counter()
+        rc, _, info = O.search(inst.op[perm], inst.x[perm], inst.y[perm], inst.z[perm], s, dec, max_nodes=cap)
+        ct = time.perf_counter() - t0
+        cpu = {"value": info["nodes"] / ct, "unit": "nodes/s", "cores": 1, "kind": "port",
+               "sample": "%s: %d nodes of the same depth-first tree (%d solutions), Gauss-Seidel per node, "
+                         "1 host thread, %.1f s" % ("the whole tree" if rc == O.OK else "the first nodes",
+                                                    info["nodes"], info["solutions"], ct)}
+    out = {
+        "metric": "search nodes/sec", "value": nodes / dev_s, "unit": "nodes/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(walls) * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic: the %d-queens model" % n,
+        "config": {"workload": "search: %d-queens, all solutions, bisection of the first unfixed queen, "
+                               "4,096 open nodes per launch" % n,
+                   "nodes": st["nodes"], "failures": st["failures"], "solutions": st["solutions"],
+                   "launches": st["launches"], "max_depth": st["max_depth"],
+                   "device_ms_per_search": dev_s * 1e3 / args.steps},
+        "roofline": None,
+        "cpu_baseline": cpu,
+        "e2e": {"value": nodes / sum(walls), "unit": "nodes/s", "h2d_bytes_per_step": None,
+                "d2h_bytes_per_step": None, "note": "whole pir_search calls: host bookkeeping, tightenings "
+                                                    "in and watched bounds out per launch"},
+        "gpu_launches": st["launches"] * args.steps, "clocks": clocks,
+    }
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -710,6 +781,8 @@ def main():
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--node-sched", default="events", choices=["events", "ac1"])
     ap.add_argument("--wake-fraction", type=float, default=1 / 32)
+    ap.add_argument("--queens", type=int, default=12, help="search workload: board size")
+    ap.add_argument("--cpu-search-nodes", type=int, default=2_000_000, help="search workload: CPU node cap")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")
@@ -721,6 +794,8 @@ def main():
         run_uneven(args)
     elif args.workload == "learned":
         run_learned(args)
+    elif args.workload == "search":
+        run_search(args)
     else:
         run_ours(args)
 

@@ -36,6 +36,9 @@ def lib():
         L.orc_deduce.argtypes = [i32, i32, i32, i32, _I32P, ctypes.POINTER(ctypes.c_int)]
         L.orc_ask.argtypes = [i32, i32, i32, i32, _I32P]
         _U8P = ctypes.POINTER(ctypes.c_uint8)
+        L.orc_search.argtypes = [i32, _I32P, _I32P, _I32P, _I32P, i32, _I32P, i32, _I32P, i32, i64, i64,
+                                 _I32P, _I64P]
+        L.orc_search.restype = ctypes.c_int
         L.orc_ask_batch.argtypes = [i64, _I32P, _I32P, _I32P, _U8P]
         L.orc_ask_batch.restype = None
         L.orc_deduce_batch.argtypes = [i64, _I32P, _I32P, _I32P, _I32P, _I32P, _U8P, _U8P, _I64P]
@@ -177,6 +180,20 @@ def deduce_batch(op, in_lb, in_ub):
 
 def ask(op, x, y, z, store):
     return bool(lib().orc_ask(op, x, y, z, _p32(store)))
+
+
+def search(op, x, y, z, store, dec, order=0, max_solutions=0, max_nodes=0):
+    """Depth-first search from `store` (installed bytecode): (status,
+    solutions (rows of decision values, up to max_solutions), dict(nodes,
+    failures, solutions))."""
+    op, x, y, z, dec = map(_c32, (op, x, y, z, dec))
+    store = _c32(store)
+    out = np.zeros((max(max_solutions, 1), len(dec)), np.int32)
+    st = np.zeros(3, np.int64)
+    rc = lib().orc_search(len(op), _p32(op), _p32(x), _p32(y), _p32(z), store.shape[0], _p32(store),
+                          len(dec), _p32(dec), order, max_solutions, max_nodes, _p32(out), _p64(st))
+    k = int(st[2]) if max_solutions else 0
+    return rc, out[:k], dict(nodes=int(st[0]), failures=int(st[1]), solutions=int(st[2]))
 
 
 def ask_batch(op, in_lb, in_ub):

@@ -750,6 +750,69 @@ int orc_fixpoint(int32_t n, const int32_t *op, const int32_t *x, const int32_t *
   return gs_fixpoint(n, op, x, y, z, nvars, store, max_sweeps, out);
 }
 
+// Depth-first search (the CPU reference of the search driver): every node is
+// the store of its parent with one bisection, brought to its Gauss-Seidel
+// fixpoint; a node with all decision variables fixed is a solution; otherwise
+// the first unfixed decision variable (order 0) or the one with the smallest
+// domain (order 1) is bisected at l + (u - l) / 2, lower half first.
+// out_stats: nodes, failures, solutions.  Solutions (decision values) go to
+// out_solutions while max_solutions allows (0: count only).
+int orc_search(int32_t n, const int32_t *op, const int32_t *x, const int32_t *y, const int32_t *z,
+               int32_t nvars, const int32_t *store, int32_t ndec, const int32_t *dec, int32_t order,
+               int64_t max_solutions, int64_t max_nodes, int32_t *out_solutions, int64_t *out_stats) {
+  std::vector<std::vector<i32>> stack;
+  stack.emplace_back(store, store + 2 * (size_t)nvars);
+  i64 nodes = 0, fails = 0, sols = 0;
+  int status = ORC_OK;
+  while (!stack.empty()) {
+    if (max_nodes > 0 && nodes >= max_nodes) {
+      status = ORC_TIMEOUT;
+      break;
+    }
+    std::vector<i32> s = std::move(stack.back());
+    stack.pop_back();
+    ++nodes;
+    if (gs_fixpoint(n, op, x, y, z, nvars, s.data(), (i64)1 << 40, nullptr) == ORC_FAILED) {
+      ++fails;
+      continue;
+    }
+    int best = -1;
+    i64 best_w = 0;
+    for (int k = 0; k < ndec; ++k) {
+      const i64 l = s[2 * (size_t)dec[k]], u = s[2 * (size_t)dec[k] + 1];
+      if (l >= u) continue;
+      if (order == 0) {
+        best = k;
+        break;
+      }
+      if (best < 0 || u - l < best_w) {
+        best = k;
+        best_w = u - l;
+      }
+    }
+    if (best < 0) {
+      if (max_solutions > 0)
+        for (int k = 0; k < ndec; ++k) out_solutions[(size_t)sols * ndec + k] = s[2 * (size_t)dec[k]];
+      ++sols;
+      if (max_solutions > 0 && sols >= max_solutions) break;
+      continue;
+    }
+    const size_t v = (size_t)dec[best];
+    const i64 lo = s[2 * v], hi = s[2 * v + 1], mid = lo + (hi - lo) / 2;
+    std::vector<i32> right = s;
+    right[2 * v] = (i32)(mid + 1);
+    s[2 * v + 1] = (i32)mid;
+    stack.push_back(std::move(right));
+    stack.push_back(std::move(s));
+  }
+  if (out_stats) {
+    out_stats[0] = nodes;
+    out_stats[1] = fails;
+    out_stats[2] = sols;
+  }
+  return status;
+}
+
 int orc_sweeps(int32_t n, const int32_t *op, const int32_t *x, const int32_t *y,
                const int32_t *z, int32_t *store, int64_t sweeps, int64_t *out) {
   g_overflows = 0;

@@ -42,6 +42,9 @@ int orc_deduce(int32_t op, int32_t x, int32_t y, int32_t z, int32_t *store, int 
 
 /* deduce(bytecode) (op[k], 0, 1, 2) over `count` private 3-variable stores
  * in_lb/in_ub[3k..3k+2]; host threads.  *overflows = intermediates outside int32. */
+int orc_search(int32_t n, const int32_t *op, const int32_t *x, const int32_t *y, const int32_t *z,
+               int32_t nvars, const int32_t *store, int32_t ndec, const int32_t *dec, int32_t order,
+               int64_t max_solutions, int64_t max_nodes, int32_t *out_solutions, int64_t *out_stats);
 void orc_ask_batch(int64_t count, const int32_t *op, const int32_t *in_lb, const int32_t *in_ub, uint8_t *out);
 void orc_deduce_batch(int64_t count, const int32_t *op, const int32_t *in_lb, const int32_t *in_ub,
                       int32_t *out_lb, int32_t *out_ub, uint8_t *out_changed, uint8_t *out_failed,

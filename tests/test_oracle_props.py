@@ -171,3 +171,25 @@ def test_queens_model_counts(oracle):
         st, perm = oracle.install(inst.op, inst.x, inst.y, inst.z, s)
         sols, _, _ = cpu_search(oracle, inst.op[perm], inst.x[perm], inst.y[perm], inst.z[perm], s, np.arange(n))
         assert len(sols) == want
+
+
+@pytest.mark.parametrize("order", [0, 1])
+def test_oracle_search_matches_reference_search(order, oracle):
+    """orc_search (the C++ CPU search, the bench's baseline) visits the same
+    nodes and finds the same solutions, in the same order, as the Python
+    reference search."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(__file__))
+    import workloads as W
+    from search_ref import cpu_search
+    cases = [(W.queens(n), np.arange(n)) for n in (5, 6, 8)] + [(W.plain(20, 24, 8, 1), np.arange(20))]
+    for inst, dec in cases:
+        s = inst.store()
+        st, perm = oracle.install(inst.op, inst.x, inst.y, inst.z, s)
+        args = (inst.op[perm], inst.x[perm], inst.y[perm], inst.z[perm])
+        ref, nodes, fails = cpu_search(oracle, *args, s, dec, order=order)
+        rc, sols, info = oracle.search(*args, s, dec, order=order, max_solutions=len(ref) + 1)
+        assert rc == oracle.OK and info["nodes"] == nodes and info["failures"] == fails
+        np.testing.assert_array_equal(sols, np.array(ref).reshape(-1, len(dec)))
+    rc, _, info = oracle.search(*args, s, dec, order=order, max_nodes=10)
+    assert rc == oracle.TIMEOUT and info["nodes"] == 10
