@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "pirgpu.hpp"
+#include "pirgpu_fzn.hpp"
 
 using namespace lala_gpu;
 
@@ -169,6 +170,29 @@ static void queens6() {
   EXPECT(r.solutions.size() == 4);
 }
 
+// The element constraint through the FlatZinc front end, told in three steps
+// (the user variables' bounds of tests/pir_test.cpp:569-582).
+static void element_fzn() {
+  fzn::Model m;
+  IDiagnostics d;
+  EXPECT(fzn::compile("array [1..3] of int: a = [10, 11, 12]; var 1..3: b; var 10..12: c;"
+                      " constraint array_int_element(b, a, c);",
+                      m, d));
+  std::unique_ptr<PIR> pir = fzn::make_pir(m);
+  const int b = m.index_of("b"), c = m.index_of("c");
+  EXPECT(pir->fixpoint() == PIR_OK);
+  EXPECT((*pir)[b] == Itv(1, 3) && (*pir)[c] == Itv(10, 12));
+  EXPECT(fzn::interpret_and_tell(*pir, m, "constraint int_le(c, 11);", d));
+  EXPECT(pir->fixpoint() == PIR_OK);
+  EXPECT((*pir)[b] == Itv(1, 2) && (*pir)[c] == Itv(10, 11));
+  fzn::interpret_and_tell(*pir, m, "var 0..1: fresh; constraint int_ge(c, 11); constraint int_le(fresh, 0);", d);
+  EXPECT(pir->fixpoint() == PIR_OK);
+  EXPECT((*pir)[b] == Itv(2, 2) && (*pir)[c] == Itv(11, 11));
+  EXPECT((*pir)[m.index_of("fresh")] == Itv(0, 0));
+  EXPECT(pir->is_extractable());
+  EXPECT(!d.has_error());
+}
+
 int main() {
   ternary_problem();
   top_prop();
@@ -179,6 +203,7 @@ int main() {
   gauss_seidel_drop_in();
   interpretation_error();
   queens6();
+  element_fzn();
   std::printf("%d failures\n", failures);
   return failures ? 1 : 0;
 }
