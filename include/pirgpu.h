@@ -296,6 +296,11 @@ int pir_sched_grad(pirgpu_ctx *ctx, int32_t count, const float *X, const float *
 /* Reads (set = 0) or writes (set = 1) the FP32 master parameters (count must
  * be the parameter count, 1377: W1[32][8], b1[32], W2[32][32], b2[32], W3[32], b3). */
 int pir_sched_params(pirgpu_ctx *ctx, float *params, int32_t count, int32_t set);
+/* Scores of count feature rows X (count x 8) with the learned fixpoint's
+ * inference path: the MLP on the tensor cores (mma, BF16 operands -- the
+ * features, the weights and the first hidden layer are rounded to BF16 --
+ * FP32 accumulation). */
+int pir_sched_score(pirgpu_ctx *ctx, int32_t count, const float *X, float *out_scores);
 
 /* Number of SMs and the library's build string (for reports). */
 int pir_device_info(pirgpu_ctx *ctx, int32_t *num_sms, char *name, size_t name_len);

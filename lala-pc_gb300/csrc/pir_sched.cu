@@ -94,24 +94,111 @@ __device__ __forceinline__ void stage_weights(const __nv_bfloat16 *wbf, float *s
   for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) sw[i] = __bfloat162float(wbf[i]);
 }
 
-__device__ __forceinline__ float mlp_forward(const float *sw, const float f[NF]) {
-  float h1[NH];
+// ------------------------------------------- tensor-core scoring (mma) -----
+// The inference MLP of 32 propagators per warp on the tensor cores
+// (mma.sync, BF16 operands, FP32 accumulation): layer 1 is a 16x8x8 product
+// per 16 propagators and 8 outputs, layer 2 two 16x8x16 products per 8
+// outputs, and the layer-1 accumulators become layer 2's A fragments in
+// registers (the m16n8 accumulator layout of two adjacent 8-column tiles is
+// the m16k16 A layout).  Fragment layouts (g = lane / 4, c = lane % 4):
+// A 16x8: {row g, cols 2c..2c+1}, {row g+8, same}; A 16x16 adds the same for
+// cols 2c+8..2c+9; B 8x8 (k x n): {k 2c..2c+1, n g}; B 16x8 adds k 2c+8..;
+// accumulators 16x8: {row g, cols 2c..2c+1}, {row g+8, cols 2c..2c+1}.
+
+__device__ __forceinline__ void mma_k8(float (&d)[4], unsigned a0, unsigned a1, unsigned b0) {
+  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a0), "r"(a1), "r"(b0));
+}
+__device__ __forceinline__ void mma_k16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ unsigned pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const unsigned *>(&v);
+}
+
+// The weights as B fragments, loaded once per thread: layer 1 per 8-output
+// tile j, layer 2 per tile j and 16-input step s (two registers).
+struct MmaWeights {
+  unsigned w1[4];
+  unsigned w2[4][2][2];
+  __device__ __forceinline__ void load(const __nv_bfloat16 *wbf) {
+    const int g = (threadIdx.x & 31) >> 2, c = threadIdx.x & 3;
+    const unsigned *w = reinterpret_cast<const unsigned *>(wbf);  // bf16 pairs; every offset below is even
 #pragma unroll
-  for (int j = 0; j < NH; ++j) {
-    float a = sw[OFF_B1 + j];
+    for (int j = 0; j < 4; ++j) {
+      w1[j] = __ldg(w + (OFF_W1 + (8 * j + g) * NF + 2 * c) / 2);
 #pragma unroll
-    for (int i = 0; i < NF; ++i) a = fmaf(sw[OFF_W1 + j * NF + i], f[i], a);
-    h1[j] = fmaxf(a, 0.f);
+      for (int k = 0; k < 2; ++k) {
+        w2[j][k][0] = __ldg(w + (OFF_W2 + (8 * j + g) * NH + 16 * k + 2 * c) / 2);
+        w2[j][k][1] = __ldg(w + (OFF_W2 + (8 * j + g) * NH + 16 * k + 2 * c + 8) / 2);
+      }
+    }
   }
-  float z = sw[OFF_B3];
-#pragma unroll 4
-  for (int j = 0; j < NH; ++j) {
-    float a = sw[OFF_B2 + j];
+};
+
+// Scores of the warp's 32 propagators (lane i holds the features of row i);
+// every lane of the warp must call it.  `tile` is the warp's 32 x 8 BF16
+// staging area in shared memory; sw holds the biases and W3 in FP32.
+__device__ __forceinline__ float mlp_forward_mma(const float f[NF], const MmaWeights &W, const float *sw,
+                                                 __nv_bfloat16 *tile) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, c = lane & 3;
+  unsigned *row = reinterpret_cast<unsigned *>(tile + lane * NF);
 #pragma unroll
-    for (int i = 0; i < NH; ++i) a = fmaf(sw[OFF_W2 + j * NH + i], h1[i], a);
-    z = fmaf(sw[OFF_W3 + j], fmaxf(a, 0.f), z);
+  for (int i = 0; i < NF / 2; ++i) row[i] = pack_bf16(f[2 * i], f[2 * i + 1]);
+  __syncwarp();
+  const unsigned *t32 = reinterpret_cast<const unsigned *>(tile);
+  float sc[2][2];
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    const unsigned a0 = t32[((16 * t + g) * NF + 2 * c) / 2], a1 = t32[((16 * t + g + 8) * NF + 2 * c) / 2];
+    float h[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float b0 = sw[OFF_B1 + 8 * j + 2 * c], b1 = sw[OFF_B1 + 8 * j + 2 * c + 1];
+      h[j][0] = b0;
+      h[j][1] = b1;
+      h[j][2] = b0;
+      h[j][3] = b1;
+      mma_k8(h[j], a0, a1, W.w1[j]);
+    }
+    unsigned A2[2][4];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      A2[k][0] = pack_bf16(fmaxf(h[2 * k][0], 0.f), fmaxf(h[2 * k][1], 0.f));
+      A2[k][1] = pack_bf16(fmaxf(h[2 * k][2], 0.f), fmaxf(h[2 * k][3], 0.f));
+      A2[k][2] = pack_bf16(fmaxf(h[2 * k + 1][0], 0.f), fmaxf(h[2 * k + 1][1], 0.f));
+      A2[k][3] = pack_bf16(fmaxf(h[2 * k + 1][2], 0.f), fmaxf(h[2 * k + 1][3], 0.f));
+    }
+    float lo = 0.f, hi = 0.f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float b0 = sw[OFF_B2 + 8 * j + 2 * c], b1 = sw[OFF_B2 + 8 * j + 2 * c + 1];
+      float o[4] = {b0, b1, b0, b1};
+      mma_k16(o, A2[0], W.w2[j][0][0], W.w2[j][0][1]);
+      mma_k16(o, A2[1], W.w2[j][1][0], W.w2[j][1][1]);
+      const float v0 = sw[OFF_W3 + 8 * j + 2 * c], v1 = sw[OFF_W3 + 8 * j + 2 * c + 1];
+      lo = fmaf(fmaxf(o[0], 0.f), v0, fmaf(fmaxf(o[1], 0.f), v1, lo));
+      hi = fmaf(fmaxf(o[2], 0.f), v0, fmaf(fmaxf(o[3], 0.f), v1, hi));
+    }
+    lo += __shfl_xor_sync(0xFFFFFFFFu, lo, 1);
+    lo += __shfl_xor_sync(0xFFFFFFFFu, lo, 2);
+    hi += __shfl_xor_sync(0xFFFFFFFFu, hi, 1);
+    hi += __shfl_xor_sync(0xFFFFFFFFu, hi, 2);
+    sc[t][0] = lo + sw[OFF_B3];
+    sc[t][1] = hi + sw[OFF_B3];
   }
-  return z;
+  __syncwarp();  // the tile is free again
+  // row `lane` = tile lane / 16, row lane % 16 of it, held by the quad of lanes 4 * (lane % 8)
+  const int src = (lane & 7) << 2;
+  const float v00 = __shfl_sync(0xFFFFFFFFu, sc[0][0], src), v01 = __shfl_sync(0xFFFFFFFFu, sc[0][1], src);
+  const float v10 = __shfl_sync(0xFFFFFFFFu, sc[1][0], src), v11 = __shfl_sync(0xFFFFFFFFu, sc[1][1], src);
+  const bool high = (lane >> 3) & 1;
+  return (lane >> 4) ? (high ? v11 : v10) : (high ? v01 : v00);
 }
 
 __device__ __forceinline__ int hist_bin(float z) {
@@ -149,20 +236,48 @@ struct StampStore {
 __device__ __forceinline__ int bc_get(const int *a, long long i) { return __ldg(a + i); }
 
 // Threshold bin of the top-k: the highest bin b such that the count of scores
-// in bins >= b reaches k.  Computed redundantly by every CTA from the global
-// histogram (2048 bins), in shared memory.
+// in bins >= b reaches k (bin 0 when it never does).  Computed redundantly by
+// every CTA from the global histogram (2048 bins) with a block-wide suffix
+// sum: thread t owns the bins of segment t counted from the top.
 __device__ int select_bin(const unsigned *hist, unsigned long long k, unsigned *sh) {
-  for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x) sh[i] = __ldcg(hist + i);
-  __syncthreads();
+  __shared__ unsigned long long s_warp[32];
   __shared__ int s_bin;
-  if (threadIdx.x == 0) {
-    unsigned long long acc = 0;
-    int b = HIST_BINS - 1;
-    for (; b > 0; --b) {
-      acc += sh[b];
-      if (acc >= k) break;
+  const int tid = threadIdx.x, nt = blockDim.x, per = (HIST_BINS + nt - 1) / nt;
+  for (int i = tid; i < HIST_BINS; i += nt) sh[i] = __ldcg(hist + i);
+  if (tid == 0) s_bin = 0;
+  __syncthreads();
+  const int hi = HIST_BINS - tid * per;  // segment [hi - per, hi)
+  unsigned long long seg = 0;
+  for (int b = hi - 1; b >= hi - per && b >= 0; --b) seg += sh[b];
+  // inclusive prefix over threads 0..tid (the bins from the top down to this segment)
+  const int lane = tid & 31, warp = tid >> 5;
+  unsigned long long x = seg;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long w = lane < (nt >> 5) ? s_warp[lane] : 0ull;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= o) w += y;
     }
-    s_bin = b;
+    if (lane < (nt >> 5)) s_warp[lane] = w;
+  }
+  __syncthreads();
+  const unsigned long long incl = x + (warp ? s_warp[warp - 1] : 0ull), above = incl - seg;
+  if (above < k && incl >= k) {
+    // the crossing is in this segment: walk it from the top
+    unsigned long long acc = above;
+    for (int b = hi - 1; b >= hi - per && b >= 0; --b) {
+      acc += sh[b];
+      if (acc >= k) {
+        s_bin = b;
+        break;
+      }
+    }
   }
   __syncthreads();
   return s_bin;
@@ -192,9 +307,15 @@ __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
   __shared__ float sw[NPARAM];
   __shared__ unsigned sh[HIST_BINS];
   __shared__ unsigned s_word;
+  __shared__ __align__(16) __nv_bfloat16 s_tile[256 / 32][32 * NF];
   stage_weights(a.wbf, sw);
+  MmaWeights W;
+  W.load(a.wbf);
+  __nv_bfloat16 *tile = s_tile[threadIdx.x >> 5];
   const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long gstride = (long long)gridDim.x * blockDim.x;
+  const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
+  const int lane = threadIdx.x & 31;
   unsigned long long woken = 0, narrowed = 0;
   long long round = 0, nbar = 0;  // nbar: grid barriers passed (thread 0)
   bool certify = false;
@@ -208,15 +329,22 @@ __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
       // (A) scores and histogram
       for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x) sh[i] = 0;
       __syncthreads();
-      for (long long p = gtid; p < a.n; p += gstride) {
-        const int o = bc_get(a.op, p), X = bc_get(a.x, p), Y = bc_get(a.y, p), Z = bc_get(a.z, p);
-        const Itv ia = st.load(X), ib = st.load(Y), ic = st.load(Z);
-        const int last = max(__ldcg(a.var_last + X), max(__ldcg(a.var_last + Y), __ldcg(a.var_last + Z)));
-        float f[NF];
-        features(o, ia, ib, ic, last, r, a.pdeg[p], f);
-        const float s = mlp_forward(sw, f);
-        a.score[p] = s;
-        atomicAdd(&sh[hist_bin(s)], 1u);
+      // 32 propagators per warp and step (the loop bound is warp-uniform:
+      // the tensor-core products need every lane)
+      for (long long w = gwarp; w * 32 < a.n; w += nwarps) {
+        const long long p = w * 32 + lane;
+        float f[NF] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (p < a.n) {
+          const int o = bc_get(a.op, p), X = bc_get(a.x, p), Y = bc_get(a.y, p), Z = bc_get(a.z, p);
+          const Itv ia = st.load(X), ib = st.load(Y), ic = st.load(Z);
+          const int last = max(__ldcg(a.var_last + X), max(__ldcg(a.var_last + Y), __ldcg(a.var_last + Z)));
+          features(o, ia, ib, ic, last, r, a.pdeg[p], f);
+        }
+        const float s = mlp_forward_mma(f, W, sw, tile);
+        if (p < a.n) {
+          a.score[p] = s;
+          atomicAdd(&sh[hist_bin(s)], 1u);
+        }
       }
       __syncthreads();
       unsigned *gh = a.hist + par * HIST_BINS;
@@ -773,6 +901,56 @@ extern "C" int pir_sched_grad(pirgpu_ctx *ctx, int32_t count, const float *X, co
   PIR_CK(cudaMemsetAsync(s->d_grad, 0, NPARAM * sizeof(float), ctx->stream));
   PIR_CK(cudaStreamSynchronize(ctx->stream));
   if (loss_out) *loss_out = loss / (float)count;
+  return PIR_OK;
+}
+
+// Scores of given feature rows with the inference path of the learned
+// fixpoint (tensor-core MLP), 32 rows per warp.
+__global__ void __launch_bounds__(256) k_score_batch(const __nv_bfloat16 *wbf, const float *X, long long count,
+                                                     float *out) {
+  __shared__ float sw[NPARAM];
+  __shared__ __align__(16) __nv_bfloat16 s_tile[256 / 32][32 * NF];
+  stage_weights(wbf, sw);
+  __syncthreads();
+  MmaWeights W;
+  W.load(wbf);
+  const int lane = threadIdx.x & 31;
+  const long long gwarp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long w = gwarp; w * 32 < count; w += nwarps) {
+    const long long p = w * 32 + lane;
+    float f[NF];
+#pragma unroll
+    for (int i = 0; i < NF; ++i) f[i] = p < count ? X[p * NF + i] : 0.f;
+    const float s = mlp_forward_mma(f, W, sw, s_tile[threadIdx.x >> 5]);
+    if (p < count) out[p] = s;
+  }
+}
+
+extern "C" int pir_sched_score(pirgpu_ctx *ctx, int32_t count, const float *X, float *out_scores) {
+  if (!ctx || count < 0 || (count > 0 && (!X || !out_scores))) return ctx ? set_err(ctx, PIR_EINVAL, "bad arguments") : PIR_EINVAL;
+  if (count == 0) return PIR_OK;
+  PIR_CK(cudaSetDevice(ctx->device));
+  int r;
+  if ((r = ensure_params(ctx))) return r;
+  SchedState *s = sched(ctx);
+  float *d = nullptr;
+  if (cudaMalloc(&d, (size_t)count * (NF + 1) * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, PIR_ENOMEM, "score buffers");
+  }
+  cudaError_t e = cudaMemcpyAsync(d, X, (size_t)count * NF * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    const int grid = std::max(1, std::min(ctx->num_sms * 8, (count + 255) / 256));
+    k_score_batch<<<grid, 256, 0, ctx->stream>>>(s->d_wbf, d, count, d + (size_t)count * NF);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out_scores, d + (size_t)count * NF, (size_t)count * sizeof(float), cudaMemcpyDeviceToHost,
+                        ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "pir_sched_score");
   return PIR_OK;
 }
 

@@ -106,6 +106,7 @@ SIGNATURES = [
     ("pir_fixpoint_nodes", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P, _I32P,
                                           ctypes.POINTER(Opts), _I32P, _I32P, _I32P, _I32P,
                                           ctypes.POINTER(Stats)]),
+    ("pir_sched_score", ctypes.c_int, [_P, ctypes.c_int32, _F32P, _F32P]),
     ("pir_fixpoint_nodes_watch", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P, _I32P,
                                                 ctypes.POINTER(Opts), ctypes.c_int32, _I32P, _I32P, _I32P,
                                                 _I32P, _I32P, ctypes.POINTER(Stats)]),
@@ -334,6 +335,13 @@ class Context:
                                         _p32(status), _p32(rounds), ctypes.byref(s))
         self._check(rc)
         return status, out_lb, out_ub, rounds, s.asdict()
+
+    def sched_score(self, X):
+        """Scores of feature rows X (n x 8) by the tensor-core inference MLP."""
+        X = np.ascontiguousarray(X, np.float32).reshape(-1, 8)
+        out = np.empty(len(X), np.float32)
+        self._check(self._L.pir_sched_score(self.h, len(X), X.ctypes.data_as(_F32P), out.ctypes.data_as(_F32P)))
+        return out
 
     def fixpoint_nodes_watch(self, off, var, lb, ub, watch, **kw):
         """Per node: status, rounds and the final bounds of the `watch` variables

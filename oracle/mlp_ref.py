@@ -31,6 +31,18 @@ def unpack(p):
             p[OFF_B2:OFF_W3], p[OFF_W3:OFF_B3], p[OFF_B3])
 
 
+def forward_inference(params, X):
+    """Scores as the device's inference path computes them: features,
+    weights and the first hidden layer rounded to BF16, sums in float64 (the
+    device accumulates in FP32, in its own order)."""
+    W1, b1, W2, b2, W3, b3 = unpack(bf16_round(params))
+    X = np.asarray(bf16_round(np.asarray(X, np.float32)), np.float64)
+    h1 = np.maximum(X @ W1.T + b1, 0)
+    h1 = np.asarray(bf16_round(h1.astype(np.float32)), np.float64)
+    h2 = np.maximum(h1 @ W2.T + b2, 0)
+    return h2 @ W3 + b3
+
+
 def loss_and_grad(params, X, Y, pos_weight=1.0, round_bf16=True):
     """Mean weighted BCE-with-logits over the batch and its gradient (float64)."""
     p = bf16_round(params) if round_bf16 else np.asarray(params, np.float32)

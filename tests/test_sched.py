@@ -62,6 +62,30 @@ def test_device_gradient_matches_reference(seed):
     np.testing.assert_allclose(g, rg, rtol=1e-3, atol=1e-6)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(3))
+def test_inference_scores_match_reference(seed):
+    """pir_sched_score (the tensor-core inference path of the learned
+    fixpoint: mma with BF16 features, weights and first hidden layer, FP32
+    accumulation) against the float64 restatement with the same roundings.
+    Tolerance: 1e-3 x (1 + |score|) on 99.5% of the rows; a first-layer value
+    that sits on a BF16 rounding boundary may round the other way on the
+    device (one BF16 ulp, 2^-8 relative), so every row is within
+    3e-2 x (1 + |score|)."""
+    import pirgpu
+    from oracle import mlp_ref as M
+    ctx = pirgpu.Context(0)
+    p = _params(seed)
+    ctx.sched_params(p)
+    X, _ = _batch(seed + 20, 4099)  # not a multiple of 32
+    X[:5] = 0.0
+    got = ctx.sched_score(X)
+    ref = M.forward_inference(p, X)
+    err = np.abs(got - ref) / (1 + np.abs(ref))
+    assert np.quantile(err, 0.995) < 1e-3
+    assert err.max() < 3e-2
+
+
 def _nodes(P, seed=0, nvars=20_000, nprops=80_000, nnodes=96):
     import workloads as W
     base = W.plain(nvars, nprops, 10**6, seed)
