@@ -120,20 +120,45 @@ static __device__ __forceinline__ void mul_inv(const Itv &r1, Itv &r2, Itv &r3) 
   } else if (xnz | (r3.l > 0) | (r3.u < 0)) {
     if (r1.l == MINF || r1.u == INF || r3.l == MINF || r3.u == INF) return;
     if (is_bot(r3)) return;
-    // r1.l > MINF here, so no quotient overflows int32 unless x is empty
-    // (then the failure is already flagged and the value is irrelevant).
-    int q0, m0, q1, m1, q2, m2, q3, m3;
-    qr32(r1.l, r3.l, q0, m0);
-    qr32(r1.l, r3.u, q1, m1);
-    qr32(r1.u, r3.l, q2, m2);
-    qr32(r1.u, r3.u, q3, m3);
-    // cdiv = q + (r != 0 && sign(r) == sign(b)); fdiv = q - (r != 0 && sign(r) != sign(b))
-    const int c0 = q0 + ((m0 != 0) & ((m0 ^ r3.l) >= 0)), f0 = q0 - ((m0 != 0) & ((m0 ^ r3.l) < 0));
-    const int c1 = q1 + ((m1 != 0) & ((m1 ^ r3.u) >= 0)), f1 = q1 - ((m1 != 0) & ((m1 ^ r3.u) < 0));
-    const int c2 = q2 + ((m2 != 0) & ((m2 ^ r3.l) >= 0)), f2 = q2 - ((m2 != 0) & ((m2 ^ r3.l) < 0));
-    const int c3 = q3 + ((m3 != 0) & ((m3 ^ r3.u) >= 0)), f3 = q3 - ((m3 != 0) & ((m3 ^ r3.u) < 0));
-    r2.l = max(r2.l, min(min(c0, c1), min(c2, c3)));
-    r2.u = min(r2.u, max(max(f0, f1), max(f2, f3)));
+    // The reference takes the min of cdiv and the max of fdiv over the four
+    // corners (x_i, z_j).  Here z is sign-definite (z > 0 or z < 0 after the
+    // zero endpoints were moved), so a / b is monotone in each argument over
+    // the box and its extremes sit at corners a sign analysis names; ceil and
+    // floor are monotone, so cdiv / fdiv at those corners are the corner
+    // minimum / maximum: two divisions instead of eight.  (An empty x gives
+    // other values than the corner search, but then the failure is already
+    // flagged and the bounds are not used.)  r1.l > MINF here, so no quotient
+    // overflows int32.
+    const bool zpos = r3.l > 0;
+    int al, bl, au, bu;  // min a/b at (al, bl), max a/b at (au, bu)
+    if (zpos) {
+      al = r1.l;
+      bl = r1.l >= 0 ? r3.u : r3.l;
+      au = r1.u;
+      bu = r1.u >= 0 ? r3.l : r3.u;
+    } else {
+      al = r1.u;
+      bl = r1.u >= 0 ? r3.u : r3.l;
+      au = r1.l;
+      bu = r1.l >= 0 ? r3.l : r3.u;
+    }
+    // A bound moves only when the quotient passes it: cdiv(a, b) > n iff
+    // a / b > n iff a > n * b (b > 0) or a < n * b (b < 0), and
+    // fdiv(a, b) < n iff a < n * b (b > 0) or a > n * b (b < 0) -- one exact
+    // 64-bit product instead of a division when nothing would change.
+    const long long nl = (long long)r2.l * bl, nu = (long long)r2.u * bu;
+    if (bl > 0 ? (long long)al > nl : (long long)al < nl) {
+      int q, m;
+      qr32(al, bl, q, m);
+      // cdiv = q + (r != 0 && sign(r) == sign(b))
+      r2.l = max(r2.l, q + ((m != 0) & ((m ^ bl) >= 0)));
+    }
+    if (bu > 0 ? (long long)au < nu : (long long)au > nu) {
+      int q, m;
+      qr32(au, bu, q, m);
+      // fdiv = q - (r != 0 && sign(r) != sign(b))
+      r2.u = min(r2.u, q - ((m != 0) & ((m ^ bu) < 0)));
+    }
   }
 }
 
@@ -163,10 +188,19 @@ static __device__ __forceinline__ void itv_div(int op, Itv &r1, Itv &r2, Itv &r3
     if (r3.u == 0) r3.u = -1;
     if (r2.l == MINF || r2.u == INF || r3.l == MINF || r3.u == INF) return;
     if (is_bot(r3)) return;
-    long long t1 = d_div(op, r2.l, r3.l), t2 = d_div(op, r2.l, r3.u);
-    long long t3 = d_div(op, r2.u, r3.l), t4 = d_div(op, r2.u, r3.u);
-    r1.l = cl(mx(r1.l, mn(mn(t1, t2), mn(t3, t4))));
-    r1.u = cl(mn(r1.u, mx(mx(t1, t2), mx(t3, t4))));
+    // The reference's min / max over the four corners: z is sign-definite
+    // here and every one of the four divisions is monotone in y / z, so the
+    // extremes are at the corners a sign analysis names (as in mul_inv).
+    long long lo, hi;
+    if (r3.l > 0) {
+      lo = d_div(op, r2.l, r2.l >= 0 ? r3.u : r3.l);
+      hi = d_div(op, r2.u, r2.u >= 0 ? r3.l : r3.u);
+    } else {
+      lo = d_div(op, r2.u, r2.u >= 0 ? r3.u : r3.l);
+      hi = d_div(op, r2.l, r2.l >= 0 ? r3.l : r3.u);
+    }
+    r1.l = cl(mx(r1.l, lo));
+    r1.u = cl(mn(r1.u, hi));
   }
 }
 
