@@ -494,7 +494,6 @@ __global__ void __launch_bounds__(512) k_nodes(NodeArgs a) {
 // probe window is full falls back to epoch stamps in global memory for that
 // key (a key takes the same path for as long as its set is not cleared).
 
-constexpr int NODE_BLOCK = 256;
 constexpr int CAND_LOG = 11, CHG_LOG = 10, TOUCH_LOG = 11, MAX_PROBE = 16;
 
 struct EvArgs {
@@ -586,7 +585,7 @@ struct NodeEvStore {
 };
 
 // Inclusive prefix sum of `x` over the CTA (blockDim.x a multiple of 32,
-// at most NODE_BLOCK); s_warp holds 32 ints.
+// at most 1024); s_warp holds 32 ints.
 __device__ __forceinline__ int block_scan_incl(int x, int *s_warp) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -612,13 +611,14 @@ __device__ __forceinline__ int block_scan_incl(int x, int *s_warp) {
   return r;
 }
 
-// MINB: resident CTAs per SM the register budget is sized for (more nodes in
-// flight against fewer registers per thread).
-template <int MINB>
-__global__ void __launch_bounds__(NODE_BLOCK, MINB) k_nodes_events(EvArgs a) {
+// NB threads per CTA (one node per CTA); MINB: resident CTAs per SM the
+// register budget is sized for (more nodes in flight against fewer registers
+// per thread).
+template <int NB, int MINB>
+__global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
   __shared__ int s_node, s_ncand, s_nd[2], s_nt;
   __shared__ int s_cand_set[1 << CAND_LOG], s_chg_set[1 << CHG_LOG], s_touch_set[1 << TOUCH_LOG];
-  __shared__ int s_beg[NODE_BLOCK], s_end[NODE_BLOCK], s_warp[32];
+  __shared__ int s_beg[NB], s_end[NB], s_warp[32];
   const size_t nv = (size_t)a.nvars;
   const int tid = threadIdx.x;
   int2 *ws = a.ws + blockIdx.x * nv;
@@ -848,13 +848,19 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
                           int32_t *out_wub = nullptr) {
   int r;
   if ((r = ensure_events_graph(ctx, b))) return r;
-  const int block = NODE_BLOCK;
-  // variant 1..5: the kernel sized for 2, 3, 4, 6, 8 resident CTAs per SM
-  static const void *const kNodeVariants[] = {(const void *)k_nodes_events<2>, (const void *)k_nodes_events<3>,
-                                              (const void *)k_nodes_events<4>, (const void *)k_nodes_events<6>,
-                                              (const void *)k_nodes_events<8>};
-  const int nvar = opts.variant >= 1 && opts.variant <= 5 ? opts.variant : 5;
-  const void *kfn = kNodeVariants[nvar - 1];
+  // variants 1..7: (threads per CTA, resident CTAs per SM the registers are sized for)
+  struct NodeVariant {
+    int block;
+    const void *fn;
+  };
+  static const NodeVariant kNodeVariants[] = {
+      {256, (const void *)k_nodes_events<256, 2>}, {256, (const void *)k_nodes_events<256, 3>},
+      {256, (const void *)k_nodes_events<256, 4>}, {256, (const void *)k_nodes_events<256, 6>},
+      {256, (const void *)k_nodes_events<256, 8>}, {128, (const void *)k_nodes_events<128, 8>},
+      {128, (const void *)k_nodes_events<128, 10>}};
+  const int nvar = opts.variant >= 1 && opts.variant <= 7 ? opts.variant : 6;
+  const int block = kNodeVariants[nvar - 1].block;
+  const void *kfn = kNodeVariants[nvar - 1].fn;
   int occ = 0;
   PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, block, 0));
   occ = std::max(occ, 1);

@@ -141,9 +141,10 @@ def test_nodes_events_parity(seed, P, oracle):
     np.testing.assert_array_equal(l2[ok], olb[ok])
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7])
 def test_nodes_events_variants(variant, P, oracle):
-    """The event node kernel sized for 2, 3, 4, 6 and 8 resident CTAs per SM."""
+    """The event node kernel: 256 threads sized for 2, 3, 4, 6 and 8 resident
+    CTAs per SM, 128 threads for 8 and 10."""
     ctx, (blb, bub), off, var, lb, ub = _nodes_setup(P, seed=4, nnodes=300)
     status, olb, oub, _, _ = ctx.fixpoint_nodes(off, var, lb, ub, sched=P.SCHED_EVENTS, variant=variant)
     op, x, y, z = ctx.bytecode()

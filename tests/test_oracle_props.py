@@ -193,3 +193,46 @@ def test_oracle_search_matches_reference_search(order, oracle):
         np.testing.assert_array_equal(sols, np.array(ref).reshape(-1, len(dec)))
     rc, _, info = oracle.search(*args, s, dec, order=order, max_nodes=10)
     assert rc == oracle.TIMEOUT and info["nodes"] == 10
+
+
+def test_quotient_extremes_at_sign_analysis_corners():
+    """The premise of the device's MUL inverse and division forward: for a
+    sign-definite divisor box, the min / max over the four corners of each
+    integer division (truncating, floor, ceiling, Euclidean) is the division
+    at the corner a sign analysis names; and the narrowing tests
+    cdiv(a, b) > n iff a > n b (b > 0) / a < n b (b < 0), fdiv(a, b) < n iff
+    a < n b (b > 0) / a > n b (b < 0) are exact."""
+    def tdiv(a, b):
+        q = abs(a) // abs(b)
+        return q if (a >= 0) == (b > 0) else -q
+
+    def fdiv(a, b):
+        return a // b
+
+    def cdiv(a, b):
+        return -((-a) // b)
+
+    def ediv(a, b):
+        q = tdiv(a, b)
+        return q - 1 if a - q * b < 0 and b > 0 else (q + 1 if a - q * b < 0 else q)
+
+    R = range(-9, 10)
+    for d in (tdiv, fdiv, cdiv, ediv):
+        for yl in R:
+            for yu in range(yl, 10):
+                for zl in R:
+                    for zu in range(zl, 10):
+                        if not (zl > 0 or zu < 0):
+                            continue
+                        c = [d(a, b) for a in (yl, yu) for b in (zl, zu)]
+                        if zl > 0:
+                            lo, hi = d(yl, zu if yl >= 0 else zl), d(yu, zl if yu >= 0 else zu)
+                        else:
+                            lo, hi = d(yu, zu if yu >= 0 else zl), d(yl, zl if yl >= 0 else zu)
+                        assert (lo, hi) == (min(c), max(c))
+    vals = list(range(-12, 13)) + [-2**31, -2**31 + 1, 2**31 - 1, -10**6, 10**6]
+    for a in vals:
+        for b in [v for v in vals if v != 0]:
+            for n in vals:
+                assert (cdiv(a, b) > n) == ((a > n * b) if b > 0 else (a < n * b))
+                assert (fdiv(a, b) < n) == ((a < n * b) if b > 0 else (a > n * b))
