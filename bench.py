@@ -407,6 +407,7 @@ def run_nodes(args):
         off, var, lb, ub = shard.select_nodes(off, var, lb, ub, parts[rank])
     nn = len(off) - 1
     sched = pirgpu.SCHED_EVENTS if args.node_sched == "events" else pirgpu.SCHED_AC1
+    tuned = ctx.autotune_nodes(off, var, lb, ub) if sched == pirgpu.SCHED_EVENTS else None
     for _ in range(args.warmup):
         ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=sched)
         cr.flush_l2()
@@ -464,16 +465,19 @@ def run_nodes(args):
     # end to end through the C ABI: host tightenings in, per-node status and
     # rounds out (what a search driver reads; the sequential loop reads the
     # same), and separately with every node's store downloaded as well
+    # (inputs from pinned host buffers, filled before the timed calls)
     e2e_t = e2e_stores_t = None
     if extras and not args.no_e2e:
+        p_off, p_var, p_lb, p_ub = (cr.pinned(len(a)) for a in (off, var, lb, ub))
+        p_off[:], p_var[:], p_lb[:], p_ub[:] = off, var, lb, ub
         ts = []
-        for _ in range(3):
+        for _ in range(5):
             t0 = time.perf_counter()
-            ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=sched)
+            ctx.fixpoint_nodes(p_off, p_var, p_lb, p_ub, want_stores=False, sched=sched)
             ts.append(time.perf_counter() - t0)
-        e2e_t = min(ts)
+        e2e_t = float(np.median(ts))
         t0 = time.perf_counter()
-        ctx.fixpoint_nodes(off, var, lb, ub, want_stores=True, sched=sched)
+        ctx.fixpoint_nodes(p_off, p_var, p_lb, p_ub, want_stores=True, sched=sched)
         e2e_stores_t = time.perf_counter() - t0
     hbm, hbm_src = peaks()
     achieved = (execs * ALG_BYTES_PER_EXEC + joins * ALG_BYTES_PER_JOIN) / dev_s / 1e9
@@ -500,6 +504,7 @@ def run_nodes(args):
                    "nodes_ok": n_ok, "nodes_failed": n_failed,
                    "max_rounds": max_rounds, "mean_rounds_rank0": float(rounds.mean()) if nn else 0.0,
                    "schedule": args.node_sched, "executions_per_step": execs // args.steps,
+                   "node_kernel_variant": list(tuned) if tuned else None,
                    "batched_ac1_ms": st_ac1["device_ms"], "batched_ac1_executions": st_ac1["executions"],
                    "first_batch_on_new_base_ms": first_ms},
         "plain_sequential": {"nodes_per_s_device": seq_dev_rate, "nodes_per_s_wall": seq_wall_rate,
@@ -594,8 +599,16 @@ def run_uneven(args):
                                                                           lb0, ub0, parts[rank])
         insts = [insts_all[i] for i in parts[rank]]
     ctx = pirgpu.Context(local)
+    # inputs in pinned host buffers (the stores are updated in place: reset before every step)
+    pinned = []
+    for a in (op, x, y, z):
+        b = cr.pinned(len(a))
+        b[:] = a
+        pinned.append(b)
+    op, x, y, z = pinned
+    lb, ub = cr.pinned(len(lb0)), cr.pinned(len(ub0))
     for _ in range(args.warmup):
-        lb, ub = lb0.copy(), ub0.copy()
+        lb[:], ub[:] = lb0, ub0
         ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
     if dist:
         dist.barrier()
@@ -604,7 +617,7 @@ def run_uneven(args):
     clk.start()
     runs, walls, per = [], [], []
     for _ in range(args.steps):
-        lb, ub = lb0.copy(), ub0.copy()
+        lb[:], ub[:] = lb0, ub0
         t0 = time.perf_counter()
         status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
         walls.append(time.perf_counter() - t0)

@@ -185,6 +185,17 @@ int pir_fixpoint_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, cons
                        int32_t *out_lb, int32_t *out_ub, int32_t *out_status,
                        int32_t *out_rounds, pir_stats *stats);
 
+/* Number of event node kernel variants (threads per CTA x resident CTAs per
+ * SM) that pir_autotune_nodes chooses from; opts.variant of the node calls. */
+#define PIR_NODE_VARIANTS 7
+
+/* Autotuner of the batched search nodes (event schedule): runs the batch with
+ * every node kernel variant (twice, keeping the faster run) and keeps the
+ * fastest for this context's later node calls with opts.variant = 0.  The
+ * node results are not returned.  out_variant / out_ms may be NULL. */
+int pir_autotune_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, const int32_t *var,
+                       const int32_t *lb, const int32_t *ub, int32_t *out_variant, float *out_ms);
+
 /* pir_fixpoint_nodes for a search driver: instead of whole stores, every node
  * reports the final bounds of the `nwatch` variables `watch` (out_wlb/out_wub,
  * nnodes x nwatch, node-major).  Runs the event schedule; the context's store

@@ -63,6 +63,7 @@ struct BatchState {
   void *d_ev = nullptr;  // per-CTA scratch block
   size_t cap_ev = 0;
   long long ev_base_version = -1;  // store version the first ev_valid_slots working stores equal
+  int node_variant = 0;            // event node kernel variant chosen by pir_autotune_nodes (0: default)
   int ev_valid_slots = 0;
   int *d_watch = nullptr;  // watched variables | their bounds per node
   size_t cap_watch = 0;
@@ -858,7 +859,9 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
       {256, (const void *)k_nodes_events<256, 4>}, {256, (const void *)k_nodes_events<256, 6>},
       {256, (const void *)k_nodes_events<256, 8>}, {128, (const void *)k_nodes_events<128, 8>},
       {128, (const void *)k_nodes_events<128, 10>}};
-  const int nvar = opts.variant >= 1 && opts.variant <= 7 ? opts.variant : 6;
+  static_assert(sizeof(kNodeVariants) / sizeof(kNodeVariants[0]) == PIR_NODE_VARIANTS, "node variant count");
+  const int nvar = opts.variant >= 1 && opts.variant <= PIR_NODE_VARIANTS ? opts.variant
+                   : (b->node_variant > 0 ? b->node_variant : 6);
   const int block = kNodeVariants[nvar - 1].block;
   const void *kfn = kNodeVariants[nvar - 1].fn;
   int occ = 0;
@@ -1358,5 +1361,37 @@ extern "C" int pir_fixpoint_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t
   st.narrowed = (int64_t)hnar;
   st.status = worst;
   if (stats) *stats = st;
+  return PIR_OK;
+}
+
+extern "C" int pir_autotune_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, const int32_t *var,
+                                  const int32_t *lb, const int32_t *ub, int32_t *out_variant, float *out_ms) {
+  if (!ctx) return PIR_EINVAL;
+  if (out_variant) *out_variant = 0;
+  if (out_ms) *out_ms = 0.f;
+  if (nnodes <= 0 || !off) return set_err(ctx, PIR_EINVAL, "no nodes to tune on");
+  std::vector<int32_t> status((size_t)nnodes);
+  int best = 0;
+  float best_ms = 0.f;
+  for (int v = 1; v <= PIR_NODE_VARIANTS; ++v) {
+    pir_opts o;
+    std::memset(&o, 0, sizeof(o));
+    o.sched = PIR_SCHED_EVENTS;
+    o.variant = v;
+    float t = -1.f;
+    for (int rep = 0; rep < 2; ++rep) {  // the first run may load the working stores
+      pir_stats st;
+      const int r = pir_fixpoint_nodes(ctx, nnodes, off, var, lb, ub, &o, nullptr, nullptr, status.data(), nullptr, &st);
+      if (r != PIR_OK) return r;
+      if (t < 0.f || st.device_ms < t) t = st.device_ms;
+    }
+    if (best == 0 || t < best_ms) {
+      best = v;
+      best_ms = t;
+    }
+  }
+  batch(ctx)->node_variant = best;
+  if (out_variant) *out_variant = best;
+  if (out_ms) *out_ms = best_ms;
   return PIR_OK;
 }

@@ -20,6 +20,7 @@ STATUS = ["OK", "FAILED", "TIMEOUT", "BARRIER_TIMEOUT", "EINVAL", "ECUDA", "ENOM
 MODE_AUTO, MODE_PERSISTENT, MODE_HOSTLOOP, MODE_SMEM = range(4)
 SCHED_AC1, SCHED_LEARNED, SCHED_EVENTS = range(3)
 PERSISTENT_VARIANTS = 10  # PIR_PERSISTENT_VARIANTS
+NODE_VARIANTS = 7  # PIR_NODE_VARIANTS
 INF = 2**31 - 1
 MINF = -2**31
 
@@ -107,6 +108,7 @@ SIGNATURES = [
                                           ctypes.POINTER(Opts), _I32P, _I32P, _I32P, _I32P,
                                           ctypes.POINTER(Stats)]),
     ("pir_sched_score", ctypes.c_int, [_P, ctypes.c_int32, _F32P, _F32P]),
+    ("pir_autotune_nodes", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P, _I32P, _I32P, _F32P]),
     ("pir_fixpoint_nodes_watch", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P, _I32P,
                                                 ctypes.POINTER(Opts), ctypes.c_int32, _I32P, _I32P, _I32P,
                                                 _I32P, _I32P, ctypes.POINTER(Stats)]),
@@ -335,6 +337,15 @@ class Context:
                                         _p32(status), _p32(rounds), ctypes.byref(s))
         self._check(rc)
         return status, out_lb, out_ub, rounds, s.asdict()
+
+    def autotune_nodes(self, off, var, lb, ub):
+        """Times the event node kernel variants on this batch; returns (variant, ms)."""
+        off, var, lb, ub = map(_c32, (off, var, lb, ub))
+        v = ctypes.c_int32(0)
+        ms = ctypes.c_float(0)
+        self._check(self._L.pir_autotune_nodes(self.h, len(off) - 1, _p32(off), _p32(var), _p32(lb), _p32(ub),
+                                               ctypes.byref(v), ctypes.byref(ms)))
+        return v.value, ms.value
 
     def sched_score(self, X):
         """Scores of feature rows X (n x 8) by the tensor-core inference MLP."""

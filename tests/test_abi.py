@@ -63,3 +63,4 @@ def test_python_constants_match_header():
     import pirgpu
     src = open(os.path.join(ROOT, "include", "pirgpu.h")).read()
     assert int(re.search(r"#define PIR_PERSISTENT_VARIANTS (\d+)", src).group(1)) == pirgpu.PERSISTENT_VARIANTS
+    assert int(re.search(r"#define PIR_NODE_VARIANTS (\d+)", src).group(1)) == pirgpu.NODE_VARIANTS

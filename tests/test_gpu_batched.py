@@ -156,6 +156,20 @@ def test_nodes_events_variants(variant, P, oracle):
     np.testing.assert_array_equal(oub[ok], ostore[ok, :, 1])
 
 
+def test_nodes_autotune(P, oracle):
+    """pir_autotune_nodes picks one of the variants and later calls use it."""
+    ctx, (blb, bub), off, var, lb, ub = _nodes_setup(P, seed=6, nnodes=256)
+    v, ms = ctx.autotune_nodes(off, var, lb, ub)
+    assert 1 <= v <= P.NODE_VARIANTS and ms > 0
+    status, olb, oub, _, _ = ctx.fixpoint_nodes(off, var, lb, ub, sched=P.SCHED_EVENTS)
+    op, x, y, z = ctx.bytecode()
+    base = np.ascontiguousarray(np.stack([blb, bub], 1))
+    ostatus, ostore, _ = oracle.fixpoint_nodes(op, x, y, z, base, off, var, lb, ub)
+    np.testing.assert_array_equal(status, ostatus)
+    ok = ostatus == oracle.OK
+    np.testing.assert_array_equal(olb[ok], ostore[ok, :, 0])
+
+
 def test_nodes_events_follow_a_changed_base(P, oracle):
     """The working stores are reused while the base store is unchanged and
     reloaded when it changes (embed + fixpoint, restore, a smaller batch):
