@@ -284,7 +284,8 @@ int pir_fixpoint_static(const int32_t *d_op, const int32_t *d_x, const int32_t *
 /* Learned propagator scheduler (used by pir_fixpoint with opts.sched =
  * PIR_SCHED_LEARNED; no counterpart in the reference, whose fixpoint loop is
  * the caller's).  An 8 -> 32 -> 32 -> 1 MLP with BF16 weights scores every
- * propagator each round; the top opts.wake_fraction of them run; a round of
+ * propagator each round (on the tensor cores); each CTA runs the top
+ * opts.wake_fraction of the propagators it scored; a round of
  * woken propagators without change is followed by a full certifying sweep,
  * so the fixpoint is the plain one bit for bit.
  *

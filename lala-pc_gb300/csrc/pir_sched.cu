@@ -6,8 +6,10 @@
 //   3-5  log2(width + 1) / 32 of x, y, z
 //   6    rounds since any of x, y, z last narrowed, clamped to 64, / 64
 //   7    log2(deg x + deg y + deg z) / 16 (static)
-// and the round runs only the top-scored propagators (a wake fraction of the
-// bytecode).  When a round of woken propagators changes nothing, one full AC-1
+// and the round runs only the top-scored propagators (each CTA wakes a fraction
+// of the propagators it scored, by a threshold on its own score histogram, so
+// a learned round needs one grid barrier).  When a round of woken propagators
+// changes nothing, one full AC-1
 // sweep certifies the fixpoint; if it changes anything, the learned rounds
 // resume.  Propagators are monotone, so any fair schedule that ends with a
 // no-change full sweep reaches the same fixpoint as the plain method: the
@@ -50,7 +52,6 @@ struct SchedState {
   int *d_deg = nullptr;       // variable degree
   unsigned char *d_pdeg = nullptr;  // per-propagator degree feature (x16 fixed point)
   float *d_score = nullptr;
-  unsigned *d_hist = nullptr;  // 2 x HIST_BINS
   unsigned long long *d_counts = nullptr;  // woken executions, samples
   float *d_tx = nullptr, *d_ty = nullptr;  // trace samples
   long long tcap = 0, tcount = 0;
@@ -61,7 +62,7 @@ void destroy_sched_state(pirgpu_ctx *ctx) {
   SchedState *s = ctx->sched;
   if (!s) return;
   void *ptrs[] = {s->d_param, s->d_m, s->d_v, s->d_grad, s->d_loss, s->d_wbf, s->d_var_last, s->d_deg,
-                  s->d_pdeg, s->d_score, s->d_hist, s->d_counts, s->d_tx, s->d_ty};
+                  s->d_pdeg, s->d_score, s->d_counts, s->d_tx, s->d_ty};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete s;
@@ -235,17 +236,16 @@ struct StampStore {
 
 __device__ __forceinline__ int bc_get(const int *a, long long i) { return __ldg(a + i); }
 
-// Threshold bin of the top-k: the highest bin b such that the count of scores
-// in bins >= b reaches k (bin 0 when it never does).  Computed redundantly by
-// every CTA from the global histogram (2048 bins) with a block-wide suffix
-// sum: thread t owns the bins of segment t counted from the top.
-__device__ int select_bin(const unsigned *hist, unsigned long long k, unsigned *sh) {
+// Threshold bin of this CTA's top fraction: the highest bin b such that the
+// count of the CTA's scores in bins >= b reaches k = ceil(frac x the CTA's
+// scored propagators) (bin 0 when it never does), from the CTA's histogram
+// `sh` in shared memory, by a block-wide suffix sum: thread t owns the bins
+// of segment t counted from the top.
+__device__ int select_bin(const unsigned *sh, float frac) {
   __shared__ unsigned long long s_warp[32];
   __shared__ int s_bin;
   const int tid = threadIdx.x, nt = blockDim.x, per = (HIST_BINS + nt - 1) / nt;
-  for (int i = tid; i < HIST_BINS; i += nt) sh[i] = __ldcg(hist + i);
   if (tid == 0) s_bin = 0;
-  __syncthreads();
   const int hi = HIST_BINS - tid * per;  // segment [hi - per, hi)
   unsigned long long seg = 0;
   for (int b = hi - 1; b >= hi - per && b >= 0; --b) seg += sh[b];
@@ -267,6 +267,9 @@ __device__ int select_bin(const unsigned *hist, unsigned long long k, unsigned *
     if (lane < (nt >> 5)) s_warp[lane] = w;
   }
   __syncthreads();
+  const unsigned long long total = s_warp[(nt >> 5) - 1];
+  const unsigned long long k =
+      total ? (unsigned long long)fmax(1.0, ceil((double)frac * (double)total)) : 1ull;
   const unsigned long long incl = x + (warp ? s_warp[warp - 1] : 0ull), above = incl - seg;
   if (above < k && incl >= k) {
     // the crossing is in this segment: walk it from the top
@@ -291,18 +294,18 @@ struct LearnedArgs {
   const unsigned char *pdeg;
   const __nv_bfloat16 *wbf;
   float *score;
-  unsigned *hist;  // 2 x HIST_BINS, zeroed
   unsigned long long *counts;  // [0] woken executions
   Control *ctl;
   long long max_rounds;
   long long timeout_ns;
-  unsigned long long k;  // woken per round
+  float frac;  // fraction of each CTA's propagators woken per round
 };
 
-// Persistent learned fixpoint: per learned round, (A) score every propagator
-// and build the score histogram, grid barrier, (B) every CTA derives the top-k
-// threshold, (C) run the woken propagators, grid barrier with the change bit.
-// A learned round without change is followed by a certifying full sweep.
+// Persistent learned fixpoint: per learned round, (A) each CTA scores its
+// propagators into a histogram in shared memory, (B) derives the threshold of
+// its top fraction, (C) runs its woken propagators; one grid barrier per
+// round carries the change bit.  A learned round without change is followed
+// by a certifying full sweep.
 __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
   __shared__ float sw[NPARAM];
   __shared__ unsigned sh[HIST_BINS];
@@ -319,7 +322,6 @@ __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
   unsigned long long woken = 0, narrowed = 0;
   long long round = 0, nbar = 0;  // nbar: grid barriers passed (thread 0)
   bool certify = false;
-  int par = 0;
   for (;;) {
     ++round;
     const int r = (int)round;
@@ -347,17 +349,8 @@ __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
         }
       }
       __syncthreads();
-      unsigned *gh = a.hist + par * HIST_BINS;
-      for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x)
-        if (sh[i]) atomicAdd(gh + i, sh[i]);
-      __syncthreads();
-      if (threadIdx.x == 0) s_word = grid_sync_rot(a.ctl, gridDim.x, nbar++, 0, 0, a.timeout_ns);
-      __syncthreads();
-      if (s_word & BIT_ERROR) break;
-      // (B) threshold; CTA 0 clears the other histogram for the next round
-      const int bin = select_bin(gh, a.k, sh);
-      if (blockIdx.x == 0)
-        for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x) a.hist[(par ^ 1) * HIST_BINS + i] = 0;
+      // (B) this CTA's threshold: the propagators it scored are the ones it runs
+      const int bin = select_bin(sh, a.frac);
       // (C) woken propagators
       for (long long p = gtid; p < a.n; p += gstride) {
         if (hist_bin(__ldcg(a.score + p)) < bin) continue;
@@ -366,7 +359,6 @@ __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
         const Itv ia = st.load(X), ib = st.load(Y), ic = st.load(Z);
         changed += deduce_loaded(o, X, Y, Z, ia, ib, ic, st, failed);
       }
-      par ^= 1;
     } else {
       // certifying full sweep
       for (long long p = gtid; p < a.n; p += gstride) {
@@ -606,7 +598,6 @@ int ensure_params(pirgpu_ctx *ctx) {
       cudaMalloc(&s->d_v, b) != cudaSuccess || cudaMalloc(&s->d_grad, b) != cudaSuccess ||
       cudaMalloc(&s->d_loss, sizeof(float)) != cudaSuccess ||
       cudaMalloc(&s->d_wbf, NPARAM * sizeof(__nv_bfloat16)) != cudaSuccess ||
-      cudaMalloc(&s->d_hist, 2 * HIST_BINS * sizeof(unsigned)) != cudaSuccess ||
       cudaMalloc(&s->d_counts, 4 * sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     return set_err(ctx, PIR_ENOMEM, "scheduler parameters");
@@ -687,7 +678,6 @@ int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   if ((r = ensure_params(ctx)) || (r = ensure_graph(ctx)) || (r = reset_stamps(ctx))) return r;
   SchedState *s = sched(ctx);
   if ((r = reset_control(ctx))) return r;
-  PIR_CK(cudaMemsetAsync(s->d_hist, 0, 2 * HIST_BINS * sizeof(unsigned), ctx->stream));
   PIR_CK(cudaMemsetAsync(s->d_counts, 0, 4 * sizeof(unsigned long long), ctx->stream));
   const float frac = opts.wake_fraction > 0.f ? std::min(opts.wake_fraction, 1.f) : 1.f / 16.f;
   LearnedArgs a;
@@ -701,12 +691,11 @@ int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   a.pdeg = s->d_pdeg;
   a.wbf = s->d_wbf;
   a.score = s->d_score;
-  a.hist = s->d_hist;
   a.counts = s->d_counts;
   a.ctl = ctx->d_ctl;
   a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
   a.timeout_ns = opts.barrier_timeout_ns > 0 ? opts.barrier_timeout_ns : 2000000000ll;
-  a.k = (unsigned long long)std::max(1.0, std::ceil((double)frac * (double)ctx->n));
+  a.frac = frac;
   int occ = 0;
   PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fixpoint_learned, 256, 0));
   if (occ < 1) return set_err(ctx, PIR_ECUDA, "learned kernel does not fit on an SM");

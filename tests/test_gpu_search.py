@@ -106,3 +106,23 @@ def test_watch_matches_full_stores(P, oracle):
     ok = s1 == P.OK
     np.testing.assert_array_equal(wl[ok], fl[ok][:, watch])
     np.testing.assert_array_equal(wu[ok], fu[ok][:, watch])
+
+
+def test_bad_arguments_are_rejected(P):
+    """Errors come back as EINVAL before anything runs; the context stays usable."""
+    import workloads as W
+    inst = W.queens(6)
+    ctx = _ctx(P, inst)
+    for bad in ([0, 1, 10**6], [-1]):
+        with pytest.raises(P.PirError, match="EINVAL"):
+            ctx.search(bad)
+    with pytest.raises(P.PirError, match="EINVAL"):
+        ctx.search(np.arange(6), max_nodes=-1)
+    with pytest.raises(P.PirError, match="EINVAL"):
+        ctx.fixpoint_nodes_watch([0, 1], [0], [0], [1], [10**6])
+    with pytest.raises(P.PirError, match="EINVAL"):
+        ctx.fixpoint_nodes_watch([0, 1], [10**6], [0], [1], [0])
+    with pytest.raises(P.PirError, match="EINVAL"):
+        ctx.fixpoint(variant=P.PERSISTENT_VARIANTS + 1, mode=P.MODE_PERSISTENT)
+    status, sols, st = ctx.search(np.arange(6), max_solutions=10)
+    assert status == P.OK and st["solutions"] == 4
