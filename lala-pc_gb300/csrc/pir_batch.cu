@@ -217,28 +217,37 @@ __global__ void __launch_bounds__(512) k_instances(InstArgs a) {
 // they leave together after a barrier that follows the last remote read.
 constexpr int CLU = 8;
 
+// The store of a large instance spread over the shared memory of its cluster
+// (variable v in CTA v % CLU).  An interval is one 64-bit load of distributed
+// shared memory (the cluster barrier between rounds orders them); joins are
+// fire-and-forget cluster-scope reductions counted against the value read,
+// as RedStore does in HBM (a concurrent tighter join can make that an
+// over-count, which costs at most one more round).
 struct DsmStore {
-  int2 *base[CLU];  // the slot array of each CTA of the cluster (generic addresses)
-  __device__ __forceinline__ int2 *slot(int v) const { return base[v & (CLU - 1)] + (v >> 3); }
+  int2 *mine;  // this CTA's slot array (generic address)
+  // v's slot: slot v / CLU of CTA v % CLU, the same offset in that CTA's
+  // shared memory (mapa)
+  __device__ __forceinline__ int2 *slot(int v) const {
+    unsigned long long a;
+    asm("mapa.u64 %0, %1, %2;" : "=l"(a) : "l"(mine + (v >> 3)), "r"(v & (CLU - 1)));
+    return reinterpret_cast<int2 *>(a);
+  }
   __device__ __forceinline__ Itv load(int v) const {
-    const volatile int2 *p = slot(v);
-    return mk(p->x, p->y);
+    const int2 t = *slot(v);
+    return mk(t.x, t.y);
   }
   __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
     int n = 0;
     int2 *p = slot(v);
-    int nl = seen.l, nu = seen.u;
     if (r.l > seen.l) {
-      const int old = atomicMax(&p->x, r.l);
-      n += old < r.l;
-      nl = max(old, r.l);
+      asm volatile("red.relaxed.cluster.max.s32 [%0], %1;" ::"l"(&p->x), "r"(r.l) : "memory");
+      ++n;
     }
     if (r.u < seen.u) {
-      const int old = atomicMin(&p->y, r.u);
-      n += old > r.u;
-      nu = min(old, r.u);
+      asm volatile("red.relaxed.cluster.min.s32 [%0], %1;" ::"l"(&p->y), "r"(r.u) : "memory");
+      ++n;
     }
-    if (n && is_bot(mk(nl, nu))) failed = 1;
+    if (n && is_bot(mk(max(seen.l, r.l), min(seen.u, r.u)))) failed = 1;
     return n;
   }
 };
@@ -263,8 +272,7 @@ __global__ void __launch_bounds__(512, 1) k_instances_cluster(CluArgs a) {
   const int rank = (int)cluster.block_rank();
   int2 *mine = reinterpret_cast<int2 *>(sm);
   DsmStore st;
-#pragma unroll
-  for (int k = 0; k < CLU; ++k) st.base[k] = cluster.map_shared_rank(mine, k);
+  st.mine = mine;
   unsigned *flags0 = cluster.map_shared_rank(&s_flags[0][0], 0);
   int *inst0 = cluster.map_shared_rank(&s_inst, 0);
   const int ctid = rank * blockDim.x + threadIdx.x, cstride = CLU * blockDim.x;
