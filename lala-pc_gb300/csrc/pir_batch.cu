@@ -11,8 +11,10 @@
 //   applying one propagator to its 32 nodes reads each interval with one
 //   coalesced 256-byte access and all lanes run the same opcode.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include <cooperative_groups.h>
@@ -67,6 +69,8 @@ struct BatchState {
   int ev_valid_slots = 0;
   int *d_watch = nullptr;  // watched variables | their bounds per node
   size_t cap_watch = 0;
+  int *h_stage = nullptr;  // pinned host staging of the installed instance bytecode
+  size_t cap_stage = 0;
   unsigned char *d_ent = nullptr;  // entailed-at-base flags per propagator
   size_t cap_ent = 0;
   long long ent_store_version = -1, ent_bc_version = -1;
@@ -75,6 +79,7 @@ struct BatchState {
 void destroy_batch_state(pirgpu_ctx *ctx) {
   BatchState *b = ctx->batch;
   if (!b) return;
+  if (b->h_stage) cudaFreeHost(b->h_stage);
   void *ptrs[] = {b->d_bc, b->d_off,    b->d_store, b->d_aux,     b->d_iout, b->d_nstore, b->d_tight,
                   b->d_nout, b->d_nio, b->d_bc4, b->d_adj_ptr, b->d_adj, b->d_ev, b->d_ent, b->d_watch};
   for (void *p : ptrs)
@@ -1041,6 +1046,23 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
 
 using namespace pirgpu;
 
+// fn(j) for j = 0 .. count-1 on the host's threads (dynamic assignment).
+template <class F>
+static void host_parallel(int count, F fn) {
+  const int nt = (int)std::max(1u, std::min({16u, std::thread::hardware_concurrency(), (unsigned)std::max(count, 1)}));
+  if (nt <= 1 || count < 2) {
+    for (int j = 0; j < count; ++j) fn(j);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nt; ++t)
+    pool.emplace_back([&] {
+      for (int j; (j = next.fetch_add(1)) < count;) fn(j);
+    });
+  for (auto &th : pool) th.join();
+}
+
 extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int64_t *prop_off, const int64_t *var_off,
                                       const int32_t *op, const int32_t *x, const int32_t *y, const int32_t *z,
                                       int32_t *lb, int32_t *ub, const pir_opts *opts_in, int32_t *out_status,
@@ -1060,14 +1082,26 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   }
   const long long nprops = prop_off[ninst], nvars = var_off[ninst];
   if (nprops > 0 && (!op || !x || !y || !z)) return set_err(ctx, PIR_EINVAL, "null bytecode");
-  for (int j = 0; j < ninst; ++j) {
+  // validation on the host's threads: the first bad instance is reported
+  std::atomic<int> bad_inst{INT32_MAX}, bad_kind{0};
+  host_parallel(ninst, [&](int j) {
     const long long nv = var_off[j + 1] - var_off[j];
     for (long long i = prop_off[j]; i < prop_off[j + 1]; ++i) {
-      if (op[i] < 0 || op[i] >= OP_COUNT) return set_err(ctx, PIR_EINVAL, "instance %d: bad opcode", j);
-      if (x[i] < 0 || x[i] >= nv || y[i] < 0 || y[i] >= nv || z[i] < 0 || z[i] >= nv)
-        return set_err(ctx, PIR_EINVAL, "instance %d: var index out of range", j);
+      const int kind = (op[i] < 0 || op[i] >= OP_COUNT) ? 1
+                       : (x[i] < 0 || x[i] >= nv || y[i] < 0 || y[i] >= nv || z[i] < 0 || z[i] >= nv) ? 2
+                                                                                                         : 0;
+      if (kind) {
+        int cur = bad_inst.load();
+        while (j < cur && !bad_inst.compare_exchange_weak(cur, j)) {
+        }
+        if (bad_inst.load() == j) bad_kind.store(kind);
+        return;
+      }
     }
-  }
+  });
+  if (bad_inst.load() != INT32_MAX)
+    return set_err(ctx, PIR_EINVAL, bad_kind.load() == 1 ? "instance %d: bad opcode" : "instance %d: var index out of range",
+                   bad_inst.load());
   PIR_CK(cudaSetDevice(ctx->device));
   BatchState *b = batch(ctx);
   // Padded chunk layout: instance j owns chunks coff[j] .. coff[j+1]-1.
@@ -1080,12 +1114,24 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   }
   voff[ninst] = var_off[ninst];
   const long long nchunks = coff[ninst];
-  std::vector<int> hb((size_t)std::max<long long>(nchunks, 1) * 16);
-  int *hop = hb.data(), *hx = hop + 4 * nchunks, *hy = hx + 4 * nchunks, *hz = hy + 4 * nchunks;
+  // pinned staging (every slot below is written: no clearing)
+  const size_t stage_ints = (size_t)std::max<long long>(nchunks, 1) * 16;
+  if (b->cap_stage < stage_ints) {
+    if (b->h_stage) cudaFreeHost(b->h_stage);
+    b->h_stage = nullptr;
+    b->cap_stage = 0;
+    if (cudaMallocHost(&b->h_stage, stage_ints * sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      return set_err(ctx, PIR_ENOMEM, "pinned staging (%zu bytes)", stage_ints * sizeof(int));
+    }
+    b->cap_stage = stage_ints;
+  }
+  int *hop = b->h_stage, *hx = hop + 4 * nchunks, *hy = hx + 4 * nchunks, *hz = hy + 4 * nchunks;
   // Install order: each instance's propagators grouped by opcode with a
   // stable counting sort (the order the reference's GPU path sorts by,
-  // pir.hpp:339-341), so that warps run one opcode at a time.
-  for (int j = 0; j < ninst; ++j) {
+  // pir.hpp:339-341), so that warps run one opcode at a time; instances on
+  // the host's threads (disjoint output ranges).
+  host_parallel(ninst, [&](int j) {
     const long long p0 = prop_off[j], p1 = prop_off[j + 1], d0 = coff[j] * 4, d1 = coff[j + 1] * 4;
     long long start[OP_COUNT + 1] = {0};
     for (long long i = p0; i < p1; ++i) ++start[op[i] + 1];
@@ -1101,7 +1147,7 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
       hop[d] = OP_NOP;
       hx[d] = hy[d] = hz[d] = 0;
     }
-  }
+  });
   std::vector<int> order(ninst);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
@@ -1133,7 +1179,7 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   if ((r = ensure(ctx, (void **)&b->d_aux, &b->cap_aux, aux_ints * sizeof(int)))) return r;
   if ((r = ensure(ctx, (void **)&b->d_iout, &b->cap_iout, (size_t)ninst * sizeof(InstOut)))) return r;
   int *d_order = b->d_aux, *d_next = d_order + ninst, *d_lb = d_next + 4, *d_ub = d_lb + nvars;
-  PIR_CK(cudaMemcpyAsync(b->d_bc, hb.data(), (size_t)nchunks * 64, cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaMemcpyAsync(b->d_bc, b->h_stage, (size_t)nchunks * 64, cudaMemcpyHostToDevice, ctx->stream));
   PIR_CK(cudaMemcpyAsync(b->d_off, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
   PIR_CK(cudaMemcpyAsync(d_order, order.data(), ninst * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   PIR_CK(cudaMemsetAsync(d_next, 0, 4 * sizeof(int), ctx->stream));

@@ -244,3 +244,22 @@ def test_instances_cluster_path(P, oracle):
         np.testing.assert_array_equal(ub[var_off[j]:var_off[j + 1]], s[:, 1])
     capped, r2, _, _ = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb.copy(), ub.copy(), max_rounds=1)
     assert np.all(r2 <= 1)
+
+
+def test_instances_reject_bad_bytecode(P):
+    """Validation (on the host's threads) names the first bad instance and
+    leaves the stores untouched."""
+    import workloads as W
+    insts = [W.plain(500, 2000, 1000, 70 + j) for j in range(40)]
+    prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
+    lb0 = lb.copy()
+    ctx = P.Context(0)
+    for j_bad, field, value, msg in [(17, "x", 10**6, "instance 17: var index out of range"),
+                                      (3, "op", 11, "instance 3: bad opcode"),
+                                      (31, "z", -1, "instance 31: var index out of range")]:
+        arrs = dict(op=op.copy(), x=x.copy(), y=y.copy(), z=z.copy())
+        arrs[field][prop_off[j_bad] + 5] = value
+        arrs["x"][prop_off[39] + 1] = 10**6  # a later bad instance is not the one reported
+        with pytest.raises(P.PirError, match=msg):
+            ctx.fixpoint_instances(prop_off, var_off, arrs["op"], arrs["x"], arrs["y"], arrs["z"], lb, ub)
+        np.testing.assert_array_equal(lb, lb0)
