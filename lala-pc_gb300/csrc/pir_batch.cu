@@ -228,6 +228,8 @@ constexpr int CLU = 8;
 // fire-and-forget cluster-scope reductions counted against the value read,
 // as RedStore does in HBM (a concurrent tighter join can make that an
 // over-count, which costs at most one more round).
+constexpr int CLU_BLOCK = 1024;  // threads per CTA of the cluster kernel
+
 struct DsmStore {
   int2 *mine;  // this CTA's slot array (generic address)
   // v's slot: slot v / CLU of CTA v % CLU, the same offset in that CTA's
@@ -268,7 +270,7 @@ struct CluArgs {
   long long max_rounds;
 };
 
-__global__ void __launch_bounds__(512, 1) k_instances_cluster(CluArgs a) {
+__global__ void __launch_bounds__(CLU_BLOCK, 1) k_instances_cluster(CluArgs a) {
   extern __shared__ int4 sm[];
   __shared__ int s_inst;
   __shared__ unsigned s_flags[3][2];  // rank 0's: [round % 3][changed, failed]
@@ -325,7 +327,9 @@ __global__ void __launch_bounds__(512, 1) k_instances_cluster(CluArgs a) {
       const int par = (int)(round % 3);
       if (rank == 0 && threadIdx.x == 0) s_flags[(round + 1) % 3][0] = s_flags[(round + 1) % 3][1] = 0;
       int ch = 0, f = 0;
-      for (int c = ctid; c < nch; c += cstride) ch += sweep_chunk(bc, c, st, f);
+      // one propagator per thread and step: 1,024 threads of 64 registers keep
+      // twice the warps of 512 x 4-wide steps resident
+      for (int c = ctid; c < nch * 4; c += cstride) ch += sweep_step<1>(bc, c, st, f);
       narrowed += ch;
       const int any_ch = __syncthreads_or(ch), any_f = __syncthreads_or(f);
       if (threadIdx.x == 0) {
@@ -1241,7 +1245,7 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
     std::memset(&cfg, 0, sizeof(cfg));
     const int nclusters = std::max(1, std::min(nbig, ctx->num_sms / CLU));
     cfg.gridDim = dim3(nclusters * CLU);
-    cfg.blockDim = dim3(512);
+    cfg.blockDim = dim3(CLU_BLOCK);
     cfg.dynamicSmemBytes = clu_cap;
     cfg.stream = ctx->stream;
     cudaLaunchAttribute attr[1];
