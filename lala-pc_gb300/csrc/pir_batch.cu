@@ -125,7 +125,8 @@ __device__ __forceinline__ void cta_rounds(const Bytecode &bc, S &st, long long 
   rounds = 0;
   for (;;) {
     int ch = 0, f = 0;
-    for (int c = threadIdx.x; c < bc.nchunks; c += blockDim.x) ch += sweep_chunk<S, GBC>(bc, c, st, f);
+    // one propagator per thread and step (63 registers: two CTAs of 512 per SM)
+    for (int c = threadIdx.x; c < bc.nchunks * 4; c += blockDim.x) ch += sweep_step<1, S, GBC>(bc, c, st, f);
     narrowed += ch;
     const int any_ch = __syncthreads_or(ch);
     const int any_f = __syncthreads_or(f);
@@ -138,7 +139,7 @@ __device__ __forceinline__ void cta_rounds(const Bytecode &bc, S &st, long long 
   }
 }
 
-__global__ void __launch_bounds__(512) k_instances(InstArgs a) {
+__global__ void __launch_bounds__(512, 2) k_instances(InstArgs a) {
   extern __shared__ int4 sm[];
   __shared__ int s_k;
   for (;;) {
