@@ -64,9 +64,7 @@ struct BatchState {
   long long ev_n = 0;
   void *d_ev = nullptr;  // per-CTA scratch block
   size_t cap_ev = 0;
-  long long ev_base_version = -1;  // store version the first ev_valid_slots working stores equal
   int node_variant = 0;            // event node kernel variant chosen by pir_autotune_nodes (0: default)
-  int ev_valid_slots = 0;
   int *d_watch = nullptr;  // watched variables | their bounds per node
   size_t cap_watch = 0;
   int *h_stage = nullptr;  // pinned host staging of the installed instance bytecode
@@ -504,14 +502,18 @@ __global__ void __launch_bounds__(512) k_nodes(NodeArgs a) {
 // (both checked exhaustively against the oracle), so they cannot change a
 // node's fixpoint -- lala-pc's FixpointSubset idea (pir.hpp:874-884).
 //
-// Each CTA keeps one working store, equal to the base between nodes (after a
-// node only the variables it touched are put back) and between launches while
-// the base store does not change, so it is copied only when it did.  Within a
-// round, the expansion of the changed variables' adjacency is spread over the
-// whole CTA (block scan of the degrees), and candidates, changed variables and
-// touched variables are deduplicated in shared-memory hash sets; a set whose
-// probe window is full falls back to epoch stamps in global memory for that
-// key (a key takes the same path for as long as its set is not cleared).
+// A node's store is an overlay on the base store: each CTA keeps a working
+// array that holds only the node's own narrowings (the whole integer range
+// where it narrowed nothing, reset there after every node), and a read meets
+// it with the base, which every CTA reads and nobody writes during the launch
+// (L2 / L1 resident).  A shared-memory bitmap marks the variables the node
+// narrowed, so reads of the others touch the base alone.  The base can change
+// between launches without anything being reloaded.  Within a round, the
+// expansion of the changed variables' adjacency is spread over the whole CTA
+// (block scan of the degrees), and candidates, changed variables and touched
+// variables are deduplicated in shared-memory hash sets; a set whose probe
+// window is full falls back to epoch stamps in global memory for that key (a
+// key takes the same path for as long as its set is not cleared).
 
 constexpr int CAND_LOG = 11, CHG_LOG = 10, TOUCH_LOG = 11, MAX_PROBE = 16;
 
@@ -521,8 +523,8 @@ struct EvArgs {
   int nvars;
   const int *adj_ptr, *adj;
   const unsigned char *ent;  // per propagator: entailed at the base store (skipped)
-  const int2 *base;
-  int copy_base;    // the working stores must be (re)loaded from the base
+  const int2 *base;  // read-only during the launch
+  int bitmap_words;  // words of the shared-memory bitmap of narrowed variables (0: none, every read meets both)
   int2 *out_store;  // node-major nnodes x nvars, or nullptr
   const int *watch;  // nwatch variables whose final bounds every node reports
   int nwatch;
@@ -530,7 +532,7 @@ struct EvArgs {
   const int *off, *var, *lb, *ub;
   int nnodes;
   int *next;
-  int2 *ws;          // grid x nvars
+  int2 *ws;          // grid x nvars: the node's narrowings, [INT_MIN, INT_MAX] elsewhere
   unsigned *vmark;   // grid x nvars: epoch a variable last entered a changed list (fallback)
   unsigned *tmark;   // grid x nvars: node tag a variable last entered the touched list (fallback)
   int *lists;        // grid x 3 x nvars: changed lists (2) and the touched list
@@ -563,27 +565,33 @@ __device__ __forceinline__ void set_clear(int *tab) {
 }
 
 struct NodeEvStore {
-  int2 *ws;
+  int2 *ws;              // the node's narrowings (overlay)
+  const int2 *base;      // the base store
+  unsigned *bits;        // shared-memory bitmap of the variables the node narrowed (null: none)
   unsigned *vmark, *tmark;
   int *dnext, *touched;
   int *nd, *nt;              // shared-memory counters
-  int *chg_set, *touch_set;  // shared-memory sets
+  int *chg_set, *touch_set;  // shared-memory sets (touch_set: only without the bitmap)
   unsigned epoch, tag;
+  // base meet overlay; the overlay is read only for variables the node narrowed
   __device__ __forceinline__ Itv load(int v) const {
+    const int2 b = __ldg(base + v);
+    if (bits && !(bits[v >> 5] & (1u << (v & 31)))) return mk(b.x, b.y);
     const int2 t = __ldcg(ws + v);
-    return mk(t.x, t.y);
+    return mk(max(b.x, t.x), min(b.y, t.y));
   }
   // v narrowed: first time this round -> next changed list; first time this
-  // node -> touched list
-  __device__ __forceinline__ void note(int v) const {
+  // node -> touched list (first: from the bitmap, -1 without it)
+  __device__ __forceinline__ void note(int v, int first) const {
     int c = set_insert<CHG_LOG>(chg_set, v);
     if (c < 0) c = atomicMax(vmark + v, epoch) < epoch ? 1 : 0;
-    if (c > 0) {
-      dnext[atomicAdd(nd, 1)] = v;
-      int t = set_insert<TOUCH_LOG>(touch_set, v);
+    if (c > 0) dnext[atomicAdd(nd, 1)] = v;
+    int t = first;
+    if (t < 0 && c > 0) {
+      t = set_insert<TOUCH_LOG>(touch_set, v);
       if (t < 0) t = atomicExch(tmark + v, tag) != tag ? 1 : 0;
-      if (t > 0) touched[atomicAdd(nt, 1)] = v;
     }
+    if (t > 0) touched[atomicAdd(nt, 1)] = v;
   }
   __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
     int n = 0;
@@ -596,7 +604,12 @@ struct NodeEvStore {
       ++n;
     }
     if (n) {
-      note(v);
+      int first = -1;
+      if (bits) {
+        const unsigned m = 1u << (v & 31);
+        first = (atomicOr(bits + (v >> 5), m) & m) ? 0 : 1;
+      }
+      note(v, first);
       if (is_bot(mk(max(seen.l, r.l), min(seen.u, r.u)))) failed = 1;
     }
     return n;
@@ -636,8 +649,13 @@ __device__ __forceinline__ int block_scan_incl(int x, int *s_warp) {
 template <int NB, int MINB>
 __global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
   __shared__ int s_node, s_ncand, s_nd[2], s_nt;
-  __shared__ int s_cand_set[1 << CAND_LOG], s_chg_set[1 << CHG_LOG], s_touch_set[1 << TOUCH_LOG];
+  __shared__ int s_cand_set[1 << CAND_LOG], s_chg_set[1 << CHG_LOG];
   __shared__ int s_beg[NB], s_end[NB], s_warp[32];
+  // dynamic: the bitmap of narrowed variables (bitmap_words words), or else
+  // the touched-variable set
+  extern __shared__ unsigned s_dyn[];
+  unsigned *bits = a.bitmap_words ? s_dyn : nullptr;
+  int *s_touch_set = a.bitmap_words ? nullptr : reinterpret_cast<int *>(s_dyn);
   const size_t nv = (size_t)a.nvars;
   const int tid = threadIdx.x;
   int2 *ws = a.ws + blockIdx.x * nv;
@@ -647,9 +665,8 @@ __global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
   unsigned *pstamp = a.pstamp + blockIdx.x * (size_t)a.n;
   int *cand = a.cand + blockIdx.x * (size_t)a.n;
   unsigned epoch = a.epochs[blockIdx.x];
-  if (a.copy_base)
-    for (size_t v = tid; v < nv; v += blockDim.x) ws[v] = a.base[v];
   unsigned long long execs = 0, narrowed = 0;
+  for (int i = tid; i < a.bitmap_words; i += blockDim.x) s_dyn[i] = 0u;  // then cleared word by word
   __syncthreads();
   for (;;) {
     if (tid == 0) {
@@ -658,26 +675,24 @@ __global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
       s_nt = 0;
     }
     set_clear<CHG_LOG>(s_chg_set);
-    set_clear<TOUCH_LOG>(s_touch_set);
+    if (!bits) set_clear<TOUCH_LOG>(s_touch_set);
     __syncthreads();
     const int node = s_node;
     if (node >= a.nnodes) break;
     ++epoch;
     const unsigned tag = epoch;
-    NodeEvStore st{ws, vmark, tmark, dl0, touched, &s_nd[0], &s_nt, s_chg_set, s_touch_set, epoch, tag};
+    NodeEvStore st{ws, a.base, bits, vmark, tmark, dl0, touched, &s_nd[0], &s_nt, s_chg_set, s_touch_set,
+                   epoch, tag};
     // tightenings: meets, the changed ones start the first changed list
     int f = 0;
     const int k0 = a.off[node], k1 = a.off[node + 1];
     for (int k = k0 + tid; k < k1; k += blockDim.x) {
       const int v = a.var[k];
-      const int ol = atomicMax(&ws[v].x, a.lb[k]), ou = atomicMin(&ws[v].y, a.ub[k]);
-      if (ol < a.lb[k] || ou > a.ub[k]) st.note(v);
+      int dummy = 0;
+      st.embed(v, st.load(v), mk(a.lb[k], a.ub[k]), dummy);
     }
     __syncthreads();
-    for (int k = k0 + tid; k < k1; k += blockDim.x) {
-      const int2 t = __ldcg(ws + a.var[k]);
-      f |= is_bot(mk(t.x, t.y));
-    }
+    for (int k = k0 + tid; k < k1; k += blockDim.x) f |= is_bot(st.load(a.var[k]));
     int failed = __syncthreads_or(f);
     int cur = 0;
     long long round = 0;
@@ -729,8 +744,8 @@ __global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
         }
         __syncthreads();
       }
-      NodeEvStore rs{ws, vmark, tmark, cur ? dl0 : dl1, touched, &s_nd[cur ^ 1], &s_nt, s_chg_set, s_touch_set,
-                     epoch, tag};
+      NodeEvStore rs{ws, a.base, bits, vmark, tmark, cur ? dl0 : dl1, touched, &s_nd[cur ^ 1], &s_nt, s_chg_set,
+                     s_touch_set, epoch, tag};
       const int nc = s_ncand;
       int f2 = 0;
       for (int i = tid; i < nc; i += blockDim.x) {
@@ -749,16 +764,23 @@ __global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
     }
     if (a.out_store) {
       int2 *dst = a.out_store + (size_t)node * nv;
-      for (size_t v = tid; v < nv; v += blockDim.x) dst[v] = __ldcg(ws + v);
+      for (size_t v = tid; v < nv; v += blockDim.x) {
+        const Itv t = st.load((int)v);
+        dst[v] = make_int2(t.l, t.u);
+      }
     }
-    for (int k = tid; k < a.nwatch; k += blockDim.x)
-      a.out_watch[(size_t)node * a.nwatch + k] = __ldcg(ws + a.watch[k]);
+    for (int k = tid; k < a.nwatch; k += blockDim.x) {
+      const Itv t = st.load(a.watch[k]);
+      a.out_watch[(size_t)node * a.nwatch + k] = make_int2(t.l, t.u);
+    }
     __syncthreads();
-    // put the touched variables back to the base store
+    // the overlay back to the whole range where this node narrowed
+    // (every bit set during the node belongs to a touched variable)
     const int nt = s_nt;
     for (int i = tid; i < nt; i += blockDim.x) {
       const int v = touched[i];
-      ws[v] = a.base[v];
+      ws[v] = make_int2(INT_MIN, INT_MAX);
+      if (bits) bits[v >> 5] = 0u;
     }
     __syncthreads();
   }
@@ -790,6 +812,11 @@ __global__ void k_nodes_unpack(const int2 *nstore, int nvars, int nnodes, int *o
     out_lb[i] = t.x;
     out_ub[i] = t.y;
   }
+}
+
+__global__ void k_fill_top(int2 *a, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] = make_int2(INT_MIN, INT_MAX);
 }
 
 __global__ void k_pack_int2(const int *lb, const int *ub, long long n, int2 *out) {
@@ -882,8 +909,12 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
                    : (b->node_variant > 0 ? b->node_variant : 6);
   const int block = kNodeVariants[nvar - 1].block;
   const void *kfn = kNodeVariants[nvar - 1].fn;
+  // the bitmap of narrowed variables, in shared memory while it takes at most 32 KB
+  const int words = (ctx->nvars + 31) / 32;
+  const int bitmap_words = words * 4 <= 32 * 1024 ? words : 0;
+  const size_t dyn_smem = bitmap_words ? (size_t)bitmap_words * 4 : ((size_t)1 << TOUCH_LOG) * sizeof(int);
   int occ = 0;
-  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, block, 0));
+  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, block, dyn_smem));
   occ = std::max(occ, 1);
   const int grid = std::max(1, std::min(nnodes, ctx->num_sms * (opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ)));
   const size_t nv = (size_t)ctx->nvars, n = (size_t)std::max<long long>(ctx->n, 1);
@@ -896,8 +927,6 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
     b->d_ev = nullptr;
     b->cap_ev = 0;
     b->ev_slots = 0;
-    b->ev_valid_slots = 0;
-    b->ev_base_version = -1;
     if (cudaMalloc(&b->d_ev, need) != cudaSuccess) {
       cudaGetLastError();
       return set_err(ctx, PIR_ENOMEM, "event scratch (%zu bytes)", need);
@@ -907,6 +936,10 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
     b->ev_nvars = ctx->nvars;
     b->ev_n = ctx->n;
     PIR_CK(cudaMemsetAsync(b->d_ev, 0, need, ctx->stream));  // stamps and epochs start at 0
+    // the overlays start at the whole integer range (the first slots * nvars int2)
+    const long long cells = (long long)slots * ctx->nvars;
+    k_fill_top<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(reinterpret_cast<int2 *>(b->d_ev), cells);
+    PIR_CK(cudaGetLastError());
   }
   const size_t slots = (size_t)b->ev_slots;
   char *base = (char *)b->d_ev;
@@ -917,8 +950,7 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
   a.adj_ptr = b->d_adj_ptr;
   a.adj = b->d_adj;
   a.base = ctx->d_store;
-  // the working stores equal the base unless the store changed since they were loaded
-  a.copy_base = (b->ev_base_version != ctx->store_version || b->ev_valid_slots < grid) ? 1 : 0;
+  a.bitmap_words = bitmap_words;
   a.ws = (int2 *)base;
   base += slots * nv * 8;
   a.vmark = (unsigned *)base;
@@ -988,7 +1020,7 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
   }
   {
     void *kargs[] = {&a};
-    PIR_CK(cudaLaunchKernel(kfn, dim3(grid), dim3(block), kargs, 0, ctx->stream));
+    PIR_CK(cudaLaunchKernel(kfn, dim3(grid), dim3(block), kargs, dyn_smem, ctx->stream));
   }
   PIR_CK(cudaGetLastError());
   PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -1018,12 +1050,6 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
     }
   }
   PIR_CK(cudaStreamSynchronize(ctx->stream));
-  // every node put its touched variables back: the first `grid` working stores
-  // (all of them when this launch loaded them) equal the base store
-  if (a.copy_base) {
-    b->ev_base_version = ctx->store_version;
-    b->ev_valid_slots = grid;
-  }
   b->ent_store_version = ctx->store_version;
   b->ent_bc_version = ctx->bytecode_version;
   pir_stats st;
