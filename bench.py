@@ -574,6 +574,7 @@ def run_learned(args):
         "learned": {"executions": e1, "device_ms": d1},
         "wall_ratio_ac1_over_learned": d0 / max(d1, 1e-9),
         "bit_exact_nodes": same, "nodes": ntest,
+        "gpu_launches": ntest,  # one learned fixpoint launch per held-out node (the timed device time)
     }
     print(json.dumps(out), flush=True)
 
@@ -668,7 +669,8 @@ def run_uneven(args):
         "e2e": {"value": n_all * args.steps / wall_max, "unit": "instances/s",
                 "h2d_bytes_per_step": int(prop_off[-1] * 16 + var_off[-1] * 8),
                 "d2h_bytes_per_step": int(var_off[-1] * 8)},
-        "gpu_launches": args.steps, "clocks": clocks,
+        # per step: store pack, the cluster kernel, the one-CTA-per-instance kernel, store unpack
+        "gpu_launches": 4 * args.steps, "clocks": clocks,
     }
     print(json.dumps(out), flush=True)
 
