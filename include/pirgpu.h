@@ -317,6 +317,85 @@ int pir_sched_score(pirgpu_ctx *ctx, int32_t count, const float *X, float *out_s
 /* Number of SMs and the library's build string (for reports). */
 int pir_device_info(pirgpu_ctx *ctx, int32_t *num_sms, char *name, size_t name_len);
 
+/* ------------------------------------------------------------------ PC ----
+ * Tree propagators: lala-pc's PC abstract domain (include/lala/pc.hpp:39-789)
+ * with its terms (terms.hpp) and formulas (formula.hpp), over the same store
+ * as the PIR propagators of this context.  A propagator is a formula tree;
+ * trees are given as a tape of nodes {kind, a, b, c} (four int32 arrays),
+ * children before parents: every index a node refers to is smaller than the
+ * node's own index.  A propagator is the index of its root formula node.  The
+ * pc_* calls run the PC propagators only; pir_fixpoint runs the PIR ones. */
+enum pc_kind {
+  /* terms: Term's alternatives in order (terms.hpp:572-589) */
+  PC_VAR = 0,      /* a = variable                           Variable :48-85 */
+  PC_CONST = 1,    /* the interval [a, b]                     Constant :19-45 */
+  PC_FORMULA = 2,  /* a = formula node, its truth value 0/1   Formula::project, formula.hpp:1097 */
+  PC_NEG = 3,      /* -t, a = t                               Unary<NegOp> :88-102, :122-175 */
+  PC_ABS = 4,      /* |t|, a = t                              Unary<AbsOp> :105-119 */
+  PC_ADD = 5,      /* a + b (a, b = terms)                    Binary<GroupAdd> :178-207, :334-435 */
+  PC_SUB = 6,      /* a - b                                   GroupSub :210-229 */
+  PC_MUL = 7,      /* a * b                                   GroupMul<EDIV> :232-262 */
+  PC_TDIV = 8,     /* a tdiv b                                GroupDiv :265-299 */
+  PC_FDIV = 9, PC_CDIV = 10, PC_EDIV = 11,
+  PC_MIN = 12,     /* min(a, b)                               GroupMinMax :302-331 */
+  PC_MAX = 13,
+  PC_NADD = 14,    /* sum of b operands: the PC_ARG nodes a .. a+b-1   Nary :438-526 */
+  PC_NMUL = 15,    /* product of b operands */
+  /* formulas: Formula's alternatives in order (formula.hpp:905-920) */
+  PC_PVAR = 16,    /* variable a is true (not 0)              VariableLiteral :81-167 */
+  PC_NVAR = 17,    /* variable a is false (0) */
+  PC_TRUE = 18, PC_FALSE = 19,  /* False :170-204, True :207-239 */
+  PC_LEQ = 20,     /* term a <= term b                        Inequality :728-845 */
+  PC_GT = 21,      /* term a > term b */
+  PC_EQ = 22,      /* term a == term b                        Equality :590-721 */
+  PC_NEQ = 23,     /* term a != term b */
+  PC_AND = 24,     /* formula a and formula b                 Conjunction :242-308 */
+  PC_OR = 25,      /*                                         Disjunction :311-378 */
+  PC_EQUIV = 26,   /*                                         Biconditional :381-451 */
+  PC_IMPLY = 27,   /*                                         Implication :454-516 */
+  PC_XOR = 28,     /*                                         ExclusiveDisjunction :519-587 */
+  PC_ARG = 29,     /* operand slot of PC_NADD / PC_NMUL: a = term */
+  PC_NUM_KINDS = 30
+};
+/* Deepest formula tree accepted (nodes on a root-to-leaf path): bounds the
+ * device call stack of the recursive evaluator. */
+#define PC_MAX_DEPTH 64
+
+/* PC::deduce(tell) (pc.hpp:625-648): appends nnodes tape nodes (indices in
+ * this call's arrays are local to it) and nprops propagators, then stably
+ * sorts all propagators by (formula kind, tree length) as the reference does.
+ * c[] is reserved and must be 0.  Checks every node (kinds, child order and
+ * kinds, variable range, depth <= PC_MAX_DEPTH) first: PIR_EINVAL changes
+ * nothing. */
+int pc_tell(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *kind, const int32_t *a, const int32_t *b,
+            const int32_t *c, int32_t nprops, const int32_t *roots);
+/* num_deductions() (pc.hpp:665-667; the sub-store adds none). */
+int64_t pc_num_deductions(const pirgpu_ctx *ctx);
+/* The propagators' root nodes in engine order (pc_num_deductions entries,
+ * indices into the context's whole tape) and the tape itself (pc_tape_size
+ * nodes). */
+int pc_get_roots(pirgpu_ctx *ctx, int32_t *roots);
+int64_t pc_tape_size(const pirgpu_ctx *ctx);
+int pc_get_tape(pirgpu_ctx *ctx, int32_t *kind, int32_t *a, int32_t *b, int32_t *c);
+/* Fixpoint of all PC propagators in Jacobi rounds, one cooperative launch:
+ * every deduction of a round reads the store the round started from, the
+ * round's joins are met in at its end, a round with no join or with an empty
+ * variable ends the loop.  The result is a deterministic function of the input
+ * (PC propagators need not be monotone, formula.hpp:497-503, and then even the
+ * reference's Gauss-Seidel result depends on the propagator order; for
+ * monotone ones every order reaches this fixpoint).  opts: max_rounds,
+ * barrier_timeout_ns, ctas_per_sm; the other fields are ignored.
+ * stats->executions counts propagator executions. */
+int pc_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts, pir_stats *stats);
+/* deduce(int i) (pc.hpp:671-681): one propagator, engine order.  *changed is
+ * the formula's has_changed as the reference computes it. */
+int pc_deduce_one(pirgpu_ctx *ctx, int64_t i, int *changed);
+/* ask(int i) (pc.hpp:661-663) of one / of every propagator (entailed[i] 0/1). */
+int pc_ask(pirgpu_ctx *ctx, int64_t i, int *entailed);
+int pc_ask_all(pirgpu_ctx *ctx, uint8_t *entailed);
+/* is_extractable() (pc.hpp:727-737): not bot and every PC propagator entailed. */
+int pc_is_extractable(pirgpu_ctx *ctx, int *extractable);
+
 #ifdef __cplusplus
 }
 #endif

@@ -382,6 +382,7 @@ void pir_ctx_destroy(pirgpu_ctx *ctx) {
     if (p) cudaFree(p);
   destroy_batch_state(ctx);
   destroy_sched_state(ctx);
+  destroy_pc_state(ctx);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -394,7 +395,8 @@ int pir_load_store(pirgpu_ctx *ctx, int32_t nvars, const int32_t *lb, const int3
   if (ctx) ++ctx->store_version;
   if (!ctx) return PIR_EINVAL;
   if (nvars < 0 || (nvars > 0 && (!lb || !ub))) return set_err(ctx, PIR_EINVAL, "bad store arguments");
-  if (nvars < ctx->max_var_used + 1) return set_err(ctx, PIR_EINVAL, "store smaller than the variables used by the bytecode");
+  if (nvars < std::max(ctx->max_var_used, pc_max_var_used(ctx)) + 1)
+    return set_err(ctx, PIR_EINVAL, "store smaller than the variables used by the propagators");
   CK(cudaSetDevice(ctx->device));
   int r;
   if ((r = ensure(ctx, (void **)&ctx->d_store, &ctx->cap_store, (size_t)nvars * sizeof(int2)))) return r;
@@ -810,6 +812,7 @@ int pir_is_extractable(pirgpu_ctx *ctx, int *extractable) {
 struct pirgpu_snapshot {
   int device;
   long long n;
+  long long pc_n;  // PC propagators (PC::snapshot_type::num_props, pc.hpp:47-51)
   int nvars;
   bool failed;
   bool at_fixpoint;
@@ -822,6 +825,7 @@ int pir_snapshot(pirgpu_ctx *ctx, pirgpu_snapshot **out) {
   pirgpu_snapshot *s = new pirgpu_snapshot();
   s->device = ctx->device;
   s->n = ctx->n;
+  s->pc_n = pc_count(ctx);
   s->nvars = ctx->nvars;
   s->failed = ctx->failed;
   s->at_fixpoint = ctx->at_fixpoint;
@@ -844,7 +848,8 @@ int pir_restore(pirgpu_ctx *ctx, const pirgpu_snapshot *snap) {
   if (ctx) ++ctx->store_version;
   if (!ctx || !snap) return PIR_EINVAL;
   if (snap->nvars != ctx->nvars) return set_err(ctx, PIR_EINVAL, "snapshot has %d vars, store has %d", snap->nvars, ctx->nvars);
-  if (snap->n > ctx->n) return set_err(ctx, PIR_EINVAL, "snapshot has more propagators than the context");
+  if (snap->n > ctx->n || snap->pc_n > pc_count(ctx))
+    return set_err(ctx, PIR_EINVAL, "snapshot has more propagators than the context");
   CK(cudaSetDevice(ctx->device));
   if (ctx->nvars > 0)
     CK(cudaMemcpyAsync(ctx->d_store, snap->d_store, (size_t)ctx->nvars * sizeof(int2), cudaMemcpyDeviceToDevice,
@@ -858,6 +863,10 @@ int pir_restore(pirgpu_ctx *ctx, const pirgpu_snapshot *snap) {
     ctx->h_z.resize((size_t)ctx->n);
     ctx->bytecode_version++;
     int r = upload_bytecode(ctx);
+    if (r) return r;
+  }
+  if (snap->pc_n != pc_count(ctx)) {
+    int r = pc_truncate(ctx, snap->pc_n);
     if (r) return r;
   }
   CK(cudaStreamSynchronize(ctx->stream));

@@ -10,6 +10,7 @@
 namespace pirgpu {
 struct BatchState;
 struct SchedState;
+struct PcState;
 }  // namespace pirgpu
 
 // One PIR (bytecode + store) on one device.
@@ -51,6 +52,7 @@ struct pirgpu_ctx {
 
   pirgpu::BatchState *batch = nullptr;
   pirgpu::SchedState *sched = nullptr;
+  pirgpu::PcState *pc = nullptr;  // PC tree propagators (pir_pc.cu)
 };
 
 namespace pirgpu {
@@ -64,6 +66,12 @@ Bytecode bytecode_view(const pirgpu_ctx *ctx);
 
 void destroy_batch_state(pirgpu_ctx *ctx);
 void destroy_sched_state(pirgpu_ctx *ctx);
+void destroy_pc_state(pirgpu_ctx *ctx);
+// PC propagators: largest variable they use, how many there are, and
+// restore()'s pop from the end of their engine order
+int pc_max_var_used(const pirgpu_ctx *ctx);
+long long pc_count(const pirgpu_ctx *ctx);
+int pc_truncate(pirgpu_ctx *ctx, long long n);
 int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);
 int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);
 // Records variables embedded since the last learned fixpoint (its "just

@@ -127,6 +127,16 @@ SIGNATURES = [
     ("pir_sched_params", ctypes.c_int, [_P, _F32P, ctypes.c_int32, ctypes.c_int32]),
     ("pir_fixpoint_static", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, _P, ctypes.c_int32,
                                            ctypes.POINTER(Opts), ctypes.POINTER(Stats), _P]),
+    ("pc_tell", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P, _I32P, ctypes.c_int32, _I32P]),
+    ("pc_num_deductions", ctypes.c_int64, [_P]),
+    ("pc_get_roots", ctypes.c_int, [_P, _I32P]),
+    ("pc_tape_size", ctypes.c_int64, [_P]),
+    ("pc_get_tape", ctypes.c_int, [_P, _I32P, _I32P, _I32P, _I32P]),
+    ("pc_fixpoint", ctypes.c_int, [_P, ctypes.POINTER(Opts), ctypes.POINTER(Stats)]),
+    ("pc_deduce_one", ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
+    ("pc_ask", ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
+    ("pc_ask_all", ctypes.c_int, [_P, _U8P]),
+    ("pc_is_extractable", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
 ]
 
 
@@ -304,6 +314,55 @@ class Context:
 
     def restore(self, snap):
         self._check(self._L.pir_restore(self.h, snap.h))
+
+    # -- PC tree propagators (pc.hpp) ----------------------------------
+    def pc_tell(self, tape, roots):
+        """PC::deduce(tell): appends the formulas of `tape` ((n, 4) int32:
+        kind, a, b, c per node; see pc.py) with propagators at `roots`."""
+        t = np.ascontiguousarray(np.asarray(tape, np.int32).reshape(-1, 4).T)
+        roots = _c32(roots)
+        self._check(self._L.pc_tell(self.h, t.shape[1], *(_p32(t[k]) for k in range(4)), len(roots),
+                                    _p32(roots)))
+
+    def pc_num_deductions(self):
+        return self._L.pc_num_deductions(self.h)
+
+    def pc_roots(self):
+        """Root node of every PC propagator, in engine order."""
+        out = np.empty(self.pc_num_deductions(), np.int32)
+        self._check(self._L.pc_get_roots(self.h, _p32(out)))
+        return out
+
+    def pc_tape(self):
+        n = self._L.pc_tape_size(self.h)
+        cols = [np.empty(n, np.int32) for _ in range(4)]
+        self._check(self._L.pc_get_tape(self.h, *map(_p32, cols)))
+        return np.stack(cols, axis=1)
+
+    def pc_fixpoint(self, **kw):
+        o = make_opts(**kw)
+        s = Stats()
+        rc = self._L.pc_fixpoint(self.h, ctypes.byref(o), ctypes.byref(s))
+        self._check(rc, (OK, FAILED, TIMEOUT, BARRIER_TIMEOUT))
+        return rc, s.asdict()
+
+    def pc_deduce_one(self, i):
+        ch = ctypes.c_int(0)
+        self._check(self._L.pc_deduce_one(self.h, i, ctypes.byref(ch)))
+        return bool(ch.value)
+
+    def pc_ask(self, i):
+        e = ctypes.c_int(0)
+        self._check(self._L.pc_ask(self.h, i, ctypes.byref(e)))
+        return bool(e.value)
+
+    def pc_ask_all(self):
+        out = np.zeros(self.pc_num_deductions(), np.uint8)
+        self._check(self._L.pc_ask_all(self.h, out.ctypes.data_as(_U8P)))
+        return out.astype(bool)
+
+    def pc_is_extractable(self):
+        return self._flag(self._L.pc_is_extractable)
 
     # -- batched -------------------------------------------------------
     def deduce_batch(self, op, in_lb, in_ub):

@@ -1,7 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles oracle/pir_oracle.cpp into oracle/_build/liboracle.so with the host
-C++ compiler.  Portable flags only (the same source builds on x86_64 and
+Compiles oracle/pir_oracle.cpp and oracle/pc_oracle.cpp into
+oracle/_build/liboracle.so with the host C++ compiler.  Portable flags only (the same source builds on x86_64 and
 aarch64 hosts).  The reference itself (lala-pc) cannot be compiled here: it
 includes lala-core and cuda-battery headers that its CMake fetches over the
 network, so the oracle is this restatement, not a build of the reference.
@@ -13,14 +13,14 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
-SOURCES = [os.path.join(HERE, "pir_oracle.cpp")]
+SOURCES = [os.path.join(HERE, "pir_oracle.cpp"), os.path.join(HERE, "pc_oracle.cpp")]
 
 
 def _stale():
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = SOURCES + [os.path.join(HERE, "pir_oracle.h")]
+    deps = SOURCES + [os.path.join(HERE, "pir_oracle.h"), os.path.join(HERE, "pc_oracle.h")]
     return any(os.path.getmtime(s) > t for s in deps)
 
 

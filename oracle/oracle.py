@@ -62,6 +62,25 @@ def lib():
         L.orc_div.restype = i64
         L.orc_mod.argtypes = [i32, i64, i64]
         L.orc_mod.restype = i64
+        T4 = [_I32P, _I32P, _I32P, _I32P]
+        L.orc_pc_validate.argtypes = [i32] + T4 + [i32, _I32P, i32]
+        L.orc_pc_validate.restype = i32
+        L.orc_pc_order.argtypes = [i32] + T4 + [i32, _I32P, _I32P]
+        L.orc_pc_order.restype = None
+        L.orc_pc_deduce.argtypes = T4 + [i32, _I32P, _I32P, _I64P]
+        L.orc_pc_deduce.restype = i32
+        L.orc_pc_ask.argtypes = T4 + [i32, _I32P, i32]
+        L.orc_pc_ask.restype = i32
+        L.orc_pc_project.argtypes = T4 + [i32, _I32P, _I32P, _I32P]
+        L.orc_pc_project.restype = None
+        L.orc_pc_embed.argtypes = T4 + [i32, i32, i32, _I32P, _I32P]
+        L.orc_pc_embed.restype = i32
+        L.orc_pc_fixpoint.argtypes = [i32] + T4 + [i32, _I32P, i32, _I32P, i64, _I64P]
+        L.orc_pc_fixpoint.restype = i32
+        L.orc_pc_fixpoint_jacobi.argtypes = [i32] + T4 + [i32, _I32P, i32, _I32P, i64, _I64P]
+        L.orc_pc_fixpoint_jacobi.restype = i32
+        L.orc_pc_itv.argtypes = [i32, i32, i32, i32, i32, _I32P, _I32P]
+        L.orc_pc_itv.restype = None
         _lib = L
     return _lib
 
@@ -246,3 +265,88 @@ def div(op, a, b):
 
 def mod(kind, a, b):
     return int(lib().orc_mod(kind, a, b))
+
+
+# --------------------------------------------------------------------- PC --
+# Tapes are int32 arrays of shape (nnodes, 4): kind, a, b, c per node (the
+# node kinds of oracle/pc_oracle.h); a propagator is its root node's index.
+
+def _tape_cols(tape):
+    t = np.ascontiguousarray(np.asarray(tape, np.int32).reshape(-1, 4).T)
+    return t, [_p32(t[k]) for k in range(4)]
+
+
+def pc_validate(tape, roots, nvars):
+    """Depth of the deepest root (>= 1), or a negative error code."""
+    t, cols = _tape_cols(tape)
+    roots = _c32(roots)
+    return int(lib().orc_pc_validate(t.shape[1], *cols, len(roots), _p32(roots), nvars))
+
+
+def pc_order(tape, roots):
+    """PC::deduce(tell)'s order: roots stably sorted by (kind, length)."""
+    t, cols = _tape_cols(tape)
+    roots = _c32(roots)
+    out = np.empty(len(roots), np.int32)
+    lib().orc_pc_order(t.shape[1], *cols, len(roots), _p32(roots), _p32(out))
+    return out
+
+
+def pc_fixpoint(tape, roots, store, max_sweeps=1 << 40):
+    """Gauss-Seidel fixpoint of the PC propagators in roots[] order; `store`
+    (nvars, 2) int32 is updated in place.  Returns (status, stats dict)."""
+    t, cols = _tape_cols(tape)
+    roots = _c32(roots)
+    assert store.dtype == np.int32 and store.flags.c_contiguous
+    out = np.zeros(4, np.int64)
+    st = lib().orc_pc_fixpoint(t.shape[1], *cols, len(roots), _p32(roots), store.shape[0], _p32(store),
+                               max_sweeps, _p64(out))
+    return st, dict(sweeps=int(out[0]), execs=int(out[1]), narrowed=int(out[2]), has_changed=bool(out[3]))
+
+
+def pc_fixpoint_jacobi(tape, roots, store, max_rounds=1 << 40):
+    """The GPU engine's schedule on the CPU: Jacobi rounds (every deduction of
+    a round reads the round's initial store).  Returns (status, stats)."""
+    t, cols = _tape_cols(tape)
+    roots = _c32(roots)
+    assert store.dtype == np.int32 and store.flags.c_contiguous
+    out = np.zeros(4, np.int64)
+    st = lib().orc_pc_fixpoint_jacobi(t.shape[1], *cols, len(roots), _p32(roots), store.shape[0], _p32(store),
+                                      max_rounds, _p64(out))
+    return st, dict(rounds=int(out[0]), execs=int(out[1]), narrowed=int(out[2]))
+
+
+def pc_deduce(tape, root, store, failed=False):
+    """One deduce of the formula at `root`: (has_changed, failed)."""
+    t, cols = _tape_cols(tape)
+    f = np.array([int(failed)], np.int32)
+    nar = np.zeros(1, np.int64)
+    ch = lib().orc_pc_deduce(*cols, int(root), _p32(store), _p32(f), _p64(nar))
+    return bool(ch), bool(f[0])
+
+
+def pc_ask(tape, root, store, failed=False):
+    t, cols = _tape_cols(tape)
+    return bool(lib().orc_pc_ask(*cols, int(root), _p32(_c32(store)), int(failed)))
+
+
+def pc_project(tape, node, store):
+    t, cols = _tape_cols(tape)
+    lo = np.zeros(1, np.int32)
+    hi = np.zeros(1, np.int32)
+    lib().orc_pc_project(*cols, int(node), _p32(_c32(store)), _p32(lo), _p32(hi))
+    return int(lo[0]), int(hi[0])
+
+
+def pc_embed(tape, node, lb, ub, store):
+    t, cols = _tape_cols(tape)
+    f = np.zeros(1, np.int32)
+    ch = lib().orc_pc_embed(*cols, int(node), int(lb), int(ub), _p32(store), _p32(f))
+    return bool(ch), bool(f[0])
+
+
+def pc_itv(op, a, b=(0, 0)):
+    lo = np.zeros(1, np.int32)
+    hi = np.zeros(1, np.int32)
+    lib().orc_pc_itv(op, a[0], a[1], b[0], b[1], _p32(lo), _p32(hi))
+    return int(lo[0]), int(hi[0])
