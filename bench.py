@@ -737,10 +737,163 @@ def run_search(args):
     print(json.dumps(out), flush=True)
 
 
+# ---------------------------------------------------------------- PC trees --
+def _pc_workload(args):
+    import workloads as W
+    tape, roots, lb, ub, _ = W.pc_mix(args.pc_vars, args.pc_props, seed=0)
+    kinds = tape[:, 0]
+    leaves = int(np.isin(kinds, [0, 16, 17]).sum())  # VAR, PVAR, NVAR nodes
+    desc = ("PC trees: %d vars / %d formula propagators (40%% 4-term linear <=, 30%% reified "
+            "differences, 20%% disjunctive temporal, 10%% max equalities; planted solution, bounds "
+            "scale 1e3), %d tape nodes" % (args.pc_vars, args.pc_props, len(tape)))
+    return tape, roots, lb, ub, leaves, desc
+
+
+def run_pc(args):
+    """Fixpoint of the PC tree propagators (pc_fixpoint): executions/s."""
+    import pirgpu
+    ws, rank, local = dist_env()
+    dist = dist_init(ws)
+    cr = Cudart()
+    cr.set_device(local)
+    tape, roots, lb, ub, leaves, desc = _pc_workload(args)
+    nvars, nprops, nnodes = len(lb), len(roots), len(tape)
+    ctx = pirgpu.Context(local)
+    ctx.load_store(lb, ub)
+    ctx.pc_tell(tape, roots)
+    snap = ctx.snapshot()
+
+    def step():
+        ctx.restore(snap)
+        rc, st = ctx.pc_fixpoint(max_rounds=args.max_rounds)
+        if rc not in ((pirgpu.OK, pirgpu.TIMEOUT) if args.max_rounds else (pirgpu.OK,)):
+            raise RuntimeError("pc fixpoint status %s" % pirgpu.STATUS[rc])
+        return st
+
+    for _ in range(args.warmup):
+        step()
+        cr.flush_l2()
+    if dist:
+        dist.barrier()
+    cr.sync()
+    clk = ClockSampler(local)
+    clk.start()
+    stats = []
+    for _ in range(args.steps):
+        stats.append(step())
+        cr.flush_l2()
+    cr.sync()
+    clocks = clk.stop()
+    dev_ms = sum(s["device_ms"] for s in stats)
+    execs = sum(s["executions"] for s in stats)
+    joins = sum(s["narrowed"] for s in stats)
+    rounds = stats[0]["rounds"]
+    t_max = dist_max(dist, dev_ms / 1e3)
+    value = dist_sum(dist, execs) / t_max
+
+    lb_h, ub_h, lb_o, ub_o = (cr.pinned(nvars) for _ in range(4))
+    lb_h[:] = lb
+    ub_h[:] = ub
+    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 3))
+    e2e_execs = 0
+    cr.sync()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.load_store(lb_h, ub_h)
+        rc, st = ctx.pc_fixpoint()
+        ctx._check(ctx._L.pir_read_store(ctx.h, lb_o.ctypes.data_as(pirgpu._I32P),
+                                         ub_o.ctypes.data_as(pirgpu._I32P)))
+        e2e_execs += st["executions"]
+    cr.sync()
+    e2e_t = dist_max(dist, time.perf_counter() - t0)
+    e2e_value = dist_sum(dist, e2e_execs) / e2e_t if e2e_steps else None
+    if rank != 0:
+        return
+    # bytes a round must move: every tree node once (16 B), every variable leaf
+    # once (8 B), the round's store copy (B -> A, 16 B per variable); per
+    # fixpoint the initial copy (16 B per variable); 4 B per narrowing join
+    per_round = nnodes * 16 + leaves * 8 + nvars * 16
+    alg_bytes = args.steps * (rounds * per_round + nvars * 16) + joins * 4
+    hbm, hbm_src = peaks()
+    achieved = alg_bytes / (dev_ms / 1e3) / 1e9
+    cpu = None
+    if ws == 1 and not args.no_cpu:
+        from oracle import oracle as O
+        s = np.ascontiguousarray(np.stack([lb, ub], 1))
+        order = O.pc_order(tape, roots)
+        t0 = time.perf_counter()
+        rc, info = O.pc_fixpoint(tape, order, s)
+        dt = time.perf_counter() - t0
+        cpu = {"value": info["execs"] / dt, "unit": "executions/s", "cores": 1, "kind": "port",
+               "sample": "the whole Gauss-Seidel fixpoint of the same instance (%d sweeps, %d executions), "
+                         "%.1f s, 1 host thread" % (info["sweeps"], info["execs"], dt)}
+    out = {
+        "metric": "propagator executions/sec", "value": value, "unit": "executions/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic: seeded generator, planted-solution instance",
+        "config": {"workload": "pc: " + desc, "nvars": nvars, "propagators": nprops, "tape_nodes": nnodes,
+                   "parallelism": "replicas" if ws > 1 else "single",
+                   "schedule": "Jacobi rounds, one cooperative launch",
+                   "l2": "flushed between steps (256 MiB cudaMemset); step timed with CUDA events",
+                   "rounds_per_step": rounds, "fixpoint": "bit-exact vs the CPU oracle in tests"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": ncu_traffic("pc_fixpoint_pc"),
+                     "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "bytes_model": "per round 16 B per tape node + 8 B per variable leaf + 16 B per variable "
+                                    "(store copy); 16 B per variable per fixpoint; 4 B per narrowing join"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "executions/s", "h2d_bytes_per_step": int(nvars * 8),
+                "d2h_bytes_per_step": int(nvars * 8), "steps": e2e_steps},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "time_to_fixpoint_ms": dev_ms / args.steps,
+        "tree_nodes_per_s": args.steps * rounds * nnodes / (dev_ms / 1e3),
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_reference_pc(args):
+    """The reference's PC loop on the host: the Gauss-Seidel fixpoint of the
+    oracle (a restatement of pc.hpp / formula.hpp / terms.hpp), 1 thread."""
+    from oracle import oracle as O
+    tape, roots, lb, ub, _, desc = _pc_workload(args)
+    order = O.pc_order(tape, roots)
+    s0 = np.ascontiguousarray(np.stack([lb, ub], 1))
+    for _ in range(args.warmup):
+        O.pc_fixpoint(tape, order, s0.copy(), max_sweeps=1)
+    times, execs = [], 0
+    for _ in range(args.steps):
+        s = s0.copy()
+        t0 = time.perf_counter()
+        rc, info = O.pc_fixpoint(tape, order, s, max_sweeps=args.ref_sweeps)
+        times.append(time.perf_counter() - t0)
+        execs += info["execs"]
+    tot = sum(times)
+    v = execs / tot
+    out = {
+        "metric": "propagator executions/sec", "value": v, "unit": "executions/s",
+        "n_gpus": dist_env()[0], "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tot * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic: seeded generator, planted-solution instance",
+        "config": {"workload": "pc: " + desc, "nvars": len(lb), "propagators": len(roots)},
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": "executions/s", "cores": 1, "kind": "port",
+                         "sample": "each step = the first %d Gauss-Seidel sweeps of the fixpoint from the "
+                                   "initial store (the reference loop is sequential: 1 host thread)"
+                                   % args.ref_sweeps},
+        "e2e": {"value": v, "unit": "executions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
+    if args.workload == "pc":
+        return run_reference_pc(args)
     inst, desc = make_workload(args.workload)
     from oracle import oracle as O
     s0 = inst.store()
@@ -798,6 +951,8 @@ def main():
     ap.add_argument("--wake-fraction", type=float, default=1 / 32)
     ap.add_argument("--queens", type=int, default=12, help="search workload: board size")
     ap.add_argument("--cpu-search-nodes", type=int, default=2_000_000, help="search workload: CPU node cap")
+    ap.add_argument("--pc-vars", type=int, default=1_000_000, help="pc workload: variables")
+    ap.add_argument("--pc-props", type=int, default=1_000_000, help="pc workload: formula propagators")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")
@@ -811,6 +966,8 @@ def main():
         run_learned(args)
     elif args.workload == "search":
         run_search(args)
+    elif args.workload == "pc":
+        run_pc(args)
     else:
         run_ours(args)
 

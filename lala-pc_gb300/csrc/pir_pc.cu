@@ -223,12 +223,52 @@ __device__ __forceinline__ bool store_embed(PcEval *e, int v, Itv u) {
   return ch;
 }
 
-__device__ Itv t_project(PcEval *e, int n);
-__device__ bool t_embed(PcEval *e, int n, Itv u);
-__device__ bool f_ask(PcEval *e, int n);
-__device__ bool f_nask(PcEval *e, int n);
-__device__ bool f_deduce(PcEval *e, int n);
-__device__ bool f_contra(PcEval *e, int n);
+// The recursive functions take the node already loaded; the inline wrappers
+// below answer leaves (variables, constants, literals) in the caller, so a
+// call, and its stack frame, is spent on inner nodes only.
+__device__ Itv t_project_rec(PcEval *e, int n, int4 d);
+__device__ bool t_embed_rec(PcEval *e, int n, int4 d, Itv u);
+__device__ bool f_ask_rec(PcEval *e, int4 d);
+__device__ bool f_nask_rec(PcEval *e, int4 d);
+__device__ bool f_deduce_rec(PcEval *e, int4 d);
+__device__ bool f_contra_rec(PcEval *e, int4 d);
+
+__device__ __forceinline__ Itv t_project(PcEval *e, int n) {
+  const int4 d = node(e, n);
+  if (d.x == K_VAR) return load(e, d.y);
+  if (d.x == K_CONST) return mk(d.y, d.z);
+  return t_project_rec(e, n, d);
+}
+__device__ __forceinline__ bool t_embed(PcEval *e, int n, Itv u) {
+  const int4 d = node(e, n);
+  if (d.x == K_VAR) return store_embed(e, d.y, u);
+  if (d.x == K_CONST) return false;
+  return t_embed_rec(e, n, d, u);
+}
+__device__ __forceinline__ bool f_ask(PcEval *e, int n) {
+  const int4 d = node(e, n);
+  if (d.x == K_PVAR) return !has0(load(e, d.y));
+  if (d.x == K_NVAR) return below_point(load(e, d.y), 0);
+  return f_ask_rec(e, d);
+}
+__device__ __forceinline__ bool f_nask(PcEval *e, int n) {
+  const int4 d = node(e, n);
+  if (d.x == K_PVAR) return below_point(load(e, d.y), 0);
+  if (d.x == K_NVAR) return !has0(load(e, d.y));
+  return f_nask_rec(e, d);
+}
+__device__ __forceinline__ bool f_deduce(PcEval *e, int n) {
+  const int4 d = node(e, n);
+  if (d.x == K_PVAR) return store_embed(e, d.y, mk(1, 1));
+  if (d.x == K_NVAR) return store_embed(e, d.y, mk(0, 0));
+  return f_deduce_rec(e, d);
+}
+__device__ __forceinline__ bool f_contra(PcEval *e, int n) {
+  const int4 d = node(e, n);
+  if (d.x == K_PVAR) return store_embed(e, d.y, mk(0, 0));
+  if (d.x == K_NVAR) return store_embed(e, d.y, mk(1, 1));
+  return f_contra_rec(e, d);
+}
 
 // Formula::project (formula.hpp:1097-1102): the truth value in {0, 1}
 static __device__ __noinline__ Itv f_project(PcEval *e, int n) {
@@ -241,8 +281,7 @@ static __device__ __noinline__ Itv f_project(PcEval *e, int n) {
 
 // Term::project (terms.hpp:741): Variable :69, Constant :35, Unary :155,
 // Binary :399, Nary :465
-__device__ __noinline__ Itv t_project(PcEval *e, int n) {
-  const int4 d = node(e, n);
+__device__ __noinline__ Itv t_project_rec(PcEval *e, int n, int4 d) {
   switch (d.x) {
     case K_VAR: return load(e, d.y);
     case K_CONST: return mk(d.y, d.z);
@@ -307,8 +346,7 @@ static __device__ __noinline__ bool f_embed(PcEval *e, int n, Itv u) {
 
 // Term::embed (terms.hpp:737): Variable :65, Constant :34, Unary :149,
 // Binary :376, Nary :480
-__device__ __noinline__ bool t_embed(PcEval *e, int n, Itv u) {
-  const int4 d = node(e, n);
+__device__ __noinline__ bool t_embed_rec(PcEval *e, int n, int4 d, Itv u) {
   switch (d.x) {
     case K_VAR: return store_embed(e, d.y, u);
     case K_CONST: return false;
@@ -403,8 +441,7 @@ static __device__ __noinline__ bool cmp_deduce(PcEval *e, int kind, int L, int R
 // VariableLiteral :101-160, False :184-195, True :220-230, Conjunction
 // :268-288, Disjunction :338-358, Biconditional :408-438, Implication
 // :482-503, ExclusiveDisjunction :546-574
-__device__ __noinline__ bool f_ask(PcEval *e, int n) {
-  const int4 d = node(e, n);
+__device__ __noinline__ bool f_ask_rec(PcEval *e, int4 d) {
   switch (d.x) {
     case K_PVAR: return !has0(load(e, d.y));
     case K_NVAR: return below_point(load(e, d.y), 0);
@@ -418,8 +455,7 @@ __device__ __noinline__ bool f_ask(PcEval *e, int n) {
     default: return cmp_ask(e, d.x, d.y, d.z);
   }
 }
-__device__ __noinline__ bool f_nask(PcEval *e, int n) {
-  const int4 d = node(e, n);
+__device__ __noinline__ bool f_nask_rec(PcEval *e, int4 d) {
   switch (d.x) {
     case K_PVAR: return below_point(load(e, d.y), 0);
     case K_NVAR: return !has0(load(e, d.y));
@@ -433,8 +469,7 @@ __device__ __noinline__ bool f_nask(PcEval *e, int n) {
     default: return cmp_ask(e, negated(d.x), d.y, d.z);
   }
 }
-__device__ __noinline__ bool f_deduce(PcEval *e, int n) {
-  const int4 d = node(e, n);
+__device__ __noinline__ bool f_deduce_rec(PcEval *e, int4 d) {
   const int f = d.y, g = d.z;
   switch (d.x) {
     case K_PVAR: return store_embed(e, d.y, mk(1, 1));
@@ -474,8 +509,7 @@ __device__ __noinline__ bool f_deduce(PcEval *e, int n) {
     default: return cmp_deduce(e, d.x, f, g);
   }
 }
-__device__ __noinline__ bool f_contra(PcEval *e, int n) {
-  const int4 d = node(e, n);
+__device__ __noinline__ bool f_contra_rec(PcEval *e, int4 d) {
   const int f = d.y, g = d.z;
   switch (d.x) {
     case K_PVAR: return store_embed(e, d.y, mk(0, 0));
@@ -646,9 +680,10 @@ PcState *pc_state(pirgpu_ctx *ctx) {
 // on an n-ary node; f_embed -> f_deduce -> cmp_deduce and f_project -> f_ask
 // -> cmp_ask on a formula), and the non-recursive helpers (residuals,
 // division) sit only at the end of a chain.  With the frames ptxas reports
-// (-Xptxas -v: t_embed 120 B, t_project 72 B, the formula functions <= 48 B,
-// left_residual + idiv 160 B) a level needs at most 192 B and the end of the
-// chain 160 B more; 256 B per level plus 1 KB covers both with room.
+// (-Xptxas -v: t_embed_rec <= 136 B, t_project_rec 72 B, f_embed 16 B +
+// f_deduce_rec 64 B + cmp_deduce <= 104 B, left_residual 48 B + idiv <= 128 B)
+// a level needs at most 208 B and the end of the chain 176 B more; 256 B per
+// level plus 1 KB covers both.
 constexpr size_t PC_FRAME_BYTES = 256;
 size_t pc_stack_need(int depth) { return (size_t)(depth + 2) * PC_FRAME_BYTES + 1024; }
 
@@ -853,6 +888,9 @@ int pc_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
   if ((r = pc_prepare_stack(ctx, s))) return r;
   const long long max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
   const long long timeout = opts.barrier_timeout_ns > 0 ? opts.barrier_timeout_ns : 2000000000ll;
+  // the kernel uses 16 B of shared memory: give the rest of the SM's
+  // on-chip memory to L1, which holds the threads' call stacks
+  PIR_CK(cudaFuncSetAttribute(k_pc_fixpoint, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
   int occ = 0;
   PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pc_fixpoint, PC_BLOCK, 0));
   if (occ < 1) return set_err(ctx, PIR_ECUDA, "PC kernel does not fit on an SM");

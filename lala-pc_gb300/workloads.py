@@ -386,3 +386,134 @@ def queens(n):
         for k in (0, j - i, i - j):
             op.append(EQ); x.append(false); y.append(d); z.append(c0 + k + n - 1)
     return Instance(lb, ub, op, x, y, z, queens=n)
+
+
+# ----------------------------------------------------------------------- PC --
+# Tree propagators for lala-pc's PC domain (tape format of include/pirgpu.h,
+# enum pc_kind), built from the constraint shapes of lala-pc's PC tests
+# (tests/pc_test.cpp): pseudo-boolean / linear sums (PseudoBoolean*), reified
+# differences (ResourceConstraint*, InfiniteDomain*), disjunctive temporal
+# constraints (TemporalConstraint*) and max equalities (MaxConstraint*).
+PC_MIX = (("linear", .40), ("reified", .30), ("disjunctive", .20), ("max", .10))
+_PC = dict(VAR=0, CONST=1, ADD=5, SUB=6, MUL=7, MAX=13, NADD=14, PVAR=16, LEQ=20, EQ=22, OR=25, EQUIV=26, ARG=29)
+
+
+def pc_mix(nvars=1_000_000, nprops=1_000_000, scale=1000, seed=0, terms=4, key=31):
+    """A planted PC instance: a hidden assignment s (s_v in [lb_v, ub_v]) is
+    drawn first and every propagator holds under it, so the fixpoint is not
+    empty and its rounds narrow domains towards s.  Shapes (nodes per tree):
+
+      linear       sum_k a_k * x_k <= b, `terms` terms, a_k ~ U[1, 5],
+                   b = sum a_k s_k + U[0, 10 * terms]      (3*terms + terms + 3)
+      reified      r <=> (x - y <= k), r a fresh 0/1 variable,
+                   k = s_x - s_y + U[-10, 10]              (7)
+      disjunctive  (x + dx <= y) or (y + dy <= x), the disjunct s satisfies
+                   with a slack drawn in [0, |s_x - s_y|]  (11)
+      max          z = max(x, y), z fresh with domain [-2S, 2S]  (5)
+
+    Returns (tape (n, 4) int32, roots int32, lb int32, ub int32, hidden int64)."""
+    rng = Rng(seed, key)
+    lb, ub = _bounds(rng, nvars, scale)
+    s = rng.integers(lb, ub, nvars)
+    counts = _counts(nprops, PC_MIX)
+    blocks, roots = [], []
+    extra_lb, extra_ub, extra_s = [], [], []
+    base = [0]
+    nv = [nvars]
+
+    def fresh(lo, hi, val):
+        n = len(val)
+        idx = np.arange(nv[0], nv[0] + n)
+        nv[0] += n
+        extra_lb.append(np.broadcast_to(np.asarray(lo, np.int64), (n,)))
+        extra_ub.append(np.broadcast_to(np.asarray(hi, np.int64), (n,)))
+        extra_s.append(np.asarray(val, np.int64))
+        return idx
+
+    def emit(rows, width, root):
+        """rows: (count, width, 4) with child fields relative to the tree."""
+        c = rows.shape[0]
+        start = base[0] + width * np.arange(c)
+        rows = rows.copy()
+        k = rows[:, :, 0]
+        refs_a = ~np.isin(k, [_PC["VAR"], _PC["CONST"], _PC["PVAR"]])
+        refs_b = np.isin(k, [_PC["ADD"], _PC["SUB"], _PC["MUL"], _PC["MAX"], _PC["LEQ"], _PC["EQ"], _PC["OR"],
+                             _PC["EQUIV"]])
+        rows[:, :, 1] += np.where(refs_a, start[:, None], 0)
+        rows[:, :, 2] += np.where(refs_b, start[:, None], 0)
+        blocks.append(rows.reshape(-1, 4))
+        roots.append(start + root)
+        base[0] += c * width
+
+    def draw(c):
+        return rng.integers(0, nvars - 1, c)
+
+    P = _PC
+    c = counts["linear"]
+    if c:
+        K = terms
+        w = 4 * K + 3
+        rows = np.zeros((c, w, 4), np.int64)
+        xs = np.stack([draw(c) for _ in range(K)], 1)
+        a = rng.integers(1, 5, c * K).reshape(c, K)
+        for t in range(K):
+            rows[:, 3 * t] = np.stack([np.full(c, P["VAR"]), xs[:, t], np.zeros(c), np.zeros(c)], 1)
+            rows[:, 3 * t + 1] = np.stack([np.full(c, P["CONST"]), a[:, t], a[:, t], np.zeros(c)], 1)
+            rows[:, 3 * t + 2] = [P["MUL"], 3 * t + 1, 3 * t, 0]
+            rows[:, 3 * K + t] = [P["ARG"], 3 * t + 2, 0, 0]
+        b = (a * s[xs]).sum(1) + rng.integers(0, 10 * K, c)
+        rows[:, 4 * K] = [P["NADD"], 3 * K, K, 0]
+        rows[:, 4 * K + 1] = np.stack([np.full(c, P["CONST"]), b, b, np.zeros(c)], 1)
+        rows[:, 4 * K + 2] = [P["LEQ"], 4 * K, 4 * K + 1, 0]
+        emit(rows, w, 4 * K + 2)
+    c = counts["reified"]
+    if c:
+        x, y = draw(c), draw(c)
+        k = s[x] - s[y] + rng.integers(-10, 10, c)
+        r = fresh(0, 1, (s[x] - s[y] <= k).astype(np.int64))
+        rows = np.zeros((c, 7, 4), np.int64)
+        rows[:, 0] = np.stack([np.full(c, P["VAR"]), x, np.zeros(c), np.zeros(c)], 1)
+        rows[:, 1] = np.stack([np.full(c, P["VAR"]), y, np.zeros(c), np.zeros(c)], 1)
+        rows[:, 2] = [P["SUB"], 0, 1, 0]
+        rows[:, 3] = np.stack([np.full(c, P["CONST"]), k, k, np.zeros(c)], 1)
+        rows[:, 4] = [P["LEQ"], 2, 3, 0]
+        rows[:, 5] = np.stack([np.full(c, P["PVAR"]), r, np.zeros(c), np.zeros(c)], 1)
+        rows[:, 6] = [P["EQUIV"], 5, 4, 0]
+        emit(rows, 7, 6)
+    c = counts["disjunctive"]
+    if c:
+        x, y = draw(c), draw(c)
+        gap = np.abs(s[x] - s[y])
+        first = s[x] <= s[y]  # x + dx <= y holds for dx <= gap
+        d_hold = rng.integers(0, gap, c)
+        d_other = rng.integers(1, 20, c)
+        dx = np.where(first, d_hold, d_other)
+        dy = np.where(first, d_other, d_hold)
+        rows = np.zeros((c, 11, 4), np.int64)
+        for j, v in ((0, x), (3, y), (5, y), (8, x)):
+            rows[:, j] = np.stack([np.full(c, P["VAR"]), v, np.zeros(c), np.zeros(c)], 1)
+        rows[:, 1] = np.stack([np.full(c, P["CONST"]), dx, dx, np.zeros(c)], 1)
+        rows[:, 6] = np.stack([np.full(c, P["CONST"]), dy, dy, np.zeros(c)], 1)
+        rows[:, 2] = [P["ADD"], 0, 1, 0]
+        rows[:, 4] = [P["LEQ"], 2, 3, 0]
+        rows[:, 7] = [P["ADD"], 5, 6, 0]
+        rows[:, 9] = [P["LEQ"], 7, 8, 0]
+        rows[:, 10] = [P["OR"], 4, 9, 0]
+        emit(rows, 11, 10)
+    c = counts["max"]
+    if c:
+        x, y = draw(c), draw(c)
+        z = fresh(-2 * scale, 2 * scale, np.maximum(s[x], s[y]))
+        rows = np.zeros((c, 5, 4), np.int64)
+        rows[:, 0] = np.stack([np.full(c, P["VAR"]), x, np.zeros(c), np.zeros(c)], 1)
+        rows[:, 1] = np.stack([np.full(c, P["VAR"]), y, np.zeros(c), np.zeros(c)], 1)
+        rows[:, 2] = [P["MAX"], 0, 1, 0]
+        rows[:, 3] = np.stack([np.full(c, P["VAR"]), z, np.zeros(c), np.zeros(c)], 1)
+        rows[:, 4] = [P["EQ"], 2, 3, 0]
+        emit(rows, 5, 4)
+    tape = np.ascontiguousarray(np.concatenate(blocks), np.int32)
+    roots = np.ascontiguousarray(np.concatenate(roots), np.int32)
+    lb_all = np.concatenate([lb] + extra_lb)
+    ub_all = np.concatenate([ub] + extra_ub)
+    hidden = np.concatenate([s] + extra_s)
+    return tape, roots, np.ascontiguousarray(lb_all, np.int32), np.ascontiguousarray(ub_all, np.int32), hidden

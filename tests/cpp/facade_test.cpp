@@ -7,6 +7,8 @@
 
 #include "pirgpu.hpp"
 #include "pirgpu_fzn.hpp"
+#include "pirgpu_fzn_pc.hpp"
+#include "pirgpu_pc.hpp"
 
 using namespace lala_gpu;
 
@@ -193,6 +195,76 @@ static void element_fzn() {
   EXPECT(!d.has_error());
 }
 
+// ---- PC (lala_gpu::PC, include/pirgpu_pc.hpp) ----
+
+// tests/pc_test.cpp:132-139 written with the term / formula factories:
+// x, y in [0, 10], x + y <= 5.
+static void pc_temporal_constraint1() {
+  using T = pc::Term;
+  using F = pc::Formula;
+  PC ipc(std::vector<Itv>{Itv(0, 10), Itv(0, 10)});
+  IDiagnostics d;
+  PC::tell_type t;
+  EXPECT(ipc.interpret_tell(F::make_leq(T::make_add(T::make_var(0), T::make_var(1)), T::make_constant(Itv(5, 5))), t, d));
+  EXPECT(ipc.interpret_tell(F::make_leq(T::make_var(0), T::make_constant(Itv(4, 4))), t, d));  // a store bound
+  EXPECT(ipc.deduce(t));
+  EXPECT(ipc.num_deductions() == 1);
+  EXPECT(ipc.fixpoint() == PIR_OK);
+  EXPECT(ipc[0] == Itv(0, 4) && ipc[1] == Itv(0, 5));
+  EXPECT(!ipc.is_extractable());
+}
+
+// tests/pc_test.cpp:360-371 through the FlatZinc front end, in two tells.
+static void pc_resource_constraint1() {
+  fzn::PcModel m;
+  IDiagnostics d;
+  EXPECT(fzn::compile_pc("var int: x; var int: y; var int: b; constraint int_ge(x, 5); constraint int_le(x, 10);"
+                         " constraint int_ge(y, 9); constraint int_le(y, 15); constraint int_ge(b, 0);"
+                         " constraint int_le(b, 1); constraint int_eq(b, bool_and(int_le(int_minus(x, y), 0),"
+                         " int_le(int_minus(y, x), 2)));",
+                         m, d));
+  std::unique_ptr<PC> ipc = fzn::make_pc(m);
+  EXPECT(ipc->num_deductions() == 1);
+  EXPECT(ipc->fixpoint() == PIR_OK);
+  EXPECT((*ipc)[0] == Itv(5, 10) && (*ipc)[1] == Itv(9, 15));
+  EXPECT(fzn::interpret_and_tell(*ipc, m, "constraint int_eq(b, 1);", d));
+  EXPECT(ipc->fixpoint() == PIR_OK);
+  EXPECT((*ipc)[0] == Itv(7, 10) && (*ipc)[1] == Itv(9, 12) && (*ipc)[2] == Itv(1, 1));
+  EXPECT(!d.has_error());
+}
+
+// The reference's loop GaussSeidelIteration{}.fixpoint(num_deductions(),
+// deduce) (tests/pc_test.cpp:91-94) over deduce(i), against fixpoint(); and
+// snapshot / restore around a tell.
+static void pc_drop_in_and_snapshot() {
+  fzn::PcModel m;
+  IDiagnostics d;
+  EXPECT(fzn::compile_pc("var 0..4: x; var 2..5: y; var 0..10: z; constraint int_min(x, y, z);"
+                         " constraint int_le(z, 3); constraint int_ne(x, 0);",
+                         m, d));
+  std::unique_ptr<PC> a = fzn::make_pc(m), b = fzn::make_pc(m);
+  bool changed = true;
+  while (changed) {
+    changed = false;
+    for (int64_t i = 0; i < a->num_deductions(); ++i) changed |= a->deduce(i);
+  }
+  EXPECT(b->fixpoint() == PIR_OK);
+  for (int v = 0; v < 3; ++v) EXPECT((*a)[v] == (*b)[v]);
+  EXPECT((*b)[0] == Itv(1, 4) && (*b)[2] == Itv(1, 3));
+  auto snap = b->snapshot();
+  EXPECT(fzn::interpret_and_tell(*b, m, "constraint int_gt(x, y);", d));
+  EXPECT(b->num_deductions() == 3);
+  EXPECT(b->fixpoint() == PIR_OK);
+  EXPECT((*b)[0] == Itv(3, 4) && (*b)[1] == Itv(2, 3));
+  // restore pops from the end of the sorted propagators (pc.hpp:717-724): the
+  // count and the store come back, the propagator dropped is the last in the
+  // (kind, length) order -- here x != 0, not the x > y just told
+  b->restore(snap);
+  EXPECT(b->num_deductions() == 2);
+  EXPECT((*b)[0] == Itv(1, 4));
+  EXPECT(!d.has_error());
+}
+
 int main() {
   ternary_problem();
   top_prop();
@@ -204,6 +276,9 @@ int main() {
   interpretation_error();
   queens6();
   element_fzn();
+  pc_temporal_constraint1();
+  pc_resource_constraint1();
+  pc_drop_in_and_snapshot();
   std::printf("%d failures\n", failures);
   return failures ? 1 : 0;
 }

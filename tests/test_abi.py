@@ -64,3 +64,22 @@ def test_python_constants_match_header():
     src = open(os.path.join(ROOT, "include", "pirgpu.h")).read()
     assert int(re.search(r"#define PIR_PERSISTENT_VARIANTS (\d+)", src).group(1)) == pirgpu.PERSISTENT_VARIANTS
     assert int(re.search(r"#define PIR_NODE_VARIANTS (\d+)", src).group(1)) == pirgpu.NODE_VARIANTS
+
+
+def test_pc_kinds_match_header_builder_and_oracle():
+    """The tape node kinds of include/pirgpu.h (enum pc_kind) are the ones the
+    Python builder (pc.py) and the oracle (oracle/pc_oracle.h) use."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "lala-pc_gb300"))
+    import pc as P
+    src = open(os.path.join(ROOT, "include", "pirgpu.h")).read()
+    orc = open(os.path.join(ROOT, "oracle", "pc_oracle.h")).read()
+    enum = src[src.index("enum pc_kind"):]
+    enum = enum[:enum.index("};")]
+    kinds = dict((m.group(1), int(m.group(2))) for m in re.finditer(r"PC_([A-Z_]+) = (\d+)", enum))
+    assert len(kinds) == 31 and kinds["NUM_KINDS"] == P.NUM_KINDS == 30
+    for name, v in kinds.items():
+        if name != "NUM_KINDS":
+            assert getattr(P, name) == v, name
+        assert int(re.search(r"ORC_PC_%s = (\d+)" % name, orc).group(1)) == v, name
+    assert int(re.search(r"#define PC_MAX_DEPTH (\d+)", src).group(1)) == P.MAX_DEPTH
