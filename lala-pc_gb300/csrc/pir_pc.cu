@@ -56,6 +56,11 @@ struct PcState {
   size_t cap_roots = 0;
   int2 *d_next = nullptr;         // the store's second copy (the joins of a Jacobi round)
   size_t cap_next = 0;
+  std::vector<int> tree_base;     // per root node: first node of its tree, or -1 (recursive path)
+  int *d_bases = nullptr;         // tree_base of each propagator, engine order
+  size_t cap_bases = 0;
+  std::vector<unsigned> stamp;    // scratch of the tree check
+  unsigned stamp_gen = 0;
   size_t stack_bytes = 0;         // per-thread stack limit this context asked for
 };
 
@@ -120,6 +125,16 @@ __device__ __forceinline__ long long xmul(long long p, long long q) {
 }
 __device__ __forceinline__ Itv imul(Itv a, Itv b) {
   if (is_bot(a) || is_bot(b)) return iempty();
+  if (b.l == b.u && b.l != MINF && b.l != INF) {  // a singleton factor: two corners suffice
+    const Itv t = a;
+    a = b;
+    b = t;
+  }
+  if (a.l == a.u && a.l != MINF && a.l != INF) {
+    const long long p0 = xmul(a.l, xl(b.l)), p1 = xmul(a.l, xu(b.u));
+    const long long lo = mn(p0, p1), hi = mx(p0, p1);
+    return mk(lo == -XINF ? MINF : cl(lo), hi == XINF ? INF : cl(hi));
+  }
   const long long p0 = xmul(xl(a.l), xl(b.l)), p1 = xmul(xl(a.l), xu(b.u));
   const long long p2 = xmul(xu(a.u), xl(b.l)), p3 = xmul(xu(a.u), xu(b.u));
   const long long lo = mn(mn(p0, p1), mn(p2, p3)), hi = mx(mx(p0, p1), mx(p2, p3));
@@ -149,7 +164,7 @@ __device__ __forceinline__ long long xquo(int op, long long y, long long z) {
 // Exact hull of { y op z : y in a, z in b, z != 0 }: the quotient is monotone
 // in each argument on a sign-definite divisor range, so the corners of b's
 // negative and positive parts bound it.
-static __device__ __noinline__ Itv idiv(int op, Itv a, Itv b) {
+static __device__ __noinline__ Itv idiv_hull(int op, Itv a, Itv b) {
   if (is_bot(a) || is_bot(b) || is_point(b, 0)) return iempty();
   const long long yl = xl(a.l), yu = xu(a.u);
   long long lo = LLONG_MAX, hi = LLONG_MIN;
@@ -166,6 +181,19 @@ static __device__ __noinline__ Itv idiv(int op, Itv a, Itv b) {
     hi = mx(hi, mx(mx(q0, q1), mx(q2, q3)));
   }
   return mk(lo <= -XINF ? MINF : cl(lo), hi >= XINF ? INF : cl(hi));
+}
+// A singleton divisor c (the coefficient of a linear term): the quotient is
+// monotone in the dividend, so the two dividend bounds give the hull -- the
+// same values idiv_hull computes at its corners.
+__device__ __forceinline__ Itv idiv(int op, Itv a, Itv b) {
+  if (b.l == b.u && b.l != 0 && b.l != MINF && b.l != INF && !is_bot(a)) {
+    const long long c = b.l;
+    const long long ql = a.l == MINF ? (c > 0 ? -XINF : XINF) : d_div(op, a.l, c);
+    const long long qu = a.u == INF ? (c > 0 ? XINF : -XINF) : d_div(op, a.u, c);
+    const long long lo = mn(ql, qu), hi = mx(ql, qu);
+    return mk(lo <= -XINF ? MINF : cl(lo), hi >= XINF ? INF : cl(hi));
+  }
+  return idiv_hull(op, a, b);
 }
 // GroupAdd::rev_op (terms.hpp:190-194): all + additive_inverse(t), the
 // inverse negating each bound without swapping them, so that the result is
@@ -305,7 +333,7 @@ __device__ __noinline__ Itv t_project_rec(PcEval *e, int n, int4 d) {
 }
 
 // Group*::left_residual (terms.hpp:196-324): x of `x op y = u`
-static __device__ __noinline__ Itv left_residual(int kind, Itv u, Itv y) {
+__device__ __forceinline__ Itv left_residual(int kind, Itv u, Itv y) {
   switch (kind) {
     case K_ADD: return isub(u, y);
     case K_SUB: return iadd(u, y);
@@ -322,7 +350,7 @@ static __device__ __noinline__ Itv left_residual(int kind, Itv u, Itv y) {
   }
 }
 // Group*::right_residual: y of `x op y = u`; r is y's interval for a division
-static __device__ __noinline__ Itv right_residual(int kind, Itv u, Itv x, Itv r) {
+__device__ __forceinline__ Itv right_residual(int kind, Itv u, Itv x, Itv r) {
   switch (kind) {
     case K_SUB: return isub(x, u);
     case K_ADD:
@@ -553,15 +581,317 @@ __device__ __noinline__ bool f_contra_rec(PcEval *e, int4 d) {
 // ---------------------------------------------------------------- kernels --
 constexpr int PC_BLOCK = 128;
 
+// ------------------------------------------- trees without the call stack --
+// In a Jacobi round every read of a propagator sees the round's initial
+// store, so what the recursive descent computes on the way down is a pure
+// function of that store: every term's projection and every formula's ask /
+// nask.  For a tree (each node reached once from the root) whose nodes are
+// the contiguous tape range [base, root] (children before parents), both
+// passes run without recursion over per-thread arrays in shared memory:
+//   pass 1, base -> root: each node's interval, or its ask (bit 0) and nask
+//     (bit 1), from its children's;
+//   pass 2, root -> base: the requests the reference's member functions
+//     would issue (deduce / contradeduce of a formula, embed of an interval
+//     into a term), each node receiving at most one.
+// The joins, and with them the round's result and its narrowing count, are
+// those of the recursive descent.  (They can differ only after a deduction
+// of the same propagator emptied a variable -- the recursive path then reads
+// the store as bot in Formula::project -- and then the round fails either
+// way.)  Other propagators take the recursive path.
+constexpr int PC_TREE_MAX = 24;  // nodes per tree on this path
+constexpr size_t PC_TREE_SMEM = (size_t)PC_TREE_MAX * PC_BLOCK * 3 * sizeof(int2);
+enum : int { RQ_NONE = 0, RQ_DEDUCE = 1, RQ_CONTRA = 2, RQ_EMBED = 3 };
+
+// ask / nask of a comparison from its operands' intervals (Equality :620,
+// Inequality :758)
+__device__ __forceinline__ bool cmp_holds(int kind, Itv l, Itv r) {
+  switch (kind) {
+    case K_EQ: return l.l == r.l && l.u == r.u && l.l == l.u;
+    case K_NEQ: return is_bot(imeet(l, r));
+    case K_LEQ: return l.u <= r.l;
+    default: return l.l > r.u;
+  }
+}
+
+// Per-thread slices of the node-major shared arrays: node j of this thread
+// is element j * PC_BLOCK, so the threads of a warp touch consecutive words.
+// The tree is staged first with independent loads -- its nodes, packed to 8
+// bytes, then the store intervals of its variable leaves -- so that a tree
+// costs two memory latencies instead of a chain of one per node.
+//   node[j].x: kind | request << 5 | first operand << 8 | second operand (or
+//              operand count) << 16, operands as indices into the tree;
+//   node[j].y: the variable of a VAR / PVAR / NVAR leaf;
+//   val[j]:    the node's interval (a CONST's value, a variable's interval,
+//              a term's projection), or ask | nask << 1 of a formula;
+//   req[j]:    the interval of an embed request, or the store interval of a
+//              literal leaf.
+struct TreeScratch {
+  int2 *node, *val, *req;
+  __device__ __forceinline__ Itv v(int j) const {
+    const int2 t = val[j * PC_BLOCK];
+    return mk(t.x, t.y);
+  }
+  __device__ __forceinline__ int bits(int j) const { return val[j * PC_BLOCK].x; }
+  __device__ __forceinline__ void set(int j, Itv a) { val[j * PC_BLOCK] = make_int2(a.l, a.u); }
+  __device__ __forceinline__ int word(int j) const { return node[j * PC_BLOCK].x; }
+  __device__ __forceinline__ void send(int j, int k) { node[j * PC_BLOCK].x |= k << 5; }
+  __device__ __forceinline__ void send(int j, Itv u) {
+    node[j * PC_BLOCK].x |= RQ_EMBED << 5;
+    req[j * PC_BLOCK] = make_int2(u.l, u.u);
+  }
+};
+
+// VStore::embed with the variable's interval already read (cur)
+__device__ __forceinline__ void join(PcEval *e, int v, Itv cur, Itv u) {
+  bool ch = false;
+  if (u.l > cur.l) {
+    asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(&e->wr[v].x), "r"(u.l) : "memory");
+    ch = true;
+    ++e->narrowed;
+  }
+  if (u.u < cur.u) {
+    asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(&e->wr[v].y), "r"(u.u) : "memory");
+    ch = true;
+    ++e->narrowed;
+  }
+  if (ch && is_bot(imeet(cur, u))) e->failed = 1;
+}
+
+__device__ __forceinline__ int pack_node(int4 d, int base) {
+  const int k = d.x;
+  if (k == K_VAR || k == K_PVAR || k == K_NVAR || k == K_CONST || k == K_TRUE || k == K_FALSE) return k;
+  if (k == K_FORMULA || k == K_NEG || k == K_ABS || k == K_ARG) return k | (d.y - base) << 8;
+  if (k == K_NADD || k == K_NMUL) return k | (d.y - base) << 8 | d.z << 16;
+  return k | (d.y - base) << 8 | (d.z - base) << 16;
+}
+
+static __device__ __noinline__ void tree_deduce(PcEval *e, int root, int base, TreeScratch sc) {
+  const int4 *tape = e->tape;
+  const int n = root - base + 1;
+  // stage the nodes, four independent loads in flight at a time
+  for (int j = 0; j < n; j += 4) {
+    int4 t[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (j + k < n) t[k] = __ldg(tape + base + j + k);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (j + k < n) {
+        sc.node[(j + k) * PC_BLOCK] = make_int2(pack_node(t[k], base), t[k].y);
+        if (t[k].x == K_CONST) sc.set(j + k, mk(t[k].y, t[k].z));
+      }
+  }
+  // then the intervals of the variable leaves
+  for (int j = 0; j < n; j += 4) {
+    int2 v[4];
+    bool is_var[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      is_var[k] = false;
+      if (j + k < n) {
+        const int2 w = sc.node[(j + k) * PC_BLOCK];
+        const int kind = w.x & 31;
+        is_var[k] = kind == K_VAR || kind == K_PVAR || kind == K_NVAR;
+        if (is_var[k]) v[k] = __ldcg(e->rd + w.y);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (is_var[k]) sc.val[(j + k) * PC_BLOCK] = v[k];
+  }
+  // pass 1: projections and entailments, children first
+  for (int j = 0; j < n; ++j) {
+    const int w = sc.word(j);
+    const int kind = w & 31, a = (w >> 8) & 255, b = w >> 16;
+    Itv r;
+    switch (kind) {
+      case K_VAR:
+      case K_CONST: continue;  // staged
+      case K_FORMULA: {
+        const int f = sc.bits(a);
+        r = mk(0, 1);
+        if (f & 1) r = imeet(r, mk(1, 1));
+        if (f & 2) r = imeet(r, mk(0, 0));
+        break;
+      }
+      case K_NEG: r = ineg(sc.v(a)); break;
+      case K_ABS: r = iabs(sc.v(a)); break;
+      case K_ARG: r = sc.v(a); break;
+      case K_NADD:
+      case K_NMUL: {
+        r = sc.v(a);
+        for (int i = 1; i < b; ++i) r = kind == K_NADD ? iadd(r, sc.v(a + i)) : imul(r, sc.v(a + i));
+        break;
+      }
+      case K_PVAR:
+      case K_NVAR: {
+        const Itv x = sc.v(j);
+        sc.req[j * PC_BLOCK] = make_int2(x.l, x.u);  // keep the literal's interval for pass 2
+        const int t = !has0(x), f = below_point(x, 0);
+        r = mk(kind == K_PVAR ? (t | f << 1) : (f | t << 1), 0);
+        break;
+      }
+      case K_TRUE: r = mk(1, 0); break;
+      case K_FALSE: r = mk(2, 0); break;
+      case K_LEQ:
+      case K_GT:
+      case K_EQ:
+      case K_NEQ: {
+        const Itv x = sc.v(a), y = sc.v(b);
+        r = mk((int)cmp_holds(kind, x, y) | (int)cmp_holds(negated(kind), x, y) << 1, 0);
+        break;
+      }
+      case K_AND:
+      case K_OR:
+      case K_EQUIV:
+      case K_IMPLY:
+      case K_XOR: {
+        const int f = sc.bits(a), g = sc.bits(b);
+        const bool af = f & 1, nf = f & 2, ag = g & 1, ng = g & 2;
+        bool ask, nask;
+        if (kind == K_AND) ask = af && ag, nask = nf || ng;
+        else if (kind == K_OR) ask = af || ag, nask = nf && ng;
+        else if (kind == K_EQUIV) ask = (af && ag) || (nf && ng), nask = (af && ng) || (nf && ag);
+        else if (kind == K_IMPLY) ask = nf || ag, nask = af && ng;
+        else ask = (af && ng) || (nf && ag), nask = (af && ag) || (af && ng);  // xor as written (:552-556)
+        r = mk((int)ask | (int)nask << 1, 0);
+        break;
+      }
+      default: r = ibinary(kind, sc.v(a), sc.v(b));
+    }
+    sc.set(j, r);
+  }
+  // pass 2: requests, parents first
+  sc.send(n - 1, RQ_DEDUCE);
+  for (int j = n - 1; j >= 0; --j) {
+    const int w = sc.word(j);
+    const int t = (w >> 5) & 3;
+    if (t == RQ_NONE) continue;
+    const int kind = w & 31, a = (w >> 8) & 255, b = w >> 16;
+    if (t == RQ_EMBED) {
+      const int2 uu = sc.req[j * PC_BLOCK];
+      const Itv u = mk(uu.x, uu.y);
+      switch (kind) {
+        case K_VAR: join(e, sc.node[j * PC_BLOCK].y, sc.v(j), u); break;
+        case K_CONST: break;
+        case K_FORMULA:
+          if (below_point(u, 1)) sc.send(a, RQ_DEDUCE);
+          else if (below_point(u, 0)) sc.send(a, RQ_CONTRA);
+          break;
+        case K_NEG: sc.send(a, ineg(u)); break;
+        case K_ABS: sc.send(a, ifjoin(u, ineg(u))); break;
+        case K_NADD:
+        case K_NMUL: {
+          const Itv all = sc.v(j);
+          if (kind == K_NMUL && is_point(all, 0)) break;
+          for (int i = 0; i < b; ++i) {
+            const int c = (sc.word(a + i) >> 8) & 255;  // the operand behind slot a + i
+            const Itv tmp = sc.v(c);
+            sc.send(c, kind == K_NADD ? isub(u, rev_add(all, tmp)) : left_residual(K_MUL, u, idiv(OP_EDIV, all, tmp)));
+          }
+          break;
+        }
+        default: {  // binary term
+          const Itv xv = sc.v(a), yv = sc.v(b);
+          if ((sc.word(a) & 31) != K_CONST) sc.send(a, left_residual(kind, u, yv));
+          if ((sc.word(b) & 31) != K_CONST)
+            sc.send(b, right_residual(kind, u, xv, (kind >= K_TDIV && kind <= K_EDIV) ? yv : itop()));
+        }
+      }
+      continue;
+    }
+    const bool c = t == RQ_CONTRA;
+    switch (kind) {
+      case K_PVAR:
+      case K_NVAR: {
+        const int2 x = sc.req[j * PC_BLOCK];
+        const bool one = (kind == K_PVAR) != c;
+        join(e, sc.node[j * PC_BLOCK].y, mk(x.x, x.y), one ? mk(1, 1) : mk(0, 0));
+        break;
+      }
+      case K_TRUE:
+        if (c) e->failed = 1;
+        break;
+      case K_FALSE:
+        if (!c) e->failed = 1;
+        break;
+      case K_LEQ:
+      case K_GT:
+      case K_EQ:
+      case K_NEQ: {
+        const int k = c ? negated(kind) : kind;
+        const bool lc = (sc.word(a) & 31) == K_CONST, rc = (sc.word(b) & 31) == K_CONST;
+        const Itv l = sc.v(a), r = sc.v(b);
+        if (k == K_EQ) {
+          if (!rc) sc.send(b, l);
+          if (!lc) sc.send(a, r);
+        } else if (k == K_NEQ) {
+          if (!rc && l.l == l.u) sc.send(b, ifjoin(mk(max(r.l, prev_lb(l.l)), r.u), mk(r.l, min(r.u, prev_ub(l.u)))));
+          else if (!lc && r.l == r.u)
+            sc.send(a, ifjoin(mk(max(l.l, prev_lb(r.l)), l.u), mk(l.l, min(l.u, prev_ub(r.u)))));
+        } else if (k == K_LEQ) {
+          if (!lc) sc.send(a, mk(MINF, r.u));
+          if (!rc) sc.send(b, mk(l.l, INF));
+        } else {  // GT
+          if (!lc) sc.send(a, mk(max(r.l, prev_lb(r.l)), INF));
+          if (!rc) sc.send(b, mk(MINF, min(l.u, prev_ub(l.u))));
+        }
+        break;
+      }
+      default: {  // connectives
+        const int f = sc.bits(a), g = sc.bits(b);
+        const bool af = f & 1, nf = f & 2, ag = g & 1, ng = g & 2;
+        switch (kind) {
+          case K_AND:
+            if (!c) {
+              sc.send(a, RQ_DEDUCE);
+              sc.send(b, RQ_DEDUCE);
+            } else if (af) sc.send(b, RQ_CONTRA);
+            else if (ag) sc.send(a, RQ_CONTRA);
+            break;
+          case K_OR:
+            if (c) {
+              sc.send(a, RQ_CONTRA);
+              sc.send(b, RQ_CONTRA);
+            } else if (nf) sc.send(b, RQ_DEDUCE);
+            else if (ng) sc.send(a, RQ_DEDUCE);
+            break;
+          case K_EQUIV:
+            if (af) sc.send(b, c ? RQ_CONTRA : RQ_DEDUCE);
+            else if (nf) sc.send(b, c ? RQ_DEDUCE : RQ_CONTRA);
+            else if (ag) sc.send(a, c ? RQ_CONTRA : RQ_DEDUCE);
+            else if (ng) sc.send(a, c ? RQ_DEDUCE : RQ_CONTRA);
+            break;
+          case K_IMPLY:
+            if (af) sc.send(b, c ? RQ_CONTRA : RQ_DEDUCE);
+            else if (ng) sc.send(a, c ? RQ_DEDUCE : RQ_CONTRA);
+            break;
+          default:  // XOR
+            if (af) sc.send(b, c ? RQ_DEDUCE : RQ_CONTRA);
+            else if (nf) sc.send(b, c ? RQ_CONTRA : RQ_DEDUCE);
+            else if (ag) sc.send(a, c ? RQ_DEDUCE : RQ_CONTRA);
+            else if (ng) sc.send(a, c ? RQ_CONTRA : RQ_DEDUCE);
+        }
+      }
+    }
+  }
+}
+
 // Persistent fixpoint over the PC propagators in Jacobi rounds: a round runs
 // every propagator once on store A (a), joining into B (b, equal to A when
 // the round starts); the round's changed / failed bits meet at the first
 // grid barrier; then B is copied into A (two variables per 16-byte access),
 // empty variables are counted, and the second barrier ends the round.
-__global__ void __launch_bounds__(PC_BLOCK) k_pc_fixpoint(const int4 *tape, const int *roots, int nprops, int2 *a,
-                                                         int2 *b, int nvars, Control *ctl, long long max_rounds,
-                                                         long long timeout_ns) {
+__global__ void __launch_bounds__(PC_BLOCK) k_pc_fixpoint(const int4 *tape, const int *roots, const int *bases,
+                                                         int nprops, int2 *a, int2 *b, int nvars, Control *ctl,
+                                                         long long max_rounds, long long timeout_ns) {
   __shared__ unsigned s_bits[2], s_word[2];
+  extern __shared__ __align__(16) unsigned char pc_smem[];
+  TreeScratch sc;
+  int2 *s0 = reinterpret_cast<int2 *>(pc_smem);
+  sc.node = s0 + threadIdx.x;
+  sc.val = s0 + PC_TREE_MAX * PC_BLOCK + threadIdx.x;
+  sc.req = s0 + 2 * PC_TREE_MAX * PC_BLOCK + threadIdx.x;
   PcEval e;
   e.tape = tape;
   e.rd = a;
@@ -593,7 +923,9 @@ __global__ void __launch_bounds__(PC_BLOCK) k_pc_fixpoint(const int4 *tape, cons
     e.narrowed = 0;
     for (int i = gtid; i < nprops; i += gstride) {
       e.failed = 0;
-      f_deduce(&e, __ldg(roots + i));
+      const int base = __ldg(bases + i);
+      if (base >= 0) tree_deduce(&e, __ldg(roots + i), base, sc);
+      else f_deduce(&e, __ldg(roots + i));
       failed |= e.failed;
     }
     narrowed += e.narrowed;
@@ -680,10 +1012,10 @@ PcState *pc_state(pirgpu_ctx *ctx) {
 // on an n-ary node; f_embed -> f_deduce -> cmp_deduce and f_project -> f_ask
 // -> cmp_ask on a formula), and the non-recursive helpers (residuals,
 // division) sit only at the end of a chain.  With the frames ptxas reports
-// (-Xptxas -v: t_embed_rec <= 136 B, t_project_rec 72 B, f_embed 16 B +
-// f_deduce_rec 64 B + cmp_deduce <= 104 B, left_residual 48 B + idiv <= 128 B)
-// a level needs at most 208 B and the end of the chain 176 B more; 256 B per
-// level plus 1 KB covers both.
+// (-Xptxas -v: t_embed_rec <= 112 B, t_project_rec <= 80 B, f_embed 16 B +
+// f_deduce_rec 64 B + cmp_deduce <= 88 B, idiv_hull <= 112 B; the residuals
+// are inlined) a level needs at most 192 B and the end of the chain 112 B
+// more; 256 B per level plus 1 KB covers both.
 constexpr size_t PC_FRAME_BYTES = 256;
 size_t pc_stack_need(int depth) { return (size_t)(depth + 2) * PC_FRAME_BYTES + 1024; }
 
@@ -700,6 +1032,42 @@ int pc_prepare_stack(pirgpu_ctx *ctx, PcState *s) {
   return PIR_OK;
 }
 
+// First node of root's tree when the nodes reached from root are each
+// reached once, form the contiguous range [base, root] and number at most
+// PC_TREE_MAX; else -1.
+int tree_base_of(PcState *s, int root) {
+  if (s->stamp.size() < s->tape.size()) s->stamp.resize(s->tape.size(), 0u);
+  if (++s->stamp_gen == 0u) {
+    std::fill(s->stamp.begin(), s->stamp.end(), 0u);
+    s->stamp_gen = 1u;
+  }
+  const unsigned gen = s->stamp_gen;
+  int todo[2 * PC_TREE_MAX + 2];
+  int top = 0, count = 0, lo = root;
+  todo[top++] = root;
+  while (top > 0) {
+    const int n = todo[--top];
+    if (s->stamp[(size_t)n] == gen || ++count > PC_TREE_MAX) return -1;
+    s->stamp[(size_t)n] = gen;
+    lo = std::min(lo, n);
+    const int4 d = s->tape[(size_t)n];
+    const int k = d.x;
+    int kids[PC_TREE_MAX + 2];
+    int nk = 0;
+    if (k == K_FORMULA || k == K_NEG || k == K_ABS || k == K_ARG) kids[nk++] = d.y;
+    else if (k == K_NADD || k == K_NMUL) {
+      if (d.z > PC_TREE_MAX) return -1;
+      for (int i = 0; i < d.z; ++i) kids[nk++] = d.y + i;
+    } else if ((k >= K_ADD && k <= K_MAX) || (k >= K_LEQ && k <= K_XOR)) {
+      kids[nk++] = d.y;
+      kids[nk++] = d.z;
+    }
+    if (top + nk > 2 * PC_TREE_MAX + 2) return -1;
+    for (int i = 0; i < nk; ++i) todo[top++] = kids[i];
+  }
+  return lo == root - count + 1 ? lo : -1;
+}
+
 int pc_upload(pirgpu_ctx *ctx, PcState *s) {
   int r;
   if (!s->tape.empty()) {
@@ -707,10 +1075,15 @@ int pc_upload(pirgpu_ctx *ctx, PcState *s) {
     PIR_CK(cudaMemcpyAsync(s->d_tape, s->tape.data(), s->tape.size() * sizeof(int4), cudaMemcpyHostToDevice,
                        ctx->stream));
   }
+  std::vector<int> bases(s->roots.size());
   if (!s->roots.empty()) {
     if ((r = ensure(ctx, (void **)&s->d_roots, &s->cap_roots, s->roots.size() * sizeof(int)))) return r;
     PIR_CK(cudaMemcpyAsync(s->d_roots, s->roots.data(), s->roots.size() * sizeof(int), cudaMemcpyHostToDevice,
-                       ctx->stream));
+                           ctx->stream));
+    for (size_t i = 0; i < s->roots.size(); ++i) bases[i] = s->tree_base[(size_t)s->roots[i]];
+    if ((r = ensure(ctx, (void **)&s->d_bases, &s->cap_bases, bases.size() * sizeof(int)))) return r;
+    PIR_CK(cudaMemcpyAsync(s->d_bases, bases.data(), bases.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           ctx->stream));
   }
   PIR_CK(cudaStreamSynchronize(ctx->stream));
   return PIR_OK;
@@ -723,6 +1096,7 @@ void destroy_pc_state(pirgpu_ctx *ctx) {
   if (ctx->pc->d_tape) cudaFree(ctx->pc->d_tape);
   if (ctx->pc->d_roots) cudaFree(ctx->pc->d_roots);
   if (ctx->pc->d_next) cudaFree(ctx->pc->d_next);
+  if (ctx->pc->d_bases) cudaFree(ctx->pc->d_bases);
   delete ctx->pc;
   ctx->pc = nullptr;
 }
@@ -829,7 +1203,11 @@ int pc_tell(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *kind, const int32_t 
     s->len.push_back(std::min(len, 1ll << 40));
     s->depth.push_back(depth[(size_t)i]);
   }
-  for (int32_t p = 0; p < nprops; ++p) s->roots.push_back(roots[p] + off);
+  s->tree_base.resize(s->tape.size(), -1);
+  for (int32_t p = 0; p < nprops; ++p) {
+    s->roots.push_back(roots[p] + off);
+    s->tree_base[(size_t)(roots[p] + off)] = tree_base_of(s, roots[p] + off);
+  }
   const std::vector<int4> &T = s->tape;
   std::stable_sort(s->roots.begin(), s->roots.end(), [&](int x, int y) {
     if (T[(size_t)x].x != T[(size_t)y].x) return T[(size_t)x].x < T[(size_t)y].x;
@@ -888,11 +1266,11 @@ int pc_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
   if ((r = pc_prepare_stack(ctx, s))) return r;
   const long long max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
   const long long timeout = opts.barrier_timeout_ns > 0 ? opts.barrier_timeout_ns : 2000000000ll;
-  // the kernel uses 16 B of shared memory: give the rest of the SM's
-  // on-chip memory to L1, which holds the threads' call stacks
-  PIR_CK(cudaFuncSetAttribute(k_pc_fixpoint, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
+  // shared memory: the per-thread scratch of the trees' two passes
+  PIR_CK(cudaFuncSetAttribute(k_pc_fixpoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PC_TREE_SMEM));
+  PIR_CK(cudaFuncSetAttribute(k_pc_fixpoint, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int occ = 0;
-  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pc_fixpoint, PC_BLOCK, 0));
+  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pc_fixpoint, PC_BLOCK, PC_TREE_SMEM));
   if (occ < 1) return set_err(ctx, PIR_ECUDA, "PC kernel does not fit on an SM");
   const int per_sm = opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ;
   const int grid = (int)std::max(1ll, std::min((long long)ctx->num_sms * per_sm, (n + PC_BLOCK - 1) / PC_BLOCK));
@@ -902,11 +1280,12 @@ int pc_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
   PIR_CK(cudaMemcpyAsync(s->d_next, ctx->d_store, (size_t)ctx->nvars * sizeof(int2), cudaMemcpyDeviceToDevice,
                          ctx->stream));
   const int4 *tape = s->d_tape;
-  const int *roots = s->d_roots;
+  const int *roots = s->d_roots, *bases = s->d_bases;
   int nprops = (int)n, nvars = ctx->nvars;
-  void *args[] = {(void *)&tape, (void *)&roots, &nprops, &ctx->d_store, &s->d_next, &nvars, &ctx->d_ctl,
-                  (void *)&max_rounds, (void *)&timeout};
-  PIR_CK(cudaLaunchCooperativeKernel((const void *)k_pc_fixpoint, dim3(grid), dim3(PC_BLOCK), args, 0, ctx->stream));
+  void *args[] = {(void *)&tape, (void *)&roots, (void *)&bases, &nprops, &ctx->d_store, &s->d_next, &nvars,
+                  &ctx->d_ctl, (void *)&max_rounds, (void *)&timeout};
+  PIR_CK(cudaLaunchCooperativeKernel((const void *)k_pc_fixpoint, dim3(grid), dim3(PC_BLOCK), args, PC_TREE_SMEM,
+                                     ctx->stream));
   PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   Control h;
   if ((r = read_control(ctx, &h))) return r;

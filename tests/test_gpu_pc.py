@@ -216,3 +216,26 @@ def test_round_cap_and_failure(gpu_ctx_factory):
     rc, st = ctx.pc_fixpoint()
     assert rc == pirgpu.FAILED and ctx.is_bot()
     assert ctx.pc_fixpoint()[0] == pirgpu.FAILED
+
+
+def test_tree_and_shared_node_paths(gpu_ctx_factory, oracle):
+    """Propagators whose formula reuses a node (x + x, a shared sub-sum) or
+    has more than 24 nodes take the recursive path, small trees the two-pass
+    one; all of them in one launch, against the oracle."""
+    rng = np.random.default_rng(5)
+    t = P.Tape()
+    nv = 40
+    store = np.stack([rng.integers(-30, 0, nv), rng.integers(0, 40, nv)], 1).astype(np.int32)
+    for k in range(30):
+        x, y = t.var(k % nv), t.var((k * 7 + 3) % nv)
+        if k % 3 == 0:
+            s = t.add(x, x)                                   # a node with two parents
+            t.prop(t.leq(s, t.var((k + 1) % nv)))
+        elif k % 3 == 1:
+            terms = [t.mul(t.constant(1 + i % 3), t.var((k + i) % nv)) for i in range(9)]
+            t.prop(t.leq(t.nadd(terms), t.constant(int(rng.integers(0, 60)))))   # 30 nodes
+        else:
+            t.prop(t.disj(t.leq(t.add(x, t.constant(2)), y), t.leq(t.add(y, t.constant(3)), x)))
+    tape, roots = t.arrays()
+    ctx = _ctx(gpu_ctx_factory, tape, roots, store)
+    _gpu_vs_oracle(ctx, oracle, tape, store)
