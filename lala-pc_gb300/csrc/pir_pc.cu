@@ -665,28 +665,30 @@ __device__ __forceinline__ int pack_node(int4 d, int base) {
   return k | (d.y - base) << 8 | (d.z - base) << 16;
 }
 
+constexpr int STAGE = 8;  // loads in flight while a tree is staged
+
 static __device__ __noinline__ void tree_deduce(PcEval *e, int root, int base, TreeScratch sc) {
   const int4 *tape = e->tape;
   const int n = root - base + 1;
-  // stage the nodes, four independent loads in flight at a time
-  for (int j = 0; j < n; j += 4) {
-    int4 t[4];
+  // stage the nodes, STAGE independent loads in flight at a time
+  for (int j = 0; j < n; j += STAGE) {
+    int4 t[STAGE];
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < STAGE; ++k)
       if (j + k < n) t[k] = __ldg(tape + base + j + k);
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < STAGE; ++k)
       if (j + k < n) {
         sc.node[(j + k) * PC_BLOCK] = make_int2(pack_node(t[k], base), t[k].y);
         if (t[k].x == K_CONST) sc.set(j + k, mk(t[k].y, t[k].z));
       }
   }
   // then the intervals of the variable leaves
-  for (int j = 0; j < n; j += 4) {
-    int2 v[4];
-    bool is_var[4];
+  for (int j = 0; j < n; j += STAGE) {
+    int2 v[STAGE];
+    bool is_var[STAGE];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < STAGE; ++k) {
       is_var[k] = false;
       if (j + k < n) {
         const int2 w = sc.node[(j + k) * PC_BLOCK];
@@ -696,7 +698,7 @@ static __device__ __noinline__ void tree_deduce(PcEval *e, int root, int base, T
       }
     }
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < STAGE; ++k)
       if (is_var[k]) sc.val[(j + k) * PC_BLOCK] = v[k];
   }
   // pass 1: projections and entailments, children first

@@ -219,9 +219,17 @@ def random_formulas(rng, nvars, nprops, depth=3, kinds="all", positive_mul=True)
         if r < 0.78:
             return t.neg(term(d - 1))
         if r < 0.86:
+            if kinds == "planted":
+                return t.add(term(d - 1), term(d - 1))
             op = [P.TDIV, P.FDIV, P.CDIV, P.EDIV][int(rng.integers(0, 4))]
+            if kinds == "all" and rng.random() < 0.3:  # a divisor that is itself a term
+                return t.binary(op, term(d - 1), term(d - 1))
             return t.binary(op, term(d - 1), t.constant(int(rng.integers(1, 6))))
         if r < 0.94:
+            if kinds == "all" and rng.random() < 0.2:
+                return t.nmul([term(d - 1) for _ in range(int(rng.integers(2, 4)))])
+            if kinds == "all" and rng.random() < 0.2:
+                return t.mul(term(d - 1), term(d - 1))
             return t.nadd([term(d - 1) for _ in range(int(rng.integers(2, 5)))])
         return t.formula(atom(d - 1))
 
@@ -244,7 +252,7 @@ def random_formulas(rng, nvars, nprops, depth=3, kinds="all", positive_mul=True)
                 return t.pvar(bv) if rng.random() < 0.5 else t.nvar(bv)
             return atom(max(d, 1))
         f, g = formula(d - 1), formula(d - 1)
-        k = [P.AND, P.OR, P.EQUIV, P.IMPLY, P.XOR][int(rng.integers(0, 5))]
+        k = [P.AND, P.OR, P.EQUIV, P.IMPLY, P.XOR][int(rng.integers(0, 4 if kinds == "planted" else 5))]
         return t._add(k, f, g)
 
     for _ in range(nprops):
@@ -259,3 +267,83 @@ def random_formulas(rng, nvars, nprops, depth=3, kinds="all", positive_mul=True)
         else:
             t.prop(formula(depth))
     return t, store
+
+
+# ----------------------------------------------------------------- planted --
+def _eval(tape, n, s):
+    """Value of node n under the assignment s: an int for a term, a bool for a
+    formula, None where a division by zero leaves it undefined."""
+    import pc as P
+    k, a, b, _ = (int(x) for x in tape[n])
+    if k == P.VAR:
+        return int(s[a])
+    if k == P.CONST:
+        return a
+    if k == P.PVAR:
+        return s[a] != 0
+    if k == P.NVAR:
+        return s[a] == 0
+    if k in (P.TRUE, P.FALSE):
+        return k == P.TRUE
+    if k in (P.NADD, P.NMUL):
+        vals = [_eval(tape, int(tape[a + i][1]), s) for i in range(b)]
+        if any(v is None for v in vals):
+            return None
+        out = 0 if k == P.NADD else 1
+        for v in vals:
+            out = out + v if k == P.NADD else out * v
+        return out
+    x = _eval(tape, a, s)
+    if x is None:
+        return None
+    if k == P.FORMULA:
+        return int(bool(x))
+    if k == P.NEG:
+        return -x
+    if k == P.ABS:
+        return abs(x)
+    y = _eval(tape, b, s)
+    if y is None:
+        return None
+    if k == P.ADD: return x + y
+    if k == P.SUB: return x - y
+    if k == P.MUL: return x * y
+    if k == P.MIN: return min(x, y)
+    if k == P.MAX: return max(x, y)
+    if k == P.LEQ: return x <= y
+    if k == P.GT: return x > y
+    if k == P.EQ: return x == y
+    if k == P.NEQ: return x != y
+    if k == P.AND: return x and y
+    if k == P.OR: return x or y
+    if k == P.EQUIV: return x == y
+    if k == P.IMPLY: return (not x) or y
+    raise ValueError(k)
+
+
+def planted_formulas(rng, nvars, nprops, depth=3):
+    """Random formulas that a hidden assignment s (inside the initial domains)
+    satisfies: each candidate is kept only if it holds under s.  Sound
+    propagation keeps s inside every domain, so the fixpoint is not empty.
+    Leaves out the two constructs whose reference propagation is not sound:
+    xor (ExclusiveDisjunction::nask as written, formula.hpp:552-556, reports
+    an entailed xor as disentailed) and division (GroupDiv::left_residual,
+    terms.hpp:272-277, bounds the dividend by u * z joined with z.ub - 1).
+    Returns (pc.Tape, store, s)."""
+    import pc as P
+    t0, store = random_formulas(rng, nvars, 0, depth=depth)
+    s = rng.integers(store[:, 0], store[:, 1] + 1)
+    t = P.Tape()
+    kept = tries = 0
+    while kept < nprops and tries < 50 * nprops:
+        tries += 1
+        sub, _ = random_formulas(rng, nvars, 1, depth=depth, kinds="planted")
+        tape, roots = sub.arrays()
+        if _eval(tape, int(roots[0]), s) is not True:
+            continue
+        off = len(t.nodes)
+        for row in offset_tape(tape, off):
+            t.nodes.append(tuple(int(v) for v in row))
+        t.roots.append(int(roots[0]) + off)
+        kept += 1
+    return t, store, s

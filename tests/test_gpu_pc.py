@@ -54,17 +54,40 @@ def test_random_parity_small(seed, gpu_ctx_factory, oracle):
     _gpu_vs_oracle(_ctx(gpu_ctx_factory, tape, roots, store), oracle, tape, store)
 
 
-@pytest.mark.parametrize("nvars,nprops,depth", [(2000, 1500, 3), (20000, 12000, 4), (100000, 30000, 3)])
+@pytest.mark.parametrize("nvars,nprops,depth", [(2000, 1500, 3), (20000, 12000, 4)])
 def test_random_parity_large(nvars, nprops, depth, gpu_ctx_factory, oracle):
-    """Larger sets: many CTAs, many rounds; OK and FAILED outcomes both occur
-    across the seeds."""
-    statuses = set()
-    for seed in range(3):
+    """Larger unconstrained sets (these end FAILED: the status is compared)."""
+    for seed in range(2):
         rng = np.random.default_rng(100 + seed)
         t, store = H.random_formulas(rng, nvars, nprops, depth=depth)
         tape, roots = t.arrays()
-        statuses.add(_gpu_vs_oracle(_ctx(gpu_ctx_factory, tape, roots, store), oracle, tape, store))
-    assert statuses <= {pirgpu.OK, pirgpu.FAILED}
+        _gpu_vs_oracle(_ctx(gpu_ctx_factory, tape, roots, store), oracle, tape, store)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_planted_parity(seed, gpu_ctx_factory, oracle):
+    """Random formulas a hidden assignment satisfies: the fixpoint is not
+    empty, equal bit for bit to the oracle's, and the assignment stays inside."""
+    rng = np.random.default_rng(300 + seed)
+    t, store, hidden = H.planted_formulas(rng, 2000, 1500, depth=3)
+    tape, roots = t.arrays()
+    ctx = _ctx(gpu_ctx_factory, tape, roots, store)
+    assert _gpu_vs_oracle(ctx, oracle, tape, store) == pirgpu.OK
+    lb, ub = ctx.read_store()
+    assert np.all((hidden >= lb) & (hidden <= ub))
+
+
+@pytest.mark.parametrize("n", [50_000, 200_000])
+def test_benchmark_mix_parity(n, gpu_ctx_factory, oracle):
+    """The benchmark's formula mix (workloads.pc_mix) at 50k and 200k trees:
+    bit-exact with the oracle, planted solution inside the fixpoint."""
+    import workloads as W
+    tape, roots, lb0, ub0, hidden = W.pc_mix(n, n, seed=2)
+    store = np.ascontiguousarray(np.stack([lb0, ub0], 1))
+    ctx = _ctx(gpu_ctx_factory, tape, roots, store)
+    assert _gpu_vs_oracle(ctx, oracle, tape, store) == pirgpu.OK
+    lb, ub = ctx.read_store()
+    assert np.all((hidden >= lb) & (hidden <= ub))
 
 
 def test_monotone_sets_match_gauss_seidel(gpu_ctx_factory, oracle):

@@ -152,3 +152,18 @@ def test_validate_rejects(oracle):
     bad[2, 1] = 2                                               # child not before parent
     assert oracle.pc_validate(bad, roots, 1) == -3
     assert oracle.pc_validate(tape, np.array([0], np.int32), 1) == -1 - len(tape)  # root is a term
+
+
+def test_planted_formulas_keep_their_solution(oracle):
+    """Soundness on whole sets: formulas that a hidden assignment satisfies
+    never lose it (Gauss-Seidel and Jacobi agree)."""
+    for seed in range(6):
+        rng = np.random.default_rng(400 + seed)
+        t, store, hidden = H.planted_formulas(rng, 300, 200, depth=3)
+        tape, roots = t.arrays()
+        order = oracle.pc_order(tape, roots)
+        a, b = store.copy(), store.copy()
+        assert oracle.pc_fixpoint(tape, order, a)[0] == oracle.OK
+        assert oracle.pc_fixpoint_jacobi(tape, order, b)[0] == oracle.OK
+        np.testing.assert_array_equal(a, b)
+        assert np.all((hidden >= a[:, 0]) & (hidden <= a[:, 1]))
