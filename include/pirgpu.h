@@ -384,7 +384,9 @@ int pc_get_tape(pirgpu_ctx *ctx, int32_t *kind, int32_t *a, int32_t *b, int32_t 
  * (PC propagators need not be monotone, formula.hpp:497-503, and then even the
  * reference's Gauss-Seidel result depends on the propagator order; for
  * monotone ones every order reaches this fixpoint).  opts: max_rounds,
- * barrier_timeout_ns, ctas_per_sm; the other fields are ignored.
+ * barrier_timeout_ns, ctas_per_sm, and sched = PIR_SCHED_EVENTS to run in a
+ * round only the formulas whose variables the previous round narrowed (the
+ * same rounds and result, fewer executions); the other fields are ignored.
  * stats->executions counts propagator executions. */
 int pc_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts, pir_stats *stats);
 /* deduce(int i) (pc.hpp:671-681): one propagator, engine order.  *changed is

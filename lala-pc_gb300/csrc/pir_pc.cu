@@ -62,6 +62,13 @@ struct PcState {
   std::vector<unsigned> stamp;    // scratch of the tree check
   unsigned stamp_gen = 0;
   size_t stack_bytes = 0;         // per-thread stack limit this context asked for
+  // event schedule: variable -> formulas (engine indices), rebuilt after a
+  // tell or a restore changed the propagators
+  bool csr_valid = false;
+  int csr_nvars = -1;             // store size the adjacency was built for
+  int *d_adj_ptr = nullptr, *d_adj = nullptr, *d_list = nullptr;
+  unsigned *d_pstamp = nullptr, *d_cnt = nullptr;
+  size_t cap_adj_ptr = 0, cap_adj = 0, cap_list = 0, cap_pstamp = 0, cap_cnt = 0;
 };
 
 namespace {
@@ -884,9 +891,67 @@ static __device__ __noinline__ void tree_deduce(PcEval *e, int root, int base, T
 // the round starts); the round's changed / failed bits meet at the first
 // grid barrier; then B is copied into A (two variables per 16-byte access),
 // empty variables are counted, and the second barrier ends the round.
+// Event schedule of the Jacobi rounds: a round runs only the formulas whose
+// variables the previous round narrowed.  A formula's deduction is a pure
+// function of its variables' intervals, so one whose variables did not change
+// since it last ran would produce the joins it produced then, which are
+// already in the store: the rounds, the stores and the result are those of
+// the full rounds.  adj_ptr / adj: variable -> formulas (engine indices,
+// CSR); stamp: per formula the last round it was listed for; list / cnt: the
+// frontier of the next round (two buffers); execs: executions counted.
+struct PcEvents {
+  const int *adj_ptr, *adj;
+  unsigned *stamp;
+  int *list0, *list1;
+  unsigned *cnt;  // cnt[2]
+};
+constexpr int PC_EXPAND = 8;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Lists the formulas of variable v for round `next` (each once: the stamp),
+// eight adjacency entries per step, one atomic per step and warp.
+__device__ __forceinline__ void pc_schedule(const PcEvents &ev, int v, unsigned next) {
+  int *list = (next & 1u) ? ev.list1 : ev.list0;
+  unsigned *cnt = ev.cnt + (next & 1u);
+  const int beg = __ldg(ev.adj_ptr + v), end = __ldg(ev.adj_ptr + v + 1);
+  for (int k0 = beg; k0 < end; k0 += PC_EXPAND) {
+    int q[PC_EXPAND];
+    unsigned take = 0;
+#pragma unroll
+    for (int j = 0; j < PC_EXPAND; ++j) {
+      q[j] = k0 + j < end ? __ldg(ev.adj + k0 + j) : -1;
+      if (q[j] >= 0 && atomicMax(ev.stamp + q[j], next) < next) take |= 1u << j;
+    }
+    const unsigned m = __activemask();
+    unsigned before = 0, total = 0, bal[PC_EXPAND];
+#pragma unroll
+    for (int j = 0; j < PC_EXPAND; ++j) {
+      bal[j] = __ballot_sync(m, (take >> j) & 1u);
+      total += __popc(bal[j]);
+    }
+    const int leader = __ffs(m) - 1, lane = threadIdx.x & 31;
+    unsigned slot = 0;
+    if (lane == leader && total) slot = atomicAdd(cnt, total);
+    slot = __shfl_sync(m, slot, leader);
+    const unsigned lt = lanemask_lt();
+#pragma unroll
+    for (int j = 0; j < PC_EXPAND; ++j) {
+      if ((take >> j) & 1u) list[slot + before + __popc(bal[j] & lt)] = q[j];
+      before += __popc(bal[j]);
+    }
+  }
+}
+
+template <bool EVENTS>
 __global__ void __launch_bounds__(PC_BLOCK) k_pc_fixpoint(const int4 *tape, const int *roots, const int *bases,
                                                          int nprops, int2 *a, int2 *b, int nvars, Control *ctl,
-                                                         long long max_rounds, long long timeout_ns) {
+                                                         long long max_rounds, long long timeout_ns,
+                                                         PcEvents ev) {
   __shared__ unsigned s_bits[2], s_word[2];
   extern __shared__ __align__(16) unsigned char pc_smem[];
   TreeScratch sc;
@@ -920,10 +985,18 @@ __global__ void __launch_bounds__(PC_BLOCK) k_pc_fixpoint(const int4 *tape, cons
     ++bar;
     return w;
   };
+  constexpr bool events = EVENTS;
+  unsigned long long execs = 0;
   for (;;) {
     int failed = 0;
     e.narrowed = 0;
-    for (int i = gtid; i < nprops; i += gstride) {
+    // this round's formulas: all of them, or the frontier the previous round listed
+    const int count = (!events || round == 0) ? nprops : (int)*(volatile unsigned *)(ev.cnt + (round & 1));
+    const int *frontier = (round & 1) ? ev.list1 : ev.list0;
+    if (events && blockIdx.x == 0 && threadIdx.x == 0) ev.cnt[(round + 1) & 1] = 0u;  // the next frontier
+    execs += count;
+    for (int k = gtid; k < count; k += gstride) {
+      const int i = (!events || round == 0) ? k : __ldcg(frontier + k);
       e.failed = 0;
       const int base = __ldg(bases + i);
       if (base >= 0) tree_deduce(&e, __ldg(roots + i), base, sc);
@@ -935,20 +1008,32 @@ __global__ void __launch_bounds__(PC_BLOCK) k_pc_fixpoint(const int4 *tape, cons
     ++round;
     bool stop = (w & BIT_ERROR) || (w & BIT_FAILED) || !(w & BIT_CHANGED);
     if (!stop) {
-      // A := B, two variables per 16-byte access, and a count of empty ones
+      // A := B and a count of empty variables; with events, only the changed
+      // variables are copied and their formulas listed for the next round
       int empty = 0;
-      const int npairs = nvars >> 1;
-      const int4 *src = reinterpret_cast<const int4 *>(b);
-      int4 *dst = reinterpret_cast<int4 *>(a);
-      for (int i = gtid; i < npairs; i += gstride) {
-        const int4 v = __ldcg(src + i);
-        dst[i] = v;
-        empty |= is_bot(mk(v.x, v.y)) | is_bot(mk(v.z, v.w));
-      }
-      if ((nvars & 1) && gtid == 0) {
-        const int2 v = __ldcg(b + nvars - 1);
-        a[nvars - 1] = v;
-        empty |= is_bot(mk(v.x, v.y));
+      if (events) {
+        for (int v = gtid; v < nvars; v += gstride) {
+          const int2 x = __ldcg(a + v), y = __ldcg(b + v);
+          if (x.x != y.x || x.y != y.y) {
+            a[v] = y;
+            empty |= is_bot(mk(y.x, y.y));
+            pc_schedule(ev, v, (unsigned)round);
+          }
+        }
+      } else {
+        const int npairs = nvars >> 1;
+        const int4 *src = reinterpret_cast<const int4 *>(b);
+        int4 *dst = reinterpret_cast<int4 *>(a);
+        for (int i = gtid; i < npairs; i += gstride) {
+          const int4 v = __ldcg(src + i);
+          dst[i] = v;
+          empty |= is_bot(mk(v.x, v.y)) | is_bot(mk(v.z, v.w));
+        }
+        if ((nvars & 1) && gtid == 0) {
+          const int2 v = __ldcg(b + nvars - 1);
+          a[nvars - 1] = v;
+          empty |= is_bot(mk(v.x, v.y));
+        }
       }
       const unsigned w2 = sync(empty ? 2u : 0u);
       if ((w2 & BIT_ERROR) || (w2 & BIT_FAILED)) {
@@ -961,6 +1046,7 @@ __global__ void __launch_bounds__(PC_BLOCK) k_pc_fixpoint(const int4 *tape, cons
     if (stop) {
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         ctl->rounds = round;
+        ctl->executions = execs;
         if (w & BIT_FAILED) ctl->failed = 1;
         if ((w & BIT_CHANGED) && !(w & (BIT_FAILED | BIT_ERROR))) ctl->changed[0] = 1;
       }
@@ -1070,8 +1156,60 @@ int tree_base_of(PcState *s, int root) {
   return lo == root - count + 1 ? lo : -1;
 }
 
+// The variable -> formula adjacency of the event schedule (CSR over the
+// engine order): the distinct variable leaves of every formula.
+int pc_build_csr(pirgpu_ctx *ctx, PcState *s) {
+  const int nv = ctx->nvars, np = (int)s->roots.size();
+  std::vector<int> deg((size_t)nv + 1, 0), seen((size_t)nv, -1), vars, todo;
+  std::vector<int> start((size_t)np + 1, 0);
+  vars.reserve((size_t)np * 6);
+  for (int i = 0; i < np; ++i) {
+    start[(size_t)i] = (int)vars.size();
+    todo.assign(1, s->roots[(size_t)i]);
+    while (!todo.empty()) {
+      const int n = todo.back();
+      todo.pop_back();
+      const int4 d = s->tape[(size_t)n];
+      const int k = d.x;
+      if (k == K_VAR || k == K_PVAR || k == K_NVAR) {
+        if (seen[(size_t)d.y] != i) {
+          seen[(size_t)d.y] = i;
+          vars.push_back(d.y);
+        }
+      } else if (k == K_FORMULA || k == K_NEG || k == K_ABS || k == K_ARG) {
+        todo.push_back(d.y);
+      } else if (k == K_NADD || k == K_NMUL) {
+        for (int j = 0; j < d.z; ++j) todo.push_back(d.y + j);
+      } else if ((k >= K_ADD && k <= K_MAX) || (k >= K_LEQ && k <= K_XOR)) {
+        todo.push_back(d.y);
+        todo.push_back(d.z);
+      }
+    }
+  }
+  start[(size_t)np] = (int)vars.size();
+  for (int v : vars) ++deg[(size_t)v + 1];
+  for (int v = 0; v < nv; ++v) deg[(size_t)v + 1] += deg[(size_t)v];
+  std::vector<int> adj(vars.size()), fill(deg.begin(), deg.end() - 1);
+  for (int i = 0; i < np; ++i)
+    for (int q = start[(size_t)i]; q < start[(size_t)i + 1]; ++q) adj[(size_t)fill[(size_t)vars[(size_t)q]]++] = i;
+  int r;
+  if ((r = ensure(ctx, (void **)&s->d_adj_ptr, &s->cap_adj_ptr, deg.size() * sizeof(int)))) return r;
+  if ((r = ensure(ctx, (void **)&s->d_adj, &s->cap_adj, std::max<size_t>(adj.size(), 1) * sizeof(int)))) return r;
+  if ((r = ensure(ctx, (void **)&s->d_list, &s->cap_list, (size_t)2 * np * sizeof(int)))) return r;
+  if ((r = ensure(ctx, (void **)&s->d_pstamp, &s->cap_pstamp, (size_t)np * sizeof(unsigned)))) return r;
+  if ((r = ensure(ctx, (void **)&s->d_cnt, &s->cap_cnt, 2 * sizeof(unsigned)))) return r;
+  PIR_CK(cudaMemcpyAsync(s->d_adj_ptr, deg.data(), deg.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  if (!adj.empty())
+    PIR_CK(cudaMemcpyAsync(s->d_adj, adj.data(), adj.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  PIR_CK(cudaStreamSynchronize(ctx->stream));
+  s->csr_valid = true;
+  s->csr_nvars = nv;
+  return PIR_OK;
+}
+
 int pc_upload(pirgpu_ctx *ctx, PcState *s) {
   int r;
+  s->csr_valid = false;
   if (!s->tape.empty()) {
     if ((r = ensure(ctx, (void **)&s->d_tape, &s->cap_tape, s->tape.size() * sizeof(int4)))) return r;
     PIR_CK(cudaMemcpyAsync(s->d_tape, s->tape.data(), s->tape.size() * sizeof(int4), cudaMemcpyHostToDevice,
@@ -1099,6 +1237,9 @@ void destroy_pc_state(pirgpu_ctx *ctx) {
   if (ctx->pc->d_roots) cudaFree(ctx->pc->d_roots);
   if (ctx->pc->d_next) cudaFree(ctx->pc->d_next);
   if (ctx->pc->d_bases) cudaFree(ctx->pc->d_bases);
+  for (void *q : {(void *)ctx->pc->d_adj_ptr, (void *)ctx->pc->d_adj, (void *)ctx->pc->d_list,
+                  (void *)ctx->pc->d_pstamp, (void *)ctx->pc->d_cnt})
+    if (q) cudaFree(q);
   delete ctx->pc;
   ctx->pc = nullptr;
 }
@@ -1268,11 +1409,13 @@ int pc_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
   if ((r = pc_prepare_stack(ctx, s))) return r;
   const long long max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
   const long long timeout = opts.barrier_timeout_ns > 0 ? opts.barrier_timeout_ns : 2000000000ll;
+  const bool events = opts.sched == PIR_SCHED_EVENTS;
+  const void *kfn = events ? (const void *)k_pc_fixpoint<true> : (const void *)k_pc_fixpoint<false>;
   // shared memory: the per-thread scratch of the trees' two passes
-  PIR_CK(cudaFuncSetAttribute(k_pc_fixpoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PC_TREE_SMEM));
-  PIR_CK(cudaFuncSetAttribute(k_pc_fixpoint, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  PIR_CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PC_TREE_SMEM));
+  PIR_CK(cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int occ = 0;
-  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pc_fixpoint, PC_BLOCK, PC_TREE_SMEM));
+  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, PC_BLOCK, PC_TREE_SMEM));
   if (occ < 1) return set_err(ctx, PIR_ECUDA, "PC kernel does not fit on an SM");
   const int per_sm = opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ;
   const int grid = (int)std::max(1ll, std::min((long long)ctx->num_sms * per_sm, (n + PC_BLOCK - 1) / PC_BLOCK));
@@ -1281,19 +1424,31 @@ int pc_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
   PIR_CK(cudaEventRecord(ctx->ev0, ctx->stream));
   PIR_CK(cudaMemcpyAsync(s->d_next, ctx->d_store, (size_t)ctx->nvars * sizeof(int2), cudaMemcpyDeviceToDevice,
                          ctx->stream));
+  PcEvents ev;
+  std::memset(&ev, 0, sizeof(ev));
+  if (events) {
+    if ((!s->csr_valid || s->csr_nvars != ctx->nvars) && (r = pc_build_csr(ctx, s))) return r;
+    PIR_CK(cudaMemsetAsync(s->d_pstamp, 0, (size_t)n * sizeof(unsigned), ctx->stream));
+    PIR_CK(cudaMemsetAsync(s->d_cnt, 0, 2 * sizeof(unsigned), ctx->stream));
+    ev.adj_ptr = s->d_adj_ptr;
+    ev.adj = s->d_adj;
+    ev.stamp = s->d_pstamp;
+    ev.list0 = s->d_list;
+    ev.list1 = s->d_list + n;
+    ev.cnt = s->d_cnt;
+  }
   const int4 *tape = s->d_tape;
   const int *roots = s->d_roots, *bases = s->d_bases;
   int nprops = (int)n, nvars = ctx->nvars;
   void *args[] = {(void *)&tape, (void *)&roots, (void *)&bases, &nprops, &ctx->d_store, &s->d_next, &nvars,
-                  &ctx->d_ctl, (void *)&max_rounds, (void *)&timeout};
-  PIR_CK(cudaLaunchCooperativeKernel((const void *)k_pc_fixpoint, dim3(grid), dim3(PC_BLOCK), args, PC_TREE_SMEM,
-                                     ctx->stream));
+                  &ctx->d_ctl, (void *)&max_rounds, (void *)&timeout, (void *)&ev};
+  PIR_CK(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(PC_BLOCK), args, PC_TREE_SMEM, ctx->stream));
   PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   Control h;
   if ((r = read_control(ctx, &h))) return r;
   PIR_CK(cudaEventElapsedTime(&st.device_ms, ctx->ev0, ctx->ev1));
   st.rounds = h.rounds;
-  st.executions = h.rounds * n;
+  st.executions = events ? (int64_t)h.executions : h.rounds * n;
   st.narrowed = (int64_t)h.narrowed;
   int status;
   if (h.status) status = h.status;
