@@ -307,3 +307,37 @@ def test_event_schedule_matches_full_rounds(kind, gpu_ctx_factory, oracle):
     ctx.load_store(np.append(lb, -5), np.append(ub, 5))
     ctx.pc_tell(*t2.arrays())
     _events_vs_full(ctx, ctx.snapshot())
+
+
+def test_error_paths_and_edge_cases(gpu_ctx_factory):
+    ctx = gpu_ctx_factory()
+    ctx.load_store(np.array([0, 0]), np.array([3, 3]))
+    # no PC propagators: the fixpoint is trivially OK, the lists empty
+    assert ctx.pc_fixpoint()[0] == pirgpu.OK
+    assert ctx.pc_num_deductions() == 0 and len(ctx.pc_roots()) == 0
+    assert ctx.pc_is_extractable()
+    t = P.Tape()
+    t.prop(t.leq(t.var(0), t.var(1)))
+    ctx.pc_tell(*t.arrays())
+    for bad in (-1, 1, 7):
+        with pytest.raises(pirgpu.PirError, match="out of range"):
+            ctx.pc_deduce_one(bad)
+        with pytest.raises(pirgpu.PirError, match="out of range"):
+            ctx.pc_ask(bad)
+    assert ctx.pc_ask(0) is False      # x <= y over [0, 3] x [0, 3]: not entailed (3 > 0)
+    # a store that is empty from the start: every call reports the failure
+    ctx.load_store(np.array([2, 0]), np.array([1, 3]))
+    assert ctx.is_bot()
+    assert ctx.pc_fixpoint()[0] == pirgpu.FAILED
+    assert ctx.pc_fixpoint(sched=pirgpu.SCHED_EVENTS)[0] == pirgpu.FAILED
+    assert not ctx.pc_is_extractable()
+    # True / False formulas: False empties the store, True is entailed
+    ctx.load_store(np.array([0, 0]), np.array([3, 3]))
+    t2 = P.Tape()
+    t2.prop(t2.true())
+    ctx.pc_tell(*t2.arrays())
+    assert ctx.pc_fixpoint()[0] == pirgpu.OK
+    t3 = P.Tape()
+    t3.prop(t3.false())
+    ctx.pc_tell(*t3.arrays())
+    assert ctx.pc_fixpoint()[0] == pirgpu.FAILED and ctx.is_bot()
