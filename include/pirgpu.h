@@ -355,7 +355,14 @@ enum pc_kind {
   PC_IMPLY = 27,   /*                                         Implication :454-516 */
   PC_XOR = 28,     /*                                         ExclusiveDisjunction :519-587 */
   PC_ARG = 29,     /* operand slot of PC_NADD / PC_NMUL: a = term */
-  PC_NUM_KINDS = 30
+  PC_AE = 30,      /* a formula of the store itself (AbstractElement :14-78): its items are nodes
+                      a .. a+b-1; ask = every PC_ASK / PC_ASK_OUT item entailed, nask = every
+                      PC_NASK / PC_NASK_OUT item, deduce = meet every PC_TELL item,
+                      contradeduce = every PC_NTELL item */
+  PC_TELL = 31, PC_NTELL = 32,   /* items {kind, var, lb, ub} (c is ub): meet [lb, ub] into var */
+  PC_ASK = 33, PC_NASK = 34,     /* entailed when var's interval is inside [lb, ub] */
+  PC_ASK_OUT = 35, PC_NASK_OUT = 36, /* entailed when var's interval misses [lb, ub] (an ask of var != c) */
+  PC_NUM_KINDS = 37
 };
 /* Deepest formula tree accepted (nodes on a root-to-leaf path): bounds the
  * device call stack of the recursive evaluator. */
@@ -364,7 +371,7 @@ enum pc_kind {
 /* PC::deduce(tell) (pc.hpp:625-648): appends nnodes tape nodes (indices in
  * this call's arrays are local to it) and nprops propagators, then stably
  * sorts all propagators by (formula kind, tree length) as the reference does.
- * c[] is reserved and must be 0.  Checks every node (kinds, child order and
+ * c[] is the upper bound of an item node and must be 0 elsewhere.  Checks every node (kinds, child order and
  * kinds, variable range, depth <= PC_MAX_DEPTH) first: PIR_EINVAL changes
  * nothing. */
 int pc_tell(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *kind, const int32_t *a, const int32_t *b,

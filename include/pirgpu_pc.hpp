@@ -40,7 +40,7 @@ namespace pc {
 // data (variable, constant bounds) and its children.
 struct Node {
   int32_t kind = PC_TRUE;
-  int32_t a = 0, b = 0;
+  int32_t a = 0, b = 0, c = 0;
   std::vector<std::shared_ptr<const Node>> kids;
 };
 using NodePtr = std::shared_ptr<const Node>;
@@ -110,6 +110,29 @@ class Formula {
   static Formula make_bicond(const Formula &f, const Formula &g) { return con(PC_EQUIV, f, g); }
   static Formula make_imply(const Formula &f, const Formula &g) { return con(PC_IMPLY, f, g); }
   static Formula make_xor(const Formula &f, const Formula &g) { return con(PC_XOR, f, g); }
+  // AbstractElement (formula.hpp:14-78): a formula of the store itself, as
+  // the store's tell / ask items (variable, interval) of the formula and of
+  // its negation
+  // (asks of "var != c" miss an interval: the _out lists)
+  using items = std::vector<std::pair<int32_t, Itv>>;
+  static Formula make_abstract_element(const items &tellv, const items &not_tellv, const items &askv,
+                                       const items &not_askv, const items &ask_outv = {},
+                                       const items &not_ask_outv = {}) {
+    std::vector<NodePtr> kids;
+    const std::pair<int32_t, const items *> lists[6] = {
+        {PC_TELL, &tellv},        {PC_NTELL, &not_tellv},   {PC_ASK, &askv},
+        {PC_NASK, &not_askv},     {PC_ASK_OUT, &ask_outv}, {PC_NASK_OUT, &not_ask_outv}};
+    for (const auto &l : lists)
+      for (const auto &it : *l.second) {
+        auto n = std::make_shared<Node>();
+        n->kind = l.first;
+        n->a = it.first;
+        n->b = it.second.lb;
+        n->c = it.second.ub;
+        kids.push_back(n);
+      }
+    return Formula(make_node(PC_AE, std::move(kids)));
+  }
 
   int32_t kind() const { return n_ ? n_->kind : -1; }
   const NodePtr &node() const { return n_; }
@@ -153,6 +176,12 @@ class TapeWriter {
         id = push(n->kind, first, (int32_t)ops.size());
         break;
       }
+      case PC_AE: {
+        const int32_t first = (int32_t)kind.size();
+        for (const NodePtr &k : n->kids) push(k->kind, k->a, k->b, k->c);
+        id = push(PC_AE, first, (int32_t)n->kids.size());
+        break;
+      }
       default: {
         const int32_t x = emit(n->kids.at(0));
         const int32_t y = emit(n->kids.at(1));
@@ -166,11 +195,11 @@ class TapeWriter {
 
  private:
   std::unordered_map<const Node *, int32_t> seen_;
-  int32_t push(int32_t k, int32_t x, int32_t y) {
+  int32_t push(int32_t k, int32_t x, int32_t y, int32_t z = 0) {
     kind.push_back(k);
     a.push_back(x);
     b.push_back(y);
-    c.push_back(0);
+    c.push_back(z);
     return (int32_t)kind.size() - 1;
   }
 };
@@ -377,7 +406,8 @@ class PC {
     while (!stack.empty()) {
       const pc::Node *n = stack.back();
       stack.pop_back();
-      if ((n->kind == PC_VAR || n->kind == PC_PVAR || n->kind == PC_NVAR) && (n->a < 0 || n->a >= vars())) {
+      if ((n->kind == PC_VAR || n->kind == PC_PVAR || n->kind == PC_NVAR || (n->kind >= PC_TELL && n->kind <= PC_NASK_OUT)) &&
+          (n->a < 0 || n->a >= vars())) {
         diagnostics.errors.push_back("Could not interpret the variables in the environment.");
         return false;
       }

@@ -78,7 +78,9 @@ constexpr int K_VAR = PC_VAR, K_CONST = PC_CONST, K_FORMULA = PC_FORMULA, K_NEG 
               K_CDIV = PC_CDIV, K_EDIV = PC_EDIV, K_MIN = PC_MIN, K_MAX = PC_MAX, K_NADD = PC_NADD,
               K_NMUL = PC_NMUL, K_PVAR = PC_PVAR, K_NVAR = PC_NVAR, K_TRUE = PC_TRUE, K_FALSE = PC_FALSE,
               K_LEQ = PC_LEQ, K_GT = PC_GT, K_EQ = PC_EQ, K_NEQ = PC_NEQ, K_AND = PC_AND, K_OR = PC_OR,
-              K_EQUIV = PC_EQUIV, K_IMPLY = PC_IMPLY, K_XOR = PC_XOR, K_ARG = PC_ARG;
+              K_EQUIV = PC_EQUIV, K_IMPLY = PC_IMPLY, K_XOR = PC_XOR, K_ARG = PC_ARG, K_AE = PC_AE,
+              K_TELL = PC_TELL, K_NTELL = PC_NTELL, K_ASK = PC_ASK, K_NASK = PC_NASK,
+              K_ASK_OUT = PC_ASK_OUT, K_NASK_OUT = PC_NASK_OUT;
 
 // ------------------------------------------------------ interval algebra --
 __device__ __forceinline__ Itv itop() { return mk(MINF, INF); }
@@ -472,12 +474,39 @@ static __device__ __noinline__ bool cmp_deduce(PcEval *e, int kind, int L, int R
   }
 }
 
+// AbstractElement (formula.hpp:14-78): a formula of the store itself.  Its
+// ask is the store's (every item's variable inside the item's interval), its
+// deduce the store's tell (meet every item); nask / contradeduce use the
+// negation's items.
+// item: K_ASK or K_NASK; the _OUT items of the same list ask that the
+// variable misses the interval (an ask of var != c)
+static __device__ __noinline__ bool ae_ask(PcEval *e, int4 d, int item) {
+  const int out = item + 2;
+  for (int i = d.y; i < d.y + d.z; ++i) {
+    const int4 t = node(e, i);
+    if (t.x != item && t.x != out) continue;
+    const Itv x = load(e, t.y);
+    if (is_bot(x)) continue;
+    if (t.x == item ? !(x.l >= t.z && x.u <= t.w) : !is_bot(imeet(x, mk(t.z, t.w)))) return false;
+  }
+  return true;
+}
+static __device__ __noinline__ bool ae_tell(PcEval *e, int4 d, int item) {
+  bool ch = false;
+  for (int i = d.y; i < d.y + d.z; ++i) {
+    const int4 t = node(e, i);
+    if (t.x == item) ch |= store_embed(e, t.y, mk(t.z, t.w));
+  }
+  return ch;
+}
+
 // ask / nask / deduce / contradeduce of every Formula alternative:
 // VariableLiteral :101-160, False :184-195, True :220-230, Conjunction
 // :268-288, Disjunction :338-358, Biconditional :408-438, Implication
 // :482-503, ExclusiveDisjunction :546-574
 __device__ __noinline__ bool f_ask_rec(PcEval *e, int4 d) {
   switch (d.x) {
+    case K_AE: return ae_ask(e, d, K_ASK);
     case K_PVAR: return !has0(load(e, d.y));
     case K_NVAR: return below_point(load(e, d.y), 0);
     case K_TRUE: return true;
@@ -492,6 +521,7 @@ __device__ __noinline__ bool f_ask_rec(PcEval *e, int4 d) {
 }
 __device__ __noinline__ bool f_nask_rec(PcEval *e, int4 d) {
   switch (d.x) {
+    case K_AE: return ae_ask(e, d, K_NASK);
     case K_PVAR: return below_point(load(e, d.y), 0);
     case K_NVAR: return !has0(load(e, d.y));
     case K_TRUE: return e->failed != 0;
@@ -507,6 +537,7 @@ __device__ __noinline__ bool f_nask_rec(PcEval *e, int4 d) {
 __device__ __noinline__ bool f_deduce_rec(PcEval *e, int4 d) {
   const int f = d.y, g = d.z;
   switch (d.x) {
+    case K_AE: return ae_tell(e, d, K_TELL);
     case K_PVAR: return store_embed(e, d.y, mk(1, 1));
     case K_NVAR: return store_embed(e, d.y, mk(0, 0));
     case K_TRUE: return false;
@@ -547,6 +578,7 @@ __device__ __noinline__ bool f_deduce_rec(PcEval *e, int4 d) {
 __device__ __noinline__ bool f_contra_rec(PcEval *e, int4 d) {
   const int f = d.y, g = d.z;
   switch (d.x) {
+    case K_AE: return ae_tell(e, d, K_NTELL);
     case K_PVAR: return store_embed(e, d.y, mk(0, 0));
     case K_NVAR: return store_embed(e, d.y, mk(1, 1));
     case K_TRUE:
@@ -1088,7 +1120,8 @@ __global__ void k_pc_ask_all(const int4 *tape, const int *roots, int nprops, int
 
 // ------------------------------------------------------------------ host --
 bool term_kind(int k) { return k >= K_VAR && k <= K_NMUL; }
-bool formula_kind(int k) { return k >= K_PVAR && k <= K_XOR; }
+bool formula_kind(int k) { return (k >= K_PVAR && k <= K_XOR) || k == K_AE; }
+bool item_kind(int k) { return k >= K_TELL && k <= K_NASK_OUT; }
 
 PcState *pc_state(pirgpu_ctx *ctx) {
   if (!ctx->pc) ctx->pc = new PcState();
@@ -1140,6 +1173,7 @@ int tree_base_of(PcState *s, int root) {
     lo = std::min(lo, n);
     const int4 d = s->tape[(size_t)n];
     const int k = d.x;
+    if (k == K_AE) return -1;  // store formulas take the recursive path
     int kids[PC_TREE_MAX + 2];
     int nk = 0;
     if (k == K_FORMULA || k == K_NEG || k == K_ABS || k == K_ARG) kids[nk++] = d.y;
@@ -1171,11 +1205,13 @@ int pc_build_csr(pirgpu_ctx *ctx, PcState *s) {
       todo.pop_back();
       const int4 d = s->tape[(size_t)n];
       const int k = d.x;
-      if (k == K_VAR || k == K_PVAR || k == K_NVAR) {
+      if (k == K_VAR || k == K_PVAR || k == K_NVAR || item_kind(k)) {
         if (seen[(size_t)d.y] != i) {
           seen[(size_t)d.y] = i;
           vars.push_back(d.y);
         }
+      } else if (k == K_AE) {
+        for (int j = 0; j < d.z; ++j) todo.push_back(d.y + j);
       } else if (k == K_FORMULA || k == K_NEG || k == K_ABS || k == K_ARG) {
         todo.push_back(d.y);
       } else if (k == K_NADD || k == K_NMUL) {
@@ -1275,7 +1311,7 @@ int pc_tell(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *kind, const int32_t 
   int max_var = s->max_var;
   for (int32_t i = 0; i < nnodes; ++i) {
     const int k = kind[i];
-    bool ok = c[i] == 0;
+    bool ok = c[i] == 0 || item_kind(k);
     int dep = 1;
     auto child = [&](int x, bool term) {
       return x >= 0 && x < i && (term ? term_kind(kind[x]) : formula_kind(kind[x]));
@@ -1284,8 +1320,18 @@ int pc_tell(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *kind, const int32_t 
       case K_VAR:
       case K_PVAR:
       case K_NVAR:
+      case K_TELL:
+      case K_NTELL:
+      case K_ASK:
+      case K_NASK:
+      case K_ASK_OUT:
+      case K_NASK_OUT:
         ok = ok && a[i] >= 0 && a[i] < ctx->nvars;
         if (ok) max_var = std::max(max_var, a[i]);
+        break;
+      case K_AE:
+        ok = ok && b[i] >= 0 && a[i] >= 0 && (long long)a[i] + b[i] <= i;
+        for (int j = 0; ok && j < b[i]; ++j) ok = item_kind(kind[a[i] + j]);
         break;
       case K_CONST:
       case K_TRUE:
@@ -1328,13 +1374,14 @@ int pc_tell(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *kind, const int32_t 
   const int off = (int)base;
   for (int32_t i = 0; i < nnodes; ++i) {
     const int k = kind[i];
-    const bool refs_a = !(k == K_VAR || k == K_PVAR || k == K_NVAR || k == K_CONST || k == K_TRUE || k == K_FALSE);
+    const bool refs_a = !(k == K_VAR || k == K_PVAR || k == K_NVAR || k == K_CONST || k == K_TRUE || k == K_FALSE ||
+                          item_kind(k));
     const bool refs_b = (k >= K_ADD && k <= K_MAX) || (k >= K_LEQ && k <= K_XOR);
     int4 nd;
     nd.x = k;
     nd.y = refs_a ? a[i] + off : a[i];
     nd.z = refs_b ? b[i] + off : b[i];
-    nd.w = 0;
+    nd.w = item_kind(k) ? c[i] : 0;
     s->tape.push_back(nd);
     long long len = 1;
     auto L = [&](int x) { return s->len[(size_t)x]; };

@@ -19,11 +19,14 @@ VAR, CONST, FORMULA, NEG, ABS, ADD, SUB, MUL, TDIV, FDIV, CDIV, EDIV, MIN, MAX, 
 # formulas (Formula's alternatives, formula.hpp:905-920)
 PVAR, NVAR, TRUE, FALSE, LEQ, GT, EQ, NEQ, AND, OR, EQUIV, IMPLY, XOR = range(16, 29)
 ARG = 29
-NUM_KINDS = 30
+AE = 30  # a formula of the store itself (AbstractElement): items TELL / NTELL / ASK / NASK
+TELL, NTELL, ASK, NASK, ASK_OUT, NASK_OUT = range(31, 37)
+NUM_KINDS = 37
 MAX_DEPTH = 64  # PC_MAX_DEPTH
 
 TERMS = frozenset(range(0, 16))
-FORMULAS = frozenset(range(16, 29))
+FORMULAS = frozenset(list(range(16, 29)) + [AE])
+ITEMS = frozenset(range(31, 37))
 BINARY_TERMS = {ADD: "+", SUB: "-", MUL: "*", TDIV: "tdiv", FDIV: "fdiv", CDIV: "cdiv", EDIV: "ediv",
                 MIN: "min", MAX: "max"}
 NEGATED = {LEQ: GT, GT: LEQ, EQ: NEQ, NEQ: EQ}
@@ -39,8 +42,8 @@ class Tape:
         self.nodes = []
         self.roots = []
 
-    def _add(self, kind, a=0, b=0):
-        self.nodes.append((kind, int(a), int(b), 0))
+    def _add(self, kind, a=0, b=0, c=0):
+        self.nodes.append((kind, int(a), int(b), int(c)))
         return len(self.nodes) - 1
 
     def kind(self, n):
@@ -148,6 +151,19 @@ class Tape:
 
     def xor(self, f, g):
         return self._add(XOR, f, g)
+
+    def abstract_element(self, tell=(), not_tell=(), ask=(), not_ask=(), ask_out=(), not_ask_out=()):
+        """A formula of the store itself (AbstractElement, formula.hpp:14-78):
+        each list holds (var, lb, ub) items; ask = every `ask` item's variable
+        inside its interval and every `ask_out` item's variable outside it,
+        deduce = meet every `tell` item (nask / contradeduce: the `not_`
+        lists)."""
+        first = len(self.nodes)
+        for kind, items in ((TELL, tell), (NTELL, not_tell), (ASK, ask), (NASK, not_ask), (ASK_OUT, ask_out),
+                            (NASK_OUT, not_ask_out)):
+            for v, lb, ub in items:
+                self._add(kind, v, lb, ub)
+        return self._add(AE, first, len(self.nodes) - first)
 
     # -- propagators ----------------------------------------------------
     def prop(self, f):

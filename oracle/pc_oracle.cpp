@@ -187,7 +187,8 @@ I itv_op(int op, I a, I b) {
 }
 
 bool is_term(int32_t k) { return k >= ORC_PC_VAR && k <= ORC_PC_NMUL; }
-bool is_formula(int32_t k) { return k >= ORC_PC_PVAR && k <= ORC_PC_XOR; }
+bool is_formula(int32_t k) { return (k >= ORC_PC_PVAR && k <= ORC_PC_XOR) || k == ORC_PC_AE; }
+bool is_item(int32_t k) { return k >= ORC_PC_TELL && k <= ORC_PC_NASK_OUT; }
 bool is_division(int32_t k) { return k >= ORC_PC_TDIV && k <= ORC_PC_EDIV; }
 
 // ------------------------------------------------------------- evaluator --
@@ -403,9 +404,32 @@ struct Eval {
     }
   }
 
+  // AbstractElement (formula.hpp:14-78): the store's own ask (every item's
+  // variable inside the item's interval) and deduce (meet every item), over
+  // the items of one kind
+  // item: ORC_PC_ASK or ORC_PC_NASK; the _OUT items of the same list ask
+  // that the variable misses the interval
+  bool ae_ask(int n, int32_t item) {
+    const int32_t out = item + 2;
+    for (int i = a[n]; i < a[n] + b[n]; ++i) {
+      if (k[i] != item && k[i] != out) continue;
+      const I x = load(a[i]);
+      if (is_bot(x)) continue;
+      if (k[i] == item ? !(x.l >= b[i] && x.u <= c[i]) : !is_bot(meet(x, I{b[i], c[i]}))) return false;
+    }
+    return true;
+  }
+  bool ae_tell(int n, int32_t item) {
+    bool ch = false;
+    for (int i = a[n]; i < a[n] + b[n]; ++i)
+      if (k[i] == item) ch |= store_embed(a[i], I{b[i], c[i]});
+    return ch;
+  }
+
   bool ask(int n) {
     const int32_t kind = k[n];
     switch (kind) {
+      case ORC_PC_AE: return ae_ask(n, ORC_PC_ASK);
       case ORC_PC_PVAR: return !has0(load(a[n]));           // VariableLiteral::ask_impl :101
       case ORC_PC_NVAR: return below_point(load(a[n]), 0);
       case ORC_PC_TRUE: return true;
@@ -421,6 +445,7 @@ struct Eval {
   bool nask(int n) {
     const int32_t kind = k[n];
     switch (kind) {
+      case ORC_PC_AE: return ae_ask(n, ORC_PC_NASK);
       case ORC_PC_PVAR: return below_point(load(a[n]), 0);
       case ORC_PC_NVAR: return !has0(load(a[n]));
       case ORC_PC_TRUE: return failed != 0;
@@ -437,6 +462,7 @@ struct Eval {
     const int32_t kind = k[n];
     const int f = a[n], g = b[n];
     switch (kind) {
+      case ORC_PC_AE: return ae_tell(n, ORC_PC_TELL);
       case ORC_PC_PVAR: return store_embed(a[n], I{1, 1});
       case ORC_PC_NVAR: return store_embed(a[n], I{0, 0});
       case ORC_PC_TRUE: return false;
@@ -478,6 +504,7 @@ struct Eval {
     const int32_t kind = k[n];
     const int f = a[n], g = b[n];
     switch (kind) {
+      case ORC_PC_AE: return ae_tell(n, ORC_PC_NTELL);
       case ORC_PC_PVAR: return store_embed(a[n], I{0, 0});
       case ORC_PC_NVAR: return store_embed(a[n], I{1, 1});
       case ORC_PC_TRUE:
@@ -552,9 +579,17 @@ int32_t orc_pc_validate(int32_t nnodes, const int32_t *k, const int32_t *a, cons
   };
   for (int32_t i = 0; i < nnodes; ++i) {
     const int32_t kind = k[i];
-    bool ok = c[i] == 0;
+    bool ok = c[i] == 0 || is_item(kind);
     int32_t d = 1;
     switch (kind) {
+      case ORC_PC_TELL:
+      case ORC_PC_NTELL:
+      case ORC_PC_ASK:
+      case ORC_PC_NASK: ok = a[i] >= 0 && a[i] < nvars; break;
+      case ORC_PC_AE:
+        ok = ok && b[i] >= 0 && a[i] >= 0 && (int64_t)a[i] + b[i] <= i;
+        for (int32_t j = 0; ok && j < b[i]; ++j) ok = is_item(k[a[i] + j]);
+        break;
       case ORC_PC_VAR:
       case ORC_PC_PVAR:
       case ORC_PC_NVAR: ok = ok && a[i] >= 0 && a[i] < nvars; break;

@@ -47,7 +47,10 @@ enum {
   ORC_PC_LEQ = 20, ORC_PC_GT = 21, ORC_PC_EQ = 22, ORC_PC_NEQ = 23, /* a, b = terms */
   ORC_PC_AND = 24, ORC_PC_OR = 25, ORC_PC_EQUIV = 26, ORC_PC_IMPLY = 27, ORC_PC_XOR = 28, /* a, b = formulas */
   ORC_PC_ARG = 29, /* operand slot of NADD / NMUL: a = term */
-  ORC_PC_NUM_KINDS = 30
+  ORC_PC_AE = 30,  /* AbstractElement: items a .. a+b-1 */
+  ORC_PC_TELL = 31, ORC_PC_NTELL = 32, ORC_PC_ASK = 33, ORC_PC_NASK = 34, /* items {kind, var, lb, ub} */
+  ORC_PC_ASK_OUT = 35, ORC_PC_NASK_OUT = 36, /* asks that the variable misses [lb, ub] */
+  ORC_PC_NUM_KINDS = 37
 };
 
 /* Checks a tape against nvars; returns the deepest root's depth (nodes on the

@@ -10,10 +10,18 @@ is_extractable() after it, and the loop's has_changed.  BOT as `after`
 means the store must become empty (is_bot()).
 
 The reference compiles the FlatZinc with lala-parsing into formulas that
-PC interprets (pc.hpp:505-605); here include/pirgpu_fzn_pc.hpp does.  The
-AbstractElement tests (:714-764) need formulas typed for the sub-domain
-(lala-core's VStore interpretation inside PC) and are not reproduced.
+PC interprets (pc.hpp:505-605); here include/pirgpu_fzn_pc.hpp does.
 Expected values are transcribed from the test source.
+
+AE_CASES restate the AbstractElement tests (:714-764), whose two comparisons
+are typed for the store (tests/pc_test.cpp:709-712), so that PC keeps each as
+an AbstractElement (formula.hpp:14-78) holding the store's tell / ask of the
+comparison and of its negation, combined by `nbool_equiv` (read as <=>, which
+the expected values require).  `x >= 5`: tell / ask x in [5, inf), negation
+x in (-inf, 4].  `x == 5`: tell / ask x in [5, 5]; its negation x != 5 has no
+interval tell (no holes) and asks that 5 is not in x.  A step is
+(store meets, before, after, extractable, changed); BOT as `after`: the store
+becomes empty.
 """
 
 INF = 2**31 - 1
@@ -216,4 +224,22 @@ CASES = [
     ("InfiniteDomain2", 778, "var int: x; var bool: b; constraint int_eq(b, int_le(x,5));",
      [one([TOP, (0, 1)]),
       one([TOP, (0, 0)], [(6, INF), (0, 0)], ua=True, tell="constraint int_eq(b, 0);")]),
+]
+
+
+AE_CASES = [
+    ("AbstractElement1", 714, "ge_le",
+     [([], [(0, 10), (0, 10)], [(0, 10), (0, 10)], False, False),
+      ([(0, 5, 5)], [(5, 5), (0, 10)], [(5, 5), (0, 5)], True, True)]),
+    ("AbstractElement2", 725, "ge_le",
+     [([], [(0, 10), (0, 10)], [(0, 10), (0, 10)], False, False),
+      ([(0, 4, 4)], [(4, 4), (0, 10)], [(4, 4), (6, 10)], True, True)]),
+    ("AbstractElement3", 736, "eq_eq",
+     [([], [(0, 10), (0, 10)], [(0, 10), (0, 10)], False, False),
+      ([(1, 6, 6)], [(0, 10), (6, 6)], [(0, 10), (6, 6)], False, False),
+      ([(0, 5, 5)], [(5, 5), (6, 6)], BOT, False, True)]),
+    ("AbstractElement4", 751, "eq_eq",
+     [([], [(0, 10), (0, 10)], [(0, 10), (0, 10)], False, False),
+      ([(1, 4, 4)], [(0, 10), (4, 4)], [(0, 10), (4, 4)], False, False),
+      ([(0, 5, 5)], [(5, 5), (4, 4)], BOT, False, True)]),
 ]

@@ -66,7 +66,7 @@ def offset_tape(tape, base):
     """Node indices of a tape shifted by `base` (the fields that are indices)."""
     t = np.array(tape, np.int32).reshape(-1, 4).copy()
     k = t[:, 0]
-    refs_a = ~np.isin(k, [0, 1, 16, 17, 18, 19])  # VAR CONST PVAR NVAR TRUE FALSE hold data in a
+    refs_a = ~np.isin(k, [0, 1, 16, 17, 18, 19, 31, 32, 33, 34, 35, 36])  # data in a: leaves and store items
     refs_b = ((k >= 5) & (k <= 13)) | ((k >= 20) & (k <= 28))
     t[refs_a, 1] += base
     t[refs_b, 2] += base
@@ -347,3 +347,36 @@ def planted_formulas(rng, nvars, nprops, depth=3):
         t.roots.append(int(roots[0]) + off)
         kept += 1
     return t, store, s
+
+
+def ae_tape(shape):
+    """The formula of the AbstractElement cases over x = 0, y = 1."""
+    import pc as P
+    t = P.Tape()
+    if shape == "ge_le":  # nbool_equiv(int_ge(x, 5), int_le(y, 5))
+        f = t.abstract_element(tell=[(0, 5, INF)], not_tell=[(0, MINF, 4)], ask=[(0, 5, INF)], not_ask=[(0, MINF, 4)])
+        g = t.abstract_element(tell=[(1, MINF, 5)], not_tell=[(1, 6, INF)], ask=[(1, MINF, 5)], not_ask=[(1, 6, INF)])
+    else:  # nbool_equiv(int_eq(x, 5), int_eq(y, 5))
+        f = t.abstract_element(tell=[(0, 5, 5)], ask=[(0, 5, 5)], not_ask_out=[(0, 5, 5)])
+        g = t.abstract_element(tell=[(1, 5, 5)], ask=[(1, 5, 5)], not_ask_out=[(1, 5, 5)])
+    t.prop(t.equiv(f, g))
+    return t.arrays()
+
+
+def run_ae_case(model_steps, case):
+    """model_steps(meets) -> (status, bounds, extractable, changed) after the
+    meets and the fixpoint; returns the mismatches of one AE case."""
+    from golden import pc_kat_cases as K
+    name, line, shape, steps = case
+    bad = []
+    for k, (meets, before, after, ua, changed) in enumerate(steps):
+        rc, b0, b1, ex, ch = model_steps(meets)
+        if b0 != [tuple(x) for x in before]:
+            bad.append((k, "before", b0, before))
+        if after == K.BOT:
+            if rc != 1:
+                bad.append((k, "status", rc))
+            continue
+        if rc != 0 or b1 != [tuple(x) for x in after] or ex != ua or ch != changed:
+            bad.append((k, rc, b1, after, ex, ua, ch, changed))
+    return bad

@@ -77,7 +77,7 @@ def test_pc_kinds_match_header_builder_and_oracle():
     enum = src[src.index("enum pc_kind"):]
     enum = enum[:enum.index("};")]
     kinds = dict((m.group(1), int(m.group(2))) for m in re.finditer(r"PC_([A-Z_]+) = (\d+)", enum))
-    assert len(kinds) == 31 and kinds["NUM_KINDS"] == P.NUM_KINDS == 30
+    assert len(kinds) == 38 and kinds["NUM_KINDS"] == P.NUM_KINDS == 37
     for name, v in kinds.items():
         if name != "NUM_KINDS":
             assert getattr(P, name) == v, name

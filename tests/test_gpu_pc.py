@@ -341,3 +341,22 @@ def test_error_paths_and_edge_cases(gpu_ctx_factory):
     t3.prop(t3.false())
     ctx.pc_tell(*t3.arrays())
     assert ctx.pc_fixpoint()[0] == pirgpu.FAILED and ctx.is_bot()
+
+
+@pytest.mark.parametrize("case", K.AE_CASES, ids=[c[0] for c in K.AE_CASES])
+def test_abstract_element_gpu(case, gpu_ctx_factory):
+    """tests/pc_test.cpp:714-764 through the C ABI (both schedules)."""
+    for sched in (pirgpu.SCHED_AC1, pirgpu.SCHED_EVENTS):
+        tape, roots = H.ae_tape(case[2])
+        ctx = _ctx(gpu_ctx_factory, tape, roots, np.array([[0, 10], [0, 10]], np.int32))
+
+        def steps(meets):
+            for v, l, u in meets:
+                ctx.embed(v, l, u)
+            lb, ub = ctx.read_store()
+            b0 = [(int(lb[i]), int(ub[i])) for i in range(2)]
+            rc, st = ctx.pc_fixpoint(sched=sched)
+            lb, ub = ctx.read_store()
+            return rc, b0, [(int(lb[i]), int(ub[i])) for i in range(2)], ctx.pc_is_extractable(), st["narrowed"] > 0
+
+        assert H.run_ae_case(steps, case) == []

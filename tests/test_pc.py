@@ -167,3 +167,22 @@ def test_planted_formulas_keep_their_solution(oracle):
         assert oracle.pc_fixpoint_jacobi(tape, order, b)[0] == oracle.OK
         np.testing.assert_array_equal(a, b)
         assert np.all((hidden >= a[:, 0]) & (hidden <= a[:, 1]))
+
+
+@pytest.mark.parametrize("case", K.AE_CASES, ids=[c[0] for c in K.AE_CASES])
+def test_abstract_element_oracle(case, oracle):
+    """tests/pc_test.cpp:714-764 on the oracle."""
+    tape, roots = H.ae_tape(case[2])
+    store = np.array([[0, 10], [0, 10]], np.int32)
+    state = {"failed": False}
+
+    def steps(meets):
+        for v, l, u in meets:
+            store[v] = [max(store[v, 0], l), min(store[v, 1], u)]
+        b0 = [tuple(int(x) for x in r) for r in store]
+        rc, info = oracle.pc_fixpoint(tape, roots, store)
+        state["failed"] = rc == oracle.FAILED
+        ex = rc == oracle.OK and all(oracle.pc_ask(tape, r, store) for r in roots)
+        return rc, b0, [tuple(int(x) for x in r) for r in store], ex, info["has_changed"]
+
+    assert H.run_ae_case(steps, case) == []
