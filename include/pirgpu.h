@@ -60,7 +60,9 @@ enum pir_sched {
   PIR_SCHED_LEARNED = 1,  /* wake set chosen by the trained scorer, certified by a full sweep */
   PIR_SCHED_EVENTS = 2    /* each round runs the propagators of the variables narrowed in the previous
                              round (the first round runs all).  pir_fixpoint: one instance, rounds
-                             with at most opts.local_frontier propagators on one CTA;
+                             with at most opts.local_frontier propagators on one CTA, the
+                             propagators of narrowed variables with at most 4 propagators run at
+                             once by the narrowing thread (opts.chase);
                              pir_fixpoint_nodes: one CTA per node, when the base store is at its
                              fixpoint (else AC-1 rounds) */
 };
@@ -79,7 +81,9 @@ typedef struct pir_opts {
   float wake_fraction;        /* learned schedule: fraction of propagators woken per round (0: 1/16) */
   int32_t variant;            /* persistent kernel variant 1..PIR_PERSISTENT_VARIANTS (0: autotuned, else the default) */
   int32_t local_frontier;     /* event schedule: rounds of at most this many propagators run on one CTA (0: 256) */
-  int32_t reserved[5];
+  int32_t chase;              /* event schedule: propagators of narrowed small variables a thread runs at once,
+                                 per frontier entry (0: 64; < 0: none, everything waits for the next round) */
+  int32_t reserved[4];
 } pir_opts;
 
 typedef struct pir_stats {

@@ -47,18 +47,91 @@ def test_events_spec_fails(seed, P, oracle):
     assert rc == orc == oracle.FAILED
 
 
+@pytest.mark.parametrize("chase", [-1, 0])
 @pytest.mark.parametrize("local", [0, 1])
-def test_events_chain_and_random(local, P, oracle):
-    """100k vars / 400k propagators plus a 3,000-link chain: the deep part runs
-    mostly in small-frontier rounds."""
+def test_events_chain_and_random(local, chase, P, oracle):
+    """100k vars / 400k propagators plus a 3,000-link chain: without chasing
+    the deep part takes a round per link, mostly small-frontier rounds; with
+    it, a few dozen rounds."""
     import workloads as W
     inst = W.add_chain(W.plain(100_000, 400_000, 10**6, 7), 3000, 10**6, 7)
-    rc, g, st, orc, o, info = _both(P, oracle, inst, local_frontier=local)
+    rc, g, st, orc, o, info = _both(P, oracle, inst, local_frontier=local, chase=chase)
     assert rc == orc == oracle.OK
     np.testing.assert_array_equal(g, o)
-    assert st["rounds"] >= 2900
-    # far fewer executions than AC-1 sweeps of every propagator
-    assert st["executions"] < st["rounds"] * inst.nprops // 20
+    if chase < 0:
+        assert st["rounds"] >= 2900
+        # far fewer executions than AC-1 sweeps of every propagator
+        assert st["executions"] < st["rounds"] * inst.nprops // 20
+    else:
+        assert st["rounds"] < 500
+        assert st["executions"] < 20 * inst.nprops
+
+
+@pytest.mark.parametrize("chase", [-1, 0])
+@pytest.mark.parametrize("local", [0, 300, 1 << 30])
+def test_events_hub_overflow(local, chase, P, oracle):
+    """A 300-link chain whose middle variable feeds 3,000 more propagators
+    y_j = x_150 + c_j: the round that narrows x_150 lists more propagators
+    than a round on one CTA keeps in shared memory (256) and than its dedupe
+    set holds (2,048), so both spill to the global list and round stamps."""
+    import workloads as W
+    empty = W.Instance(np.zeros(0, np.int32), np.zeros(0, np.int32), *(np.zeros(0, np.int32),) * 4)
+    chain = W.add_chain(empty, 300, 10**6, 5)
+    n0, k, hub = chain.nvars, 3000, 150
+    c = np.random.default_rng(5).integers(1, 6, k)
+    ys, cs = np.arange(n0, n0 + k), np.arange(n0 + k, n0 + 2 * k)
+    inst = W.Instance(np.concatenate([chain.lb, np.full(k, -10**6), c]),
+                      np.concatenate([chain.ub, np.full(k, 10**6), c]),
+                      np.concatenate([chain.op, np.full(k, W.ADD)]), np.concatenate([chain.x, ys]),
+                      np.concatenate([chain.y, np.full(k, hub)]), np.concatenate([chain.z, cs]))
+    rc, g, st, orc, o, info = _both(P, oracle, inst, local_frontier=local, chase=chase)
+    assert rc == orc == oracle.OK
+    np.testing.assert_array_equal(g, o)
+    # (a round may read bounds joined earlier in the same round, so the waves
+    # can move faster than one link per round)
+    assert st["rounds"] >= (100 if chase < 0 else 2)
+    # x_150 narrows in about 150 rounds, each listing its 3,002 propagators
+    # (once each): fewer executions than the oracle's 301 sweeps
+    assert st["executions"] < info["execs"]
+
+
+@pytest.mark.parametrize("chase", [-1, 1, 3, 64, 100_000])
+@pytest.mark.parametrize("local", [1, 256, 1 << 30])
+def test_events_chase(chase, local, P, oracle):
+    """The chase budget (runs of small variables' propagators done at once by
+    the narrowing thread; -1: none) changes the rounds, never the fixpoint."""
+    import workloads as W
+    inst = W.add_chain(W.plain(30_000, 120_000, 10**6, 11), 2000, 10**6, 11)
+    rc, g, st, orc, o, _ = _both(P, oracle, inst, local_frontier=local, chase=chase)
+    assert rc == orc == oracle.OK
+    np.testing.assert_array_equal(g, o)
+    if chase < 0:
+        assert st["rounds"] >= 1900  # one link per round
+    elif chase >= 64:
+        assert st["rounds"] < 1000
+
+
+@pytest.mark.parametrize("chase", [-1, 0, 2])
+@pytest.mark.parametrize("seed", range(3))
+def test_events_chase_failures_and_divisions(seed, chase, P, oracle):
+    import workloads as W
+    for inst in [W.single_small(seed, variant="spec")] + W.uneven(3, 2000, 20_000, seed):
+        rc, g, _, orc, o, _ = _both(P, oracle, inst, chase=chase)
+        assert rc == orc
+        if orc == oracle.OK:
+            np.testing.assert_array_equal(g, o)
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_events_chain_local_everywhere(seed, P, oracle):
+    """Every round after the first on one CTA, frontiers of thousands
+    included, on the chain-and-random instance."""
+    import workloads as W
+    inst = W.add_chain(W.plain(20_000, 80_000, 10**6, seed), 1000, 10**6, seed)
+    rc, g, st, orc, o, _ = _both(P, oracle, inst, local_frontier=1 << 30)
+    assert rc == orc
+    if orc == oracle.OK:
+        np.testing.assert_array_equal(g, o)
 
 
 def test_events_uneven_divisions(P, oracle):
@@ -74,12 +147,12 @@ def test_events_round_cap(P, oracle):
     import workloads as W
     empty = W.Instance(np.zeros(0, np.int32), np.zeros(0, np.int32), *(np.zeros(0, np.int32),) * 4)
     inst = W.add_chain(empty, 2000, 10**6, 1)
-    for local in (0, 1):
+    for local, chase, cap in ((0, -1, 100), (1, -1, 100), (0, 0, 2), (1, 0, 2)):
         ctx = P.Context(0)
         ctx.load_store(inst.lb, inst.ub)
         ctx.tell(inst.op, inst.x, inst.y, inst.z)
-        rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS, max_rounds=100, local_frontier=local)
-        assert rc == P.TIMEOUT and st["rounds"] == 100
+        rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS, max_rounds=cap, local_frontier=local, chase=chase)
+        assert rc == P.TIMEOUT and st["rounds"] == cap
         rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS)
         assert rc == P.OK
         lb, ub = ctx.read_store()
