@@ -82,7 +82,8 @@ typedef struct pir_opts {
   int32_t variant;            /* persistent kernel variant 1..PIR_PERSISTENT_VARIANTS (0: autotuned, else the default) */
   int32_t local_frontier;     /* event schedule: rounds of at most this many propagators run on one CTA (0: 256) */
   int32_t chase;              /* event schedule: propagators of narrowed small variables a thread runs at once,
-                                 per frontier entry (0: 64; < 0: none, everything waits for the next round) */
+                                 per frontier entry (0: 64; at most 256; < 0: none, everything waits for the next
+                                 round) */
   int32_t reserved[4];
 } pir_opts;
 

@@ -72,7 +72,10 @@ __device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
 // round, which is all the event schedule needs (the propagators are
 // monotone).  A deep chain of small variables then advances up to `chase`
 // links per round instead of one.
-constexpr int CHASE_DEG = 4, CHASE_CAP = 8, CLOSE_RUNS = 4, CHASE_DEFAULT = 64;
+// The budget is capped: a chase is dependent L2 round trips (a few us each,
+// more when many chasers narrow the same variables), and the grid's other
+// CTAs wait for the round at a barrier with a time limit.
+constexpr int CHASE_DEG = 4, CHASE_CAP = 8, CLOSE_RUNS = 4, CHASE_DEFAULT = 64, CHASE_MAX = 256;
 
 // One run's joins: red to the store as RedStore does, and the run's view of
 // its three variables (the intervals it read, met with what it joined) for
@@ -510,7 +513,7 @@ int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
   a.timeout_ns = opts.barrier_timeout_ns > 0 ? opts.barrier_timeout_ns : 2000000000ll;
   a.local_max = opts.local_frontier > 0 ? (unsigned)opts.local_frontier : 256u;
-  a.chase = opts.chase > 0 ? opts.chase : (opts.chase < 0 ? 0 : CHASE_DEFAULT);
+  a.chase = opts.chase > 0 ? std::min(opts.chase, CHASE_MAX) : (opts.chase < 0 ? 0 : CHASE_DEFAULT);
   int occ = 0;
   PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fixpoint_events, 256, 0));
   if (occ < 1) return set_err(ctx, PIR_ECUDA, "event kernel does not fit on an SM");

@@ -95,7 +95,7 @@ def test_events_hub_overflow(local, chase, P, oracle):
     assert st["executions"] < info["execs"]
 
 
-@pytest.mark.parametrize("chase", [-1, 1, 3, 64, 100_000])
+@pytest.mark.parametrize("chase", [-1, 1, 3, 64, 100_000])  # 100,000: capped at 256
 @pytest.mark.parametrize("local", [1, 256, 1 << 30])
 def test_events_chase(chase, local, P, oracle):
     """The chase budget (runs of small variables' propagators done at once by
@@ -109,6 +109,29 @@ def test_events_chase(chase, local, P, oracle):
         assert st["rounds"] >= 1900  # one link per round
     elif chase >= 64:
         assert st["rounds"] < 1000
+
+
+def test_events_long_chain_capped_chase(P):
+    """A 100,000-link chain x_{i+1} = x_i + c_i with x_0 in [0, 1e6] and every
+    x_i in [-1e6, 1e6]: its fixpoint is x_i in [prefix sum, 1e6 - suffix sum].
+    An unbounded chase request is capped, so no round outlasts the grid
+    barrier's wait limit."""
+    import workloads as W
+    L = 100_000
+    empty = W.Instance(np.zeros(0, np.int32), np.zeros(0, np.int32), *(np.zeros(0, np.int32),) * 4)
+    inst = W.add_chain(empty, L, 10**6, 3)
+    c = inst.lb[L + 1:].astype(np.int64)
+    want_lb = np.concatenate([[0], np.cumsum(c)])
+    want_ub = 10**6 - np.concatenate([np.cumsum(c[::-1])[::-1], [0]])
+    ctx = P.Context(0)
+    ctx.load_store(inst.lb, inst.ub)
+    ctx.tell(inst.op, inst.x, inst.y, inst.z)
+    rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS, chase=1 << 30)
+    assert rc == P.OK
+    lb, ub = ctx.read_store()
+    np.testing.assert_array_equal(lb[:L + 1], want_lb)
+    np.testing.assert_array_equal(ub[:L + 1], want_ub)
+    assert st["rounds"] >= L // 256
 
 
 @pytest.mark.parametrize("chase", [-1, 0, 2])
