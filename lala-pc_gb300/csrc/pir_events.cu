@@ -75,11 +75,15 @@ __device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
 // The budget is capped: a chase is dependent L2 round trips (a few us each,
 // more when many chasers narrow the same variables), and the grid's other
 // CTAs wait for the round at a barrier with a time limit.
-constexpr int CHASE_DEG = 4, CHASE_CAP = 8, CLOSE_RUNS = 4, CHASE_DEFAULT = 64, CHASE_MAX = 256;
+constexpr int CHASE_DEG = 4, CHASE_CAP = 8, CLOSE_RUNS = 4, CHASE_DEFAULT = 64, CHASE_MAX = 256, DEFER_CAP = 8;
 
 // One run's joins: red to the store as RedStore does, and the run's view of
 // its three variables (the intervals it read, met with what it joined) for
 // a repeat on its own results; hit = the slots whose variable narrowed.
+// (Atomics whose old value tells whether a join moved the stored bound would
+// let only that run propagate, but waiting for the old value puts an L2
+// round trip on every chased step: 62 -> 80 ms on 1M vars / 4M propagators
+// plus a 20,000-link chain.)
 struct RunView {
   int2 *s;
   int var[3];
@@ -130,6 +134,21 @@ struct EvSched {
   __device__ __forceinline__ void list_prop(int q) const {
     if (atomicMax(pstamp + q, next_round) < next_round) next[atomicAdd(next_cnt, 1u)] = q;
   }
+  // Lists the cnt (<= DEFER_CAP) propagators buf[0], buf[stride], ...
+  __device__ __forceinline__ void list_batch(const int *buf, int cnt, int stride) const {
+    int q[DEFER_CAP];
+    unsigned take = 0;
+#pragma unroll
+    for (int j = 0; j < DEFER_CAP; ++j) q[j] = j < cnt ? buf[j * stride] : -1;
+#pragma unroll
+    for (int j = 0; j < DEFER_CAP; ++j)
+      if (q[j] >= 0 && atomicMax(pstamp + q[j], next_round) < next_round) take |= 1u << j;
+    if (!take) return;
+    unsigned slot = atomicAdd(next_cnt, (unsigned)__popc(take));
+#pragma unroll
+    for (int j = 0; j < DEFER_CAP; ++j)
+      if (take & (1u << j)) next[slot++] = q[j];
+  }
   // Lists v's propagators (adjacency range r) for the next round.
   __device__ __forceinline__ void schedule(int v, int2 r) const {
     if (atomicMax(vstamp + v, next_round) >= next_round) return;
@@ -162,15 +181,20 @@ __device__ __forceinline__ EvSched ev_sched(const EvFixArgs &a, long long round)
 }
 
 // Runs frontier entry q and what it chases (stack: this thread's CHASE_CAP
-// slots, blockDim.x apart).  Returns the bounds narrowed.
+// slots, blockDim.x apart; defer: its DEFER_CAP slots).  Returns the bounds
+// narrowed.  A run whose variable is chased is itself listed for the next
+// round: its repeat on its own results does not see what a concurrent run of
+// the same propagator joined, and the next round reads the store after the
+// barrier.  Those listings wait in `defer` and go out DEFER_CAP at a time
+// (their stamp atomics in flight together), off the chase's critical path.
 template <class Sched>
-__device__ __forceinline__ int run_entry(int q, const EvFixArgs &a, const Sched &sc, int *stack, int budget,
-                                         unsigned long long &execs, int &failed) {
+__device__ __forceinline__ int run_entry(int q, const EvFixArgs &a, const Sched &sc, int *stack, int *defer,
+                                         int budget, unsigned long long &execs, int &failed) {
   const int stride = blockDim.x;
   const int close = budget > 0 ? CLOSE_RUNS : 1;
   RunView w;
   w.s = a.store;
-  int sp = 0, changed = 0;
+  int sp = 0, dn = 0, changed = 0;
   for (;;) {
     const int4 b = __ldg(a.bc + q);
     w.var[0] = b.y;
@@ -197,6 +221,7 @@ __device__ __forceinline__ int run_entry(int q, const EvFixArgs &a, const Sched 
     }
     if (failed) return changed;  // the round fails
     if (k == close) sc.list_prop(q);
+    bool chased = false;
     // each distinct variable once (a hit marks every slot of its variable)
     if (b.z == b.y) hit &= ~2u;
     if (b.w == b.y || b.w == b.z) hit &= ~4u;
@@ -212,8 +237,16 @@ __device__ __forceinline__ int run_entry(int q, const EvFixArgs &a, const Sched 
 #pragma unroll
         for (int j = 0; j < CHASE_DEG; ++j)
           if (e[j] != q) stack[(sp++) * stride] = e[j];
+        chased = true;
       } else {
         sc.schedule(v, r);
+      }
+    }
+    if (chased && k < close) {
+      defer[(dn++) * stride] = q;
+      if (dn == DEFER_CAP) {
+        sc.list_batch(defer, dn, stride);
+        dn = 0;
       }
     }
     if (sp == 0) break;
@@ -224,19 +257,21 @@ __device__ __forceinline__ int run_entry(int q, const EvFixArgs &a, const Sched 
     q = stack[(--sp) * stride];
     --budget;
   }
+  if (dn) sc.list_batch(defer, dn, stride);
   return changed;
 }
 
 // Runs the frontier entries i = first, first + stride, ... < items of round
 // `round` (round 0: every propagator).  Returns the bounds narrowed.
 __device__ __forceinline__ int run_frontier(const EvFixArgs &a, long long round, long long items, long long first,
-                                            long long stride, int *stack, unsigned long long &execs, int &failed) {
+                                            long long stride, int *stack, int *defer, unsigned long long &execs,
+                                            int &failed) {
   const EvSched sc = ev_sched(a, round);
   const int *cur = (round & 1) ? a.list1 : a.list0;
   int changed = 0;
   for (long long i = first; i < items && !failed; i += stride) {
     const int q = round == 0 ? (int)i : __ldcg(cur + i);
-    changed += run_entry(q, a, sc, stack, a.chase, execs, failed);
+    changed += run_entry(q, a, sc, stack, defer, a.chase, execs, failed);
   }
   return changed;
 }
@@ -295,6 +330,9 @@ struct LocalSched {
   __device__ __forceinline__ void list_prop(int q) const {
     if (claim(q)) append(q, atomicAdd(next_cnt, 1u));
   }
+  __device__ __forceinline__ void list_batch(const int *buf, int cnt, int stride) const {
+    for (int j = 0; j < cnt; ++j) list_prop(buf[j * stride]);
+  }
   __device__ __forceinline__ void schedule(int v, int2 r) const {
     const int fresh = local_insert<LV_LOG>(vset, v);
     if (fresh == 0) return;
@@ -322,7 +360,7 @@ struct LocalSched {
 // the outcome to the control block, and on a hand-over the frontier size to
 // the global counter (thread 0; the writes precede its release at the next
 // grid barrier).
-__device__ void run_local(const EvFixArgs &a, long long round, int *stack, unsigned long long &execs,
+__device__ void run_local(const EvFixArgs &a, long long round, int *stack, int *defer, unsigned long long &execs,
                           unsigned long long &narrowed) {
   __shared__ LocalShared sh;
   const int tid = threadIdx.x;
@@ -369,7 +407,7 @@ __device__ void run_local(const EvFixArgs &a, long long round, int *stack, unsig
     int failed = 0, changed = 0;
     for (unsigned i = tid; i < items && !failed; i += blockDim.x) {
       const int q = i < (unsigned)LOCAL_CAP ? sh.q[p][i] : __ldcg(cur + i);
-      changed += run_entry(q, a, sc, stack, a.chase, execs, failed);
+      changed += run_entry(q, a, sc, stack, defer, a.chase, execs, failed);
     }
     narrowed += changed;
     const unsigned bits = __reduce_or_sync(0xFFFFFFFFu, (changed ? 1u : 0u) | (failed ? 2u : 0u));
@@ -404,7 +442,7 @@ __device__ void run_local(const EvFixArgs &a, long long round, int *stack, unsig
 
 __global__ void __launch_bounds__(256, 2) k_fixpoint_events(EvFixArgs a) {
   __shared__ unsigned s_bits[2], s_word[2];
-  __shared__ int s_stack[CHASE_CAP * 256];
+  __shared__ int s_stack[CHASE_CAP * 256], s_defer[DEFER_CAP * 256];
   const int tid = threadIdx.x;
   const long long gtid = blockIdx.x * (long long)blockDim.x + tid;
   const long long gstride = (long long)gridDim.x * blockDim.x;
@@ -418,7 +456,7 @@ __global__ void __launch_bounds__(256, 2) k_fixpoint_events(EvFixArgs a) {
     const int p = (int)(nbar & 1);
     if (round > 0 && items <= (long long)a.local_max) {
       // small frontier: CTA 0 runs the rounds, everyone meets at the next grid barrier
-      if (blockIdx.x == 0) run_local(a, round, s_stack + tid, execs, narrowed);
+      if (blockIdx.x == 0) run_local(a, round, s_stack + tid, s_defer + tid, execs, narrowed);
       __syncthreads();
       if (tid == 0) s_word[p] = grid_sync_rot(a.ctl, gridDim.x, nbar, 0, 0, a.timeout_ns, &a.ctl->hb);
       __syncthreads();
@@ -435,7 +473,7 @@ __global__ void __launch_bounds__(256, 2) k_fixpoint_events(EvFixArgs a) {
     // the counter of round + 2 was last read in round - 1
     if (blockIdx.x == 0 && tid == 0) a.cnt[((round + 2) % 3) * CNT_STRIDE] = 0u;
     int failed = 0;
-    const int changed = run_frontier(a, round, items, gtid, gstride, s_stack + tid, execs, failed);
+    const int changed = run_frontier(a, round, items, gtid, gstride, s_stack + tid, s_defer + tid, execs, failed);
     narrowed += changed;
     const unsigned bits = __reduce_or_sync(0xFFFFFFFFu, (changed ? 1u : 0u) | (failed ? 2u : 0u));
     if ((tid & 31) == 0 && bits) atomicOr(&s_bits[p], bits);

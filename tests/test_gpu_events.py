@@ -111,6 +111,48 @@ def test_events_chase(chase, local, P, oracle):
         assert st["rounds"] < 1000
 
 
+def _mixed_chain(L, seed):
+    """x_{i+1} = x_i op c_i with op in {+, max, min, *} and c_i in [1, 3],
+    each x_{i+1} also reified against a constant (b_i <-> x_{i+1} <= t_i or
+    x_{i+1} = t_i); the last link's upper bound is cut so that a wave also
+    runs back.  Every variable has at most 3 propagators, so chases run
+    through all of it, including reified propagators whose result needs both
+    bounds of a variable."""
+    import workloads as W
+    rng = np.random.default_rng(seed)
+    lb, ub, op, X, Y, Z = [], [], [], [], [], []
+
+    def var(lo, hi):
+        lb.append(lo)
+        ub.append(hi)
+        return len(lb) - 1
+
+    x = var(0, 20)
+    for _ in range(L):
+        c = int(rng.integers(1, 4))
+        cv = var(c, c)
+        nx = var(-10**6, 10**6)
+        op.append([W.ADD, W.MAX, W.MIN, W.MUL][int(rng.integers(0, 4))])
+        X.append(nx), Y.append(x), Z.append(cv)
+        t = int(rng.integers(0, 40))
+        op.append(W.LEQ if rng.integers(0, 2) else W.EQ)
+        X.append(var(0, 1)), Y.append(nx), Z.append(var(t, t))
+        x = nx
+    ub[x] = int(rng.integers(5, 60))
+    return W.Instance(lb, ub, op, X, Y, Z)
+
+
+@pytest.mark.parametrize("chase", [-1, 0, 1, 256])
+@pytest.mark.parametrize("seed", range(6))
+def test_events_chase_mixed_chains(seed, chase, P, oracle):
+    inst = _mixed_chain(1500, seed)
+    for local in (0, 1 << 30):
+        rc, g, _, orc, o, _ = _both(P, oracle, inst, local_frontier=local, chase=chase)
+        assert rc == orc
+        if orc == oracle.OK:
+            np.testing.assert_array_equal(g, o)
+
+
 def test_events_long_chain_capped_chase(P):
     """A 100,000-link chain x_{i+1} = x_i + c_i with x_0 in [0, 1e6] and every
     x_i in [-1e6, 1e6]: its fixpoint is x_i in [prefix sum, 1e6 - suffix sum].
