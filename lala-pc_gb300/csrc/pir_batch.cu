@@ -72,14 +72,34 @@ struct BatchState {
   unsigned char *d_ent = nullptr;  // entailed-at-base flags per propagator
   size_t cap_ent = 0;
   long long ent_store_version = -1, ent_bc_version = -1;
+  // staged node batches (the search driver): pinned input / output staging,
+  // their device images, and the graph of one batch (clear the counters,
+  // copy in, node kernel, copy out), rebuilt when a buffer moves or the
+  // kernel variant changes, else updated in place
+  int32_t *h_sin = nullptr;
+  size_t cap_sin = 0;
+  char *h_sout = nullptr;
+  size_t cap_sout = 0;
+  void *d_sin = nullptr, *d_sout = nullptr;
+  size_t cap_dsin = 0, cap_dsout = 0;
+  cudaGraph_t sg = nullptr;
+  cudaGraphExec_t sgx = nullptr;
+  cudaGraphNode_t sg_in = nullptr, sg_kernel = nullptr, sg_out = nullptr;
+  const void *sg_kfn = nullptr;
+  const void *sg_bufs[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 void destroy_batch_state(pirgpu_ctx *ctx) {
   BatchState *b = ctx->batch;
   if (!b) return;
   if (b->h_stage) cudaFreeHost(b->h_stage);
+  if (b->sgx) cudaGraphExecDestroy(b->sgx);
+  if (b->sg) cudaGraphDestroy(b->sg);
+  if (b->h_sin) cudaFreeHost(b->h_sin);
+  if (b->h_sout) cudaFreeHost(b->h_sout);
   void *ptrs[] = {b->d_bc, b->d_off,    b->d_store, b->d_aux,     b->d_iout, b->d_nstore, b->d_tight,
-                  b->d_nout, b->d_nio, b->d_bc4, b->d_adj_ptr, b->d_adj, b->d_ev, b->d_ent, b->d_watch};
+                  b->d_nout, b->d_nio, b->d_bc4, b->d_adj_ptr, b->d_adj, b->d_ev, b->d_ent, b->d_watch,
+                  b->d_sin, b->d_sout};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete b;
@@ -887,11 +907,18 @@ int events_graph(pirgpu_ctx *ctx, const int4 **bc, const int **adj_ptr, const in
   return PIR_OK;
 }
 
-int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const int32_t *off, const int32_t *var,
-                          const int32_t *lb, const int32_t *ub, const pir_opts &opts, int32_t *out_lb,
-                          int32_t *out_ub, int32_t *out_status, int32_t *out_rounds, pir_stats *stats,
-                          int32_t nwatch = 0, const int32_t *watch = nullptr, int32_t *out_wlb = nullptr,
-                          int32_t *out_wub = nullptr) {
+// A launch of the event node kernel for nnodes nodes, all but the nodes' own
+// arrays: the variant, the grid, the per-CTA scratch and the propagators
+// entailed at the base store (recomputed when the store or bytecode changed).
+struct NodePlan {
+  const void *kfn;
+  int grid, block;
+  size_t dyn_smem;
+  bool need_ent;
+  EvArgs a;
+};
+
+static int plan_nodes(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const pir_opts &opts, NodePlan *plan) {
   int r;
   if ((r = ensure_events_graph(ctx, b))) return r;
   // variants 1..7: (threads per CTA, resident CTAs per SM the registers are sized for)
@@ -968,6 +995,29 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
   if ((r = ensure(ctx, (void **)&b->d_ent, &b->cap_ent, n))) return r;
   const bool need_ent = b->ent_store_version != ctx->store_version || b->ent_bc_version != ctx->bytecode_version;
   a.ent = b->d_ent;
+  plan->kfn = kfn;
+  plan->grid = grid;
+  plan->block = block;
+  plan->dyn_smem = dyn_smem;
+  plan->need_ent = need_ent;
+  plan->a = a;
+  return PIR_OK;
+}
+
+int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const int32_t *off, const int32_t *var,
+                          const int32_t *lb, const int32_t *ub, const pir_opts &opts, int32_t *out_lb,
+                          int32_t *out_ub, int32_t *out_status, int32_t *out_rounds, pir_stats *stats,
+                          int32_t nwatch = 0, const int32_t *watch = nullptr, int32_t *out_wlb = nullptr,
+                          int32_t *out_wub = nullptr) {
+  int r;
+  NodePlan plan;
+  if ((r = plan_nodes(ctx, b, nnodes, opts, &plan))) return r;
+  EvArgs a = plan.a;
+  const void *kfn = plan.kfn;
+  const int grid = plan.grid, block = plan.block;
+  const size_t dyn_smem = plan.dyn_smem;
+  const bool need_ent = plan.need_ent;
+  const size_t nv = (size_t)ctx->nvars;
   // tightenings, counters, outputs
   const int ntight = off[nnodes];
   if ((r = ensure(ctx, (void **)&b->d_tight, &b->cap_tight, ((size_t)nnodes + 1 + 3 * (size_t)ntight + 8) * sizeof(int))))
@@ -1073,6 +1123,152 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
   return PIR_OK;
 }
 
+// Pinned host buffer of at least `bytes` (a power of two, so that growing
+// batches reallocate, and move the staged graph's buffers, rarely).
+static int ensure_pinned(pirgpu_ctx *ctx, void **ptr, size_t *cap, size_t bytes) {
+  if (*cap >= bytes && *ptr) return PIR_OK;
+  size_t want = 4096;
+  while (want < bytes) want <<= 1;
+  if (*ptr) cudaFreeHost(*ptr);
+  *ptr = nullptr;
+  *cap = 0;
+  if (cudaHostAlloc(ptr, want, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return set_err(ctx, PIR_ENOMEM, "cudaHostAlloc(%zu) failed", want);
+  }
+  *cap = want;
+  return PIR_OK;
+}
+
+static size_t pow2_at_least(size_t bytes) {
+  size_t want = 4096;
+  while (want < bytes) want <<= 1;
+  return want;
+}
+
+// Staged batch layout.  In (int32, host and device alike): watch (nwatch) |
+// off (nnodes + 1) | var | lb | ub (ntight each).  Out (device, copied back
+// whole): execution and narrowing counters (2 x u64) | work counter (4 x
+// int) | NodeOut x nnodes | watched bounds int2 x nnodes x nwatch.
+static size_t stage_in_bytes(int32_t nnodes, int32_t ntight, int32_t nwatch) {
+  return ((size_t)nwatch + (size_t)nnodes + 1 + 3 * (size_t)ntight) * sizeof(int32_t);
+}
+static size_t stage_out_bytes(int32_t nnodes, int32_t nwatch) {
+  return 32 + (size_t)nnodes * sizeof(NodeOut) + (size_t)nnodes * (size_t)nwatch * sizeof(int2);
+}
+
+int nodes_stage(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch, int32_t **in) {
+  BatchState *b = batch(ctx);
+  int r;
+  if ((r = ensure_pinned(ctx, (void **)&b->h_sin, &b->cap_sin, stage_in_bytes(nnodes, ntight, nwatch)))) return r;
+  *in = b->h_sin;
+  return PIR_OK;
+}
+
+static int build_stage_graph(pirgpu_ctx *ctx, BatchState *b, size_t bytes_in, size_t bytes_out,
+                             const cudaKernelNodeParams &kp) {
+  if (b->sgx) cudaGraphExecDestroy(b->sgx);
+  if (b->sg) cudaGraphDestroy(b->sg);
+  b->sgx = nullptr;
+  b->sg = nullptr;
+  b->sg_kfn = nullptr;
+  PIR_CK(cudaGraphCreate(&b->sg, 0));
+  cudaMemsetParams ms;
+  std::memset(&ms, 0, sizeof(ms));
+  ms.dst = b->d_sout;
+  ms.value = 0;
+  ms.elementSize = 4;
+  ms.width = 8;  // the counters: 32 bytes
+  ms.height = 1;
+  cudaGraphNode_t clear, e0, e1;
+  PIR_CK(cudaGraphAddMemsetNode(&clear, b->sg, nullptr, 0, &ms));
+  PIR_CK(cudaGraphAddMemcpyNode1D(&b->sg_in, b->sg, &clear, 1, b->d_sin, b->h_sin, bytes_in, cudaMemcpyHostToDevice));
+  PIR_CK(cudaGraphAddEventRecordNode(&e0, b->sg, &b->sg_in, 1, ctx->ev0));
+  PIR_CK(cudaGraphAddKernelNode(&b->sg_kernel, b->sg, &e0, 1, &kp));
+  PIR_CK(cudaGraphAddEventRecordNode(&e1, b->sg, &b->sg_kernel, 1, ctx->ev1));
+  PIR_CK(cudaGraphAddMemcpyNode1D(&b->sg_out, b->sg, &e1, 1, b->h_sout, b->d_sout, bytes_out, cudaMemcpyDeviceToHost));
+  PIR_CK(cudaGraphInstantiate(&b->sgx, b->sg, 0));
+  b->sg_kfn = kp.func;
+  b->sg_bufs[0] = b->h_sin;
+  b->sg_bufs[1] = b->h_sout;
+  b->sg_bufs[2] = b->d_sin;
+  b->sg_bufs[3] = b->d_sout;
+  return PIR_OK;
+}
+
+int nodes_run_staged(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch, const pir_opts &opts,
+                     int32_t *out_status, const int2 **wout, pir_stats *stats) {
+  BatchState *b = batch(ctx);
+  int r;
+  NodePlan plan;
+  if ((r = plan_nodes(ctx, b, nnodes, opts, &plan))) return r;
+  const size_t bytes_in = stage_in_bytes(nnodes, ntight, nwatch), bytes_out = stage_out_bytes(nnodes, nwatch);
+  if ((r = ensure(ctx, &b->d_sin, &b->cap_dsin, pow2_at_least(bytes_in)))) return r;
+  if ((r = ensure(ctx, &b->d_sout, &b->cap_dsout, pow2_at_least(bytes_out)))) return r;
+  if ((r = ensure_pinned(ctx, (void **)&b->h_sout, &b->cap_sout, bytes_out))) return r;
+  EvArgs a = plan.a;
+  int32_t *din = static_cast<int32_t *>(b->d_sin);
+  char *dout = static_cast<char *>(b->d_sout);
+  a.nwatch = nwatch;
+  a.watch = nwatch > 0 ? din : nullptr;
+  a.off = din + nwatch;
+  a.var = a.off + nnodes + 1;
+  a.lb = a.var + ntight;
+  a.ub = a.lb + ntight;
+  a.nnodes = nnodes;
+  a.execs = reinterpret_cast<unsigned long long *>(dout);
+  a.narrowed = a.execs + 1;
+  a.next = reinterpret_cast<int *>(dout + 16);
+  a.out = reinterpret_cast<NodeOut *>(dout + 32);
+  a.out_watch = nwatch > 0 ? reinterpret_cast<int2 *>(dout + 32 + (size_t)nnodes * sizeof(NodeOut)) : nullptr;
+  a.out_store = nullptr;
+  a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
+  void *kargs[] = {&a};
+  cudaKernelNodeParams kp;
+  std::memset(&kp, 0, sizeof(kp));
+  kp.func = const_cast<void *>(plan.kfn);
+  kp.gridDim = dim3(plan.grid);
+  kp.blockDim = dim3(plan.block);
+  kp.sharedMemBytes = (unsigned)plan.dyn_smem;
+  kp.kernelParams = kargs;
+  if (plan.need_ent) {
+    k_entailed<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(b->d_bc4, ctx->n, ctx->d_store, b->d_ent);
+    PIR_CK(cudaGetLastError());
+  }
+  const bool moved = b->sg_bufs[0] != b->h_sin || b->sg_bufs[1] != b->h_sout || b->sg_bufs[2] != b->d_sin ||
+                     b->sg_bufs[3] != b->d_sout;
+  if (!b->sgx || moved || b->sg_kfn != plan.kfn) {
+    if ((r = build_stage_graph(ctx, b, bytes_in, bytes_out, kp))) return r;
+  } else {
+    PIR_CK(cudaGraphExecMemcpyNodeSetParams1D(b->sgx, b->sg_in, b->d_sin, b->h_sin, bytes_in, cudaMemcpyHostToDevice));
+    PIR_CK(cudaGraphExecKernelNodeSetParams(b->sgx, b->sg_kernel, &kp));
+    PIR_CK(cudaGraphExecMemcpyNodeSetParams1D(b->sgx, b->sg_out, b->h_sout, b->d_sout, bytes_out,
+                                              cudaMemcpyDeviceToHost));
+  }
+  PIR_CK(cudaGraphLaunch(b->sgx, ctx->stream));
+  PIR_CK(cudaStreamSynchronize(ctx->stream));
+  b->ent_store_version = ctx->store_version;
+  b->ent_bc_version = ctx->bytecode_version;
+  const unsigned long long *cnt = reinterpret_cast<const unsigned long long *>(b->h_sout);
+  const NodeOut *no = reinterpret_cast<const NodeOut *>(b->h_sout + 32);
+  pir_stats st;
+  std::memset(&st, 0, sizeof(st));
+  PIR_CK(cudaEventElapsedTime(&st.device_ms, ctx->ev0, ctx->ev1));
+  int worst = PIR_OK;
+  for (int j = 0; j < nnodes; ++j) {
+    out_status[j] = no[j].status;
+    st.rounds = std::max<int64_t>(st.rounds, no[j].rounds);
+    if (no[j].status == PIR_TIMEOUT) worst = PIR_TIMEOUT;
+  }
+  st.executions = (int64_t)cnt[0];
+  st.narrowed = (int64_t)cnt[1];
+  st.status = worst;
+  if (stats) *stats = st;
+  *wout = reinterpret_cast<const int2 *>(b->h_sout + 32 + (size_t)nnodes * sizeof(NodeOut));
+  return PIR_OK;
+}
+
 }  // namespace pirgpu
 
 using namespace pirgpu;
@@ -1149,6 +1345,10 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   const size_t stage_ints = (size_t)std::max<long long>(nchunks, 1) * 16;
   if (b->cap_stage < stage_ints) {
     if (b->h_stage) cudaFreeHost(b->h_stage);
+  if (b->sgx) cudaGraphExecDestroy(b->sgx);
+  if (b->sg) cudaGraphDestroy(b->sg);
+  if (b->h_sin) cudaFreeHost(b->h_sin);
+  if (b->h_sout) cudaFreeHost(b->h_sout);
     b->h_stage = nullptr;
     b->cap_stage = 0;
     if (cudaMallocHost(&b->h_stage, stage_ints * sizeof(int)) != cudaSuccess) {

@@ -3,7 +3,10 @@
 // (branch, propagate with deduce, snapshot / restore: pir.hpp:857-870), with
 // the children of up to `batch` open nodes propagated in one launch of the
 // event node kernel.  Host code: node bookkeeping and branching; every
-// propagation runs on the GPU.
+// propagation runs on the GPU.  A batch's tightenings (the bisections on each
+// node's path) are written straight into pinned staging and the batch runs
+// as one CUDA graph (clear the counters, copy in, node kernel, copy out),
+// updated in place from batch to batch.
 #include <algorithm>
 #include <climits>
 #include <cstring>
@@ -18,6 +21,11 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
                           const int32_t *lb, const int32_t *ub, const pir_opts &opts, int32_t *out_lb,
                           int32_t *out_ub, int32_t *out_status, int32_t *out_rounds, pir_stats *stats,
                           int32_t nwatch, const int32_t *watch, int32_t *out_wlb, int32_t *out_wub);
+// Staged batches (pir_batch.cu): pinned inputs filled in place, one graph
+// launch per batch, outputs read from pinned memory.
+int nodes_stage(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch, int32_t **in);
+int nodes_run_staged(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch, const pir_opts &opts,
+                     int32_t *out_status, const int2 **wout, pir_stats *stats);
 }  // namespace pirgpu
 
 using namespace pirgpu;
@@ -115,6 +123,17 @@ extern "C" int pir_search(pirgpu_ctx *ctx, int32_t ndec, const int32_t *dec, con
   std::memset(&no, 0, sizeof(no));
   int rc = PIR_OK;
   bool done = false;
+  // the base at its fixpoint first; a failed or empty base takes the plain
+  // path (every node is the base met with its tightenings)
+  if (!ctx->failed && ctx->n > 0 && !ctx->at_fixpoint) {
+    rc = pir_fixpoint(ctx, &no, nullptr);
+    if (rc != PIR_OK && rc != PIR_FAILED) return rc;
+    rc = PIR_OK;
+  }
+  const bool staged = !ctx->failed && ctx->n > 0;
+  pir_opts eo = no;
+  eo.sched = PIR_SCHED_EVENTS;
+  const int2 *wout = nullptr;
   while (!open.empty() && !done) {
     int64_t take = std::min<int64_t>(bmax, (int64_t)open.size());
     if (opts.max_nodes > 0) take = std::min<int64_t>(take, opts.max_nodes - st.nodes);
@@ -126,25 +145,53 @@ extern "C" int pir_search(pirgpu_ctx *ctx, int32_t ndec, const int32_t *dec, con
     std::vector<int> ids((size_t)take);
     for (int64_t i = 0; i < take; ++i) ids[(size_t)i] = open[open.size() - 1 - (size_t)i];
     open.resize(open.size() - (size_t)take);
-    off.assign(1, 0);
-    tv.clear();
-    tl.clear();
-    tu.clear();
-    for (int id : ids) {
-      for (int p = id; p >= 0 && pool[(size_t)p].var >= 0; p = pool[(size_t)p].parent) {
-        tv.push_back(pool[(size_t)p].var);
-        tl.push_back(pool[(size_t)p].lb);
-        tu.push_back(pool[(size_t)p].ub);
-      }
-      off.push_back((int32_t)tv.size());
-    }
     status.assign((size_t)take, 0);
-    wlb.assign((size_t)take * ndec, 0);
-    wub.assign((size_t)take * ndec, 0);
     pir_stats ns;
-    rc = pir_fixpoint_nodes_watch(ctx, (int32_t)take, off.data(), tv.data(), tl.data(), tu.data(), &no, ndec, dec,
-                                  wlb.data(), wub.data(), status.data(), nullptr, &ns);
+    if (staged) {
+      // a node's path holds one bisection per level
+      int64_t ntight = 0;
+      for (int id : ids) ntight += pool[(size_t)id].depth;
+      int32_t *in = nullptr;
+      if ((rc = nodes_stage(ctx, (int32_t)take, (int32_t)ntight, ndec, &in))) break;
+      int32_t *w = in, *o = w + ndec, *v = o + take + 1, *l = v + ntight, *u = l + ntight;
+      std::copy(dec, dec + ndec, w);
+      int64_t t = 0;
+      o[0] = 0;
+      for (int64_t i = 0; i < take; ++i) {
+        for (int p = ids[(size_t)i]; p >= 0 && pool[(size_t)p].var >= 0; p = pool[(size_t)p].parent, ++t) {
+          v[t] = pool[(size_t)p].var;
+          l[t] = pool[(size_t)p].lb;
+          u[t] = pool[(size_t)p].ub;
+        }
+        o[i + 1] = (int32_t)t;
+      }
+      rc = nodes_run_staged(ctx, (int32_t)take, (int32_t)ntight, ndec, eo, status.data(), &wout, &ns);
+    } else {
+      off.assign(1, 0);
+      tv.clear();
+      tl.clear();
+      tu.clear();
+      for (int id : ids) {
+        for (int p = id; p >= 0 && pool[(size_t)p].var >= 0; p = pool[(size_t)p].parent) {
+          tv.push_back(pool[(size_t)p].var);
+          tl.push_back(pool[(size_t)p].lb);
+          tu.push_back(pool[(size_t)p].ub);
+        }
+        off.push_back((int32_t)tv.size());
+      }
+      wlb.assign((size_t)take * ndec, 0);
+      wub.assign((size_t)take * ndec, 0);
+      rc = pir_fixpoint_nodes_watch(ctx, (int32_t)take, off.data(), tv.data(), tl.data(), tu.data(), &no, ndec, dec,
+                                    wlb.data(), wub.data(), status.data(), nullptr, &ns);
+    }
     if (rc != PIR_OK) break;
+    // watched bounds of node i, decision k
+    auto lo = [&](int64_t i, int k) -> int32_t {
+      return staged ? wout[(size_t)i * ndec + k].x : wlb[(size_t)i * ndec + k];
+    };
+    auto hi = [&](int64_t i, int k) -> int32_t {
+      return staged ? wout[(size_t)i * ndec + k].y : wub[(size_t)i * ndec + k];
+    };
     st.nodes += take;
     st.launches += 1;
     st.device_ms += ns.device_ms;
@@ -157,12 +204,12 @@ extern "C" int pir_search(pirgpu_ctx *ctx, int32_t ndec, const int32_t *dec, con
         ++st.failures;
         continue;
       }
-      const int32_t *l = wlb.data() + (size_t)i * ndec, *u = wub.data() + (size_t)i * ndec;
       int best = -1;
       long long best_w = LLONG_MAX;
       for (int k = 0; k < ndec; ++k) {
-        if (l[k] >= u[k]) continue;
-        const long long w = (long long)u[k] - (long long)l[k];
+        const int32_t lk = lo(i, k), uk = hi(i, k);
+        if (lk >= uk) continue;
+        const long long w = (long long)uk - (long long)lk;
         if (opts.order == PIR_ORDER_INPUT) {
           best = k;
           break;
@@ -173,7 +220,8 @@ extern "C" int pir_search(pirgpu_ctx *ctx, int32_t ndec, const int32_t *dec, con
         }
       }
       if (best < 0) {
-        if (opts.max_solutions > 0) std::copy(l, l + ndec, out_solutions + (size_t)st.solutions * ndec);
+        if (opts.max_solutions > 0)
+          for (int k = 0; k < ndec; ++k) out_solutions[(size_t)st.solutions * ndec + k] = lo(i, k);
         ++st.solutions;
         if (opts.max_solutions > 0 && st.solutions >= opts.max_solutions) done = true;
         continue;
@@ -185,12 +233,12 @@ extern "C" int pir_search(pirgpu_ctx *ctx, int32_t ndec, const int32_t *dec, con
     for (int64_t i = take - 1; i >= 0; --i) {
       const int k = branch[(size_t)i];
       if (k < 0) continue;
-      const int32_t lo = wlb[(size_t)i * ndec + k], hi = wub[(size_t)i * ndec + k];
-      const int32_t mid = (int32_t)((long long)lo + ((long long)hi - (long long)lo) / 2);
+      const int32_t lk = lo(i, k), hk = hi(i, k);
+      const int32_t mid = (int32_t)((long long)lk + ((long long)hk - (long long)lk) / 2);
       const int parent = ids[(size_t)i], depth = pool[(size_t)parent].depth + 1;
-      pool.push_back(SearchNode{parent, dec[k], mid + 1, hi, depth});
+      pool.push_back(SearchNode{parent, dec[k], mid + 1, hk, depth});
       open.push_back((int)pool.size() - 1);
-      pool.push_back(SearchNode{parent, dec[k], lo, mid, depth});
+      pool.push_back(SearchNode{parent, dec[k], lk, mid, depth});
       open.push_back((int)pool.size() - 1);
     }
   }
