@@ -83,3 +83,49 @@ def test_pc_kinds_match_header_builder_and_oracle():
             assert getattr(P, name) == v, name
         assert int(re.search(r"ORC_PC_%s = (\d+)" % name, orc).group(1)) == v, name
     assert int(re.search(r"#define PC_MAX_DEPTH (\d+)", src).group(1)) == P.MAX_DEPTH
+
+
+def _struct_fields(header, name):
+    src = open(os.path.join(ROOT, "include", header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), src, flags=re.S).group(1)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if decl:
+            m = re.match(r"[A-Za-z_0-9 ]+?\s+([a-z_0-9]+)(?:\[(\d+)\])?$", decl)
+            fields.append(m.group(1))
+    return fields
+
+
+def test_python_structs_match_header_layout(tmp_path):
+    """The ctypes mirrors of the C structs: same fields, offsets and sizes as
+    the C compiler lays them out from include/pirgpu.h."""
+    import shutil
+    import subprocess
+    import pirgpu
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    pairs = [("pir_opts", pirgpu.Opts), ("pir_stats", pirgpu.Stats), ("pir_search_opts", pirgpu.SearchOpts),
+             ("pir_search_stats", pirgpu.SearchStats)]
+    lines = ['#include <stdio.h>', '#include "pirgpu.h"', "int main(void) {"]
+    for cname, _ in pairs:
+        lines.append('  printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f in _struct_fields("pirgpu.h", cname):
+            lines.append('  printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines.append("  return 0;\n}")
+    c = tmp_path / "layout.c"
+    c.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        s, f, v = line.split()
+        got[(s, f)] = int(v)
+    for cname, py in pairs:
+        assert [f for f, _ in py._fields_] == _struct_fields("pirgpu.h", cname), cname
+        assert ctypes.sizeof(py) == got[(cname, "sizeof")], cname
+        for f, _ in py._fields_:
+            assert getattr(py, f).offset == got[(cname, f)], (cname, f)
