@@ -16,10 +16,12 @@
 //   int_times int_div int_tdiv int_fdiv int_cdiv int_ediv int_mod int_tmod
 //   int_fmod int_emod int_min int_max int_abs int_negate,
 //   int_lin_eq int_lin_ne int_lin_le int_lin_lt int_lin_ge (+ _reif),
+//   bool_lin_eq bool_lin_le, array_int_maximum array_int_minimum,
 //   bool_eq bool_ne bool_le bool_lt bool_not bool_and bool_or bool_xor
-//   bool_clause bool2int array_bool_and array_bool_or (+ bool_*_reif),
-//   set_in set_in_reif, array_int_element array_var_int_element
-//   array_bool_element array_var_bool_element.
+//   bool_clause bool2int array_bool_and array_bool_or array_bool_xor
+//   (+ bool_*_reif), set_in set_in_reif, array_int_element
+//   array_var_int_element array_bool_element array_var_bool_element; every
+//   reifiable one also half-reified, f_imp(args..., r): r -> f(args...).
 // Decompositions: x < y is 0 = (y <= x); x != y is 0 = (x == y);
 // x = y - z is y = x + z; -x is 0 = t + x; |x| = max(x, -x); integer
 // modulo m of y by z is q = y div z, p = q * z, y = p + m; a linear sum is a
@@ -492,6 +494,22 @@ class Compiler {
       out = rr;
       return true;
     }
+    const bool imp_form = f.size() > 4 && f.compare(f.size() - 4, 4, "_imp") == 0;
+    if (imp_form) {
+      // f_imp(args..., r): r -> f(args...), as r <= (f reified into a fresh 0/1 variable)
+      if (A.empty()) return error(f + ": no arguments");
+      int rr;
+      if (!value(A.back(), rr)) return false;
+      Expr inner = e;
+      inner.id = f.substr(0, f.size() - 4);
+      inner.args.pop_back();
+      const int t = boolvar();
+      int dummy;
+      if (!call(inner, t, dummy)) return false;
+      cmp_le(rr, t, -1);
+      out = rr;
+      return true;
+    }
     // boolean functions: the variable they are reified into (-1: imposed)
     auto reified = [&](int &rv) {
       rv = r >= 0 ? r : (r == VALUE ? boolvar() : -1);
@@ -566,15 +584,16 @@ class Compiler {
       out = c;
       return true;
     }
-    if (g == "int_lin_eq" || g == "int_lin_ne" || g == "int_lin_le" || g == "int_lin_lt" || g == "int_lin_ge") {
+    if (g == "int_lin_eq" || g == "int_lin_ne" || g == "int_lin_le" || g == "int_lin_lt" || g == "int_lin_ge" ||
+        g == "bool_lin_eq" || g == "bool_lin_le") {
       if (!arity(3)) return false;
       int s;
       if (!linear(A[0], A[1], s) || !value(A[2], c)) return false;
       int rv;
       reified(rv);
-      if (g == "int_lin_eq") cmp_eq(s, c, rv);
+      if (g == "int_lin_eq" || g == "bool_lin_eq") cmp_eq(s, c, rv);
       else if (g == "int_lin_ne") cmp_ne(s, c, rv);
-      else if (g == "int_lin_le") cmp_le(s, c, rv);
+      else if (g == "int_lin_le" || g == "bool_lin_le") cmp_le(s, c, rv);
       else if (g == "int_lin_lt") cmp_lt(s, c, rv);
       else cmp_le(c, s, rv);
       out = rv;
@@ -624,6 +643,46 @@ class Compiler {
       prop(g == "bool_and" ? MIN : MAX, t, a, b);
       if (rv < 0) cmp_eq(t, constant(1), -1);
       out = t;
+      return true;
+    }
+    if (g == "array_int_maximum" || g == "array_int_minimum") {
+      // m = max (min) of xs: a chain of MAX (MIN) ending in m
+      if (r >= 0) return error(f + " is not a boolean function");
+      if (!arity(2)) return false;
+      int m;
+      std::vector<int> xs;
+      if (!value(A[0], m) || !values(A[1], xs)) return false;
+      if (xs.empty()) return error(f + ": empty array");
+      const int32_t op = g == "array_int_maximum" ? MAX : MIN;
+      if (xs.size() == 1) cmp_eq(m, xs[0], -1);
+      int acc = xs[0];
+      for (size_t k = 1; k < xs.size(); ++k) {
+        const int t = k + 1 == xs.size() ? m : fresh(Itv::top());
+        prop(op, t, acc, xs[k]);
+        acc = t;
+      }
+      out = m;
+      return true;
+    }
+    if (g == "array_bool_xor") {
+      // odd parity: p_k = (p_{k-1} != x_k)
+      std::vector<int> xs;
+      if (!arity(1) || !values(A[0], xs)) return false;
+      int rv;
+      reified(rv);
+      int p = xs.empty() ? constant(0) : xs[0];
+      for (size_t k = 1; k < xs.size(); ++k) {
+        const int t = boolvar();
+        cmp_ne(p, xs[k], t);
+        p = t;
+      }
+      if (rv >= 0) {
+        cmp_eq(rv, p, -1);
+        out = rv;
+      } else {
+        cmp_eq(p, constant(1), -1);
+        out = p;
+      }
       return true;
     }
     if (g == "array_bool_and" || g == "array_bool_or") {

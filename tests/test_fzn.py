@@ -63,6 +63,13 @@ def test_errors_are_reported(fzn):
         fzn("var int: x; constraint int_le(x, y);")
     with pytest.raises(ValueError, match="FlatZinc"):
         fzn("var int x;")
+    # half reification of functions that are not boolean
+    with pytest.raises(ValueError, match="not a boolean function"):
+        fzn("var 0..3: x; var 0..3: y; var 0..6: z; var bool: r; constraint int_plus_imp(x, y, z, r);")
+    with pytest.raises(ValueError, match="not a boolean function"):
+        fzn("var 0..3: m; var 0..3: x; var bool: r; constraint array_int_maximum_imp(m, [x], r);")
+    with pytest.raises(ValueError, match="empty array"):
+        fzn("var 0..3: m; constraint array_int_minimum(m, []);")
 
 
 def _search_oracle(oracle, dom, props, dec):
@@ -126,3 +133,102 @@ def test_send_more_money_and_queens_gpu(fzn):
     ctx = _gpu_ctx(dom, props)
     status, sols, st = ctx.search([names[q] for q in qs], max_solutions=100)
     assert st["solutions"] == 92
+
+
+# -------------------------------------------------- builtins, exhaustively ----
+
+def _tdiv(a, b):
+    q = abs(a) // abs(b)
+    return q if (a >= 0) == (b > 0) else -q
+
+
+def _cdiv(a, b):
+    return -((-a) // b)
+
+
+def _ediv(a, b):
+    return (a - a % abs(b)) // b
+
+
+_DIVS = {"int_div": _tdiv, "int_tdiv": _tdiv, "int_fdiv": lambda a, b: a // b, "int_cdiv": _cdiv,
+         "int_ediv": _ediv}
+_MODS = {"int_mod": _tdiv, "int_tmod": _tdiv, "int_fmod": lambda a, b: a // b, "int_cmod": _cdiv,
+         "int_emod": _ediv}
+
+BUILTINS = [
+    ("array_int_maximum", "var -3..3: m; var -2..2: x; var -2..2: y; var -2..2: z; "
+     "constraint array_int_maximum(m, [x, y, z]);", "m x y z", lambda m, x, y, z: m == max(x, y, z)),
+    ("array_int_minimum", "var -3..3: m; var -2..2: x; var -2..2: y; var 0..2: z; "
+     "constraint array_int_minimum(m, [x, y, z]);", "m x y z", lambda m, x, y, z: m == min(x, y, z)),
+    ("array_int_maximum_one", "var -3..3: m; var -2..2: x; constraint array_int_maximum(m, [x]);", "m x",
+     lambda m, x: m == x),
+    ("bool_lin_eq", "var bool: a; var bool: b; var bool: c; constraint bool_lin_eq([2, 3, -1], [a, b, c], 2);",
+     "a b c", lambda a, b, c: 2 * a + 3 * b - c == 2),
+    ("bool_lin_le", "var bool: a; var bool: b; var bool: c; constraint bool_lin_le([1, 1, 1], [a, b, c], 1);",
+     "a b c", lambda a, b, c: a + b + c <= 1),
+    ("array_bool_xor", "var bool: a; var bool: b; var bool: c; var bool: d; "
+     "constraint array_bool_xor([a, b, c, d]);", "a b c d", lambda a, b, c, d: (a + b + c + d) % 2 == 1),
+    ("int_lin_le_imp", "var -2..2: x; var -2..2: y; var bool: r; constraint int_lin_le_imp([1, 2], [x, y], 1, r);",
+     "x y r", lambda x, y, r: not r or x + 2 * y <= 1),
+    ("int_lin_ne_reif", "var -2..2: x; var -2..2: y; var bool: r; "
+     "constraint int_lin_ne_reif([1, -1], [x, y], 1, r);", "x y r", lambda x, y, r: r == (x - y != 1)),
+    ("int_eq_imp", "var -2..2: x; var -2..2: y; var bool: r; constraint int_eq_imp(x, y, r);", "x y r",
+     lambda x, y, r: not r or x == y),
+    ("int_ne_imp", "var -2..2: x; var -2..2: y; var bool: r; constraint int_ne_imp(x, y, r);", "x y r",
+     lambda x, y, r: not r or x != y),
+    ("int_lt_imp", "var -2..2: x; var -2..2: y; var bool: r; constraint int_lt_imp(x, y, r);", "x y r",
+     lambda x, y, r: not r or x < y),
+    ("set_in_imp", "var -3..3: x; var bool: r; constraint set_in_imp(x, {-1, 2}, r);", "x r",
+     lambda x, r: not r or x in (-1, 2)),
+    ("bool_clause_imp", "var bool: a; var bool: b; var bool: c; var bool: r; "
+     "constraint bool_clause_imp([a, b], [c], r);", "a b c r", lambda a, b, c, r: not r or a or b or not c),
+    ("int_times", "var -3..3: x; var -3..3: y; var -9..9: z; constraint int_times(x, y, z);", "x y z",
+     lambda x, y, z: z == x * y),
+    ("int_abs", "var -3..3: x; var -3..3: y; constraint int_abs(x, y);", "x y", lambda x, y: y == abs(x)),
+    ("int_max_reif_nested", "var -2..2: x; var -2..2: y; var bool: r; "
+     "constraint int_le_reif(int_max(x, y), 1, r);", "x y r", lambda x, y, r: r == (max(x, y) <= 1)),
+] + [
+    ("%s_%s" % (f, sign), "var -7..7: x; var %s: y; var -8..8: q; constraint %s(x, y, q);" % (dom, f), "x y q",
+     (lambda d: lambda x, y, q: q == d(x, y))(d))
+    for f, d in _DIVS.items() for sign, dom in (("pos", "1..3"), ("neg", "-3..-1"))
+] + [
+    ("%s_%s" % (f, sign), "var -7..7: x; var %s: y; var -3..3: m; constraint %s(x, y, m);" % (dom, f), "x y m",
+     (lambda d: lambda x, y, m: m == x - y * d(x, y))(d))
+    for f, d in _MODS.items() for sign, dom in (("pos", "1..3"), ("neg", "-3..-1"))
+]
+
+
+@pytest.mark.parametrize("case", BUILTINS, ids=[c[0] for c in BUILTINS])
+def test_builtin_solutions_match_brute_force(case, fzn, oracle):
+    """Every solution of the compiled model (the oracle's search over the
+    user variables) and nothing else satisfies the builtin's definition."""
+    import itertools
+    name, text, users, pred = case
+    users = users.split()
+    dom, props, names = fzn(text)
+    dec = [names[u] for u in users]
+    want = sorted(t for t in itertools.product(*(range(dom[v][0], dom[v][1] + 1) for v in dec)) if pred(*t))
+    assert len(props) > 0
+    s = np.ascontiguousarray(dom, np.int32)
+    _, perm = oracle.install(props[:, 0], props[:, 1], props[:, 2], props[:, 3], s)
+    p = props[perm]
+    _, sols, _ = oracle.search(p[:, 0], p[:, 1], p[:, 2], p[:, 3], s, dec, max_solutions=100_000)
+    got = sorted(tuple(int(v) for v in row) for row in sols)
+    assert want and got == want, name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", BUILTINS, ids=[c[0] for c in BUILTINS])
+def test_builtin_solutions_match_brute_force_gpu(case, fzn):
+    import itertools
+    import pirgpu
+    name, text, users, pred = case
+    users = users.split()
+    dom, props, names = fzn(text)
+    dec = [names[u] for u in users]
+    want = sorted(t for t in itertools.product(*(range(dom[v][0], dom[v][1] + 1) for v in dec)) if pred(*t))
+    ctx = _gpu_ctx(dom, props)
+    status, sols, st = ctx.search(dec, max_solutions=100_000)
+    assert status == pirgpu.OK
+    got = sorted(tuple(int(v) for v in row) for row in sols)
+    assert got == want, name
