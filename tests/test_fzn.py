@@ -188,6 +188,59 @@ BUILTINS = [
     ("int_max_reif_nested", "var -2..2: x; var -2..2: y; var bool: r; "
      "constraint int_le_reif(int_max(x, y), 1, r);", "x y r", lambda x, y, r: r == (max(x, y) <= 1)),
 ] + [
+    # comparisons, imposed and reified
+    ("%s%s" % (f, "_reif" if reif else ""),
+     "var -2..2: x; var -2..2: y;%s constraint %s%s(x, y%s);" % (
+         " var bool: r;" if reif else "", f, "_reif" if reif else "", ", r" if reif else ""),
+     "x y r" if reif else "x y",
+     (lambda c, reif: (lambda x, y, r: r == c(x, y)) if reif else (lambda x, y: c(x, y)))(c, reif))
+    for f, c in (("int_eq", lambda x, y: x == y), ("int_ne", lambda x, y: x != y), ("int_le", lambda x, y: x <= y),
+                 ("int_lt", lambda x, y: x < y), ("int_ge", lambda x, y: x >= y), ("int_gt", lambda x, y: x > y))
+    for reif in (False, True)
+] + [
+    ("%s%s" % (f, "_reif" if reif else ""),
+     "var bool: a; var bool: b;%s constraint %s%s(a, b%s);" % (
+         " var bool: r;" if reif else "", f, "_reif" if reif else "", ", r" if reif else ""),
+     "a b r" if reif else "a b",
+     (lambda c, reif: (lambda a, b, r: r == c(a, b)) if reif else (lambda a, b: c(a, b)))(c, reif))
+    for f, c in (("bool_eq", lambda a, b: a == b), ("bool_ne", lambda a, b: a != b), ("bool_le", lambda a, b: a <= b),
+                 ("bool_lt", lambda a, b: a < b), ("bool_and", lambda a, b: bool(a and b)),
+                 ("bool_or", lambda a, b: bool(a or b)), ("bool_xor", lambda a, b: a != b))
+    for reif in (False, True)
+] + [
+    ("bool_not", "var bool: a; var bool: b; constraint bool_not(a, b);", "a b", lambda a, b: b == 1 - a),
+    ("bool2int", "var bool: a; var 0..3: i; constraint bool2int(a, i);", "a i", lambda a, i: i == a),
+    ("bool_clause", "var bool: a; var bool: b; var bool: c; constraint bool_clause([a, b], [c]);", "a b c",
+     lambda a, b, c: bool(a or b or not c)),
+    ("bool_clause_reif", "var bool: a; var bool: b; var bool: r; constraint bool_clause_reif([a], [b], r);",
+     "a b r", lambda a, b, r: r == bool(a or not b)),
+    ("array_bool_and_reif", "var bool: a; var bool: b; var bool: c; var bool: r; "
+     "constraint array_bool_and([a, b, c], r);", "a b c r", lambda a, b, c, r: r == bool(a and b and c)),
+    ("array_bool_or", "var bool: a; var bool: b; var bool: c; constraint array_bool_or([a, b, c], true);",
+     "a b c", lambda a, b, c: bool(a or b or c)),
+    ("set_in", "var -3..3: x; constraint set_in(x, {-2, 0, 3});", "x", lambda x: x in (-2, 0, 3)),
+    ("set_in_range_reif", "var -3..3: x; var bool: r; constraint set_in_reif(x, -1..1, r);", "x r",
+     lambda x, r: r == (-1 <= x <= 1)),
+    ("array_int_element", "var 1..4: i; var -5..5: x; constraint array_int_element(i, [3, -1, 4, 1], x);", "i x",
+     lambda i, x: x == [3, -1, 4, 1][i - 1]),
+    ("array_var_int_element", "var 1..3: i; var 0..2: a; var 0..2: b; var 0..2: c; var 0..2: x; "
+     "constraint array_var_int_element(i, [a, b, c], x);", "i a b c x",
+     lambda i, a, b, c, x: x == [a, b, c][i - 1]),
+    ("array_var_bool_element", "var 1..2: i; var bool: a; var bool: b; var bool: x; "
+     "constraint array_var_bool_element(i, [a, b], x);", "i a b x", lambda i, a, b, x: x == [a, b][i - 1]),
+    ("int_lin_eq", "var -2..2: x; var -2..2: y; var -2..2: z; constraint int_lin_eq([2, -3, 1], [x, y, z], 1);",
+     "x y z", lambda x, y, z: 2 * x - 3 * y + z == 1),
+    ("int_lin_lt_reif", "var -2..2: x; var -2..2: y; var bool: r; "
+     "constraint int_lin_lt_reif([1, 1], [x, y], 0, r);", "x y r", lambda x, y, r: r == (x + y < 0)),
+    ("int_lin_ge", "var -2..2: x; var -2..2: y; constraint int_lin_ge([3, -1], [x, y], 2);", "x y",
+     lambda x, y: 3 * x - y >= 2),
+    ("int_plus_minus_negate", "var -3..3: x; var -3..3: y; var -6..6: s; var -6..6: d; var -3..3: n; "
+     "constraint int_plus(x, y, s); constraint int_minus(x, y, d); constraint int_negate(x, n);",
+     "x y s d n", lambda x, y, s, d, n: s == x + y and d == x - y and n == -x),
+    ("int_min_max", "var -2..2: x; var -2..2: y; var -2..2: lo; var -2..2: hi; "
+     "constraint int_min(x, y, lo); constraint int_max(x, y, hi);", "x y lo hi",
+     lambda x, y, lo, hi: lo == min(x, y) and hi == max(x, y)),
+] + [
     ("%s_%s" % (f, sign), "var -7..7: x; var %s: y; var -8..8: q; constraint %s(x, y, q);" % (dom, f), "x y q",
      (lambda d: lambda x, y, q: q == d(x, y))(d))
     for f, d in _DIVS.items() for sign, dom in (("pos", "1..3"), ("neg", "-3..-1"))
