@@ -22,9 +22,12 @@
 //   int_lin_eq int_lin_ne int_lin_le int_lin_lt int_lin_ge int_lin_gt: a
 //                              binary sum for two terms, an n-ary one beyond
 //                              (pc.hpp:278-297)
+//   bool_lin_eq bool_lin_le:   as int_lin_*
+//   array_int_maximum array_int_minimum: m == max (min) chain of the terms
 //   bool_and bool_or bool_xor bool_not, array_bool_and array_bool_or,
-//   bool_clause:               connectives, clauses as right-nested
+//   array_bool_xor, bool_clause: connectives, clauses as right-nested
 //                              disjunctions of literals (binarize, pc.hpp:467-476)
+//   f_imp(args..., r):         r => f(args...) for every boolean f
 //   set_in (+ _reif):          a range is a store bound; a set is a
 //                              disjunction of its runs (x == v, or
 //                              lo <= x and x <= hi)
@@ -182,10 +185,11 @@ class PcCompiler {
                                   "bool_lt", "bool_eq", "bool_ne", "bool_and", "bool_or", "bool_xor",
                                   "bool_not", "bool_clause", "array_bool_and", "array_bool_or", "set_in",
                                   "int_lin_eq", "int_lin_ne", "int_lin_le", "int_lin_lt", "int_lin_ge",
-                                  "int_lin_gt"};
+                                  "int_lin_gt", "bool_lin_eq", "bool_lin_le", "array_bool_xor"};
     for (const char *n : names)
       if (f == n) return true;
-    return f.size() > 5 && f.compare(f.size() - 5, 5, "_reif") == 0;
+    return (f.size() > 5 && f.compare(f.size() - 5, 5, "_reif") == 0) ||
+           (f.size() > 4 && f.compare(f.size() - 4, 4, "_imp") == 0);
   }
   bool is_predicate(const Expr &e) const { return e.kind == Expr::CALL && is_bool_fn(e.id); }
 
@@ -330,6 +334,16 @@ class PcCompiler {
       out = F::make_bicond(r, g);
       return true;
     }
+    if (f.size() > 4 && f.compare(f.size() - 4, 4, "_imp") == 0) {  // r => f(args)
+      if (A.empty()) return error(f + ": no arguments");
+      Expr inner = e;
+      inner.id = f.substr(0, f.size() - 4);
+      inner.args.pop_back();
+      F r, g;
+      if (!formula(A.back(), r) || !formula(inner, g)) return false;
+      out = F::make_imply(r, g);
+      return true;
+    }
     const bool cmp = f == "int_le" || f == "int_lt" || f == "int_ge" || f == "int_gt" || f == "int_eq" ||
                      f == "int_ne" || f == "bool_le" || f == "bool_lt" || f == "bool_eq" || f == "bool_ne";
     if (cmp || f == "bool_and" || f == "bool_or" || f == "bool_xor") {
@@ -417,11 +431,40 @@ class PcCompiler {
       if (A.size() != 2 || !term(A[0], x)) return error("set_in: two arguments");
       return member(x, A[1], out);
     }
-    if (f.compare(0, 8, "int_lin_") == 0) {
+    if (f == "array_bool_xor") {  // odd parity: x1 xor (x2 xor (... xor xn))
+      std::vector<Expr> xs;
+      if (A.size() != 1 || !elements(A[0], xs)) return error(f + ": an array");
+      if (xs.empty()) return out = F::make_false(), true;
+      F r;
+      if (!formula(xs.back(), r)) return false;
+      for (size_t k = xs.size() - 1; k-- > 0;) {
+        F l;
+        if (!formula(xs[k], l)) return false;
+        r = F::make_xor(l, r);
+      }
+      out = r;
+      return true;
+    }
+    if (f == "array_int_maximum" || f == "array_int_minimum") {  // m == max (min) of xs
+      std::vector<Expr> xs;
+      T m;
+      if (A.size() != 2 || !term(A[0], m) || !elements(A[1], xs)) return error(f + ": a term and an array");
+      if (xs.empty()) return error(f + ": empty array");
+      T acc;
+      if (!term(xs[0], acc)) return false;
+      for (size_t k = 1; k < xs.size(); ++k) {
+        T t;
+        if (!term(xs[k], t)) return false;
+        acc = f == "array_int_maximum" ? T::make_max(acc, t) : T::make_min(acc, t);
+      }
+      out = F::make_eq(m, acc);
+      return true;
+    }
+    if (f.compare(0, 8, "int_lin_") == 0 || f.compare(0, 9, "bool_lin_") == 0) {
       if (A.size() != 3) return error(f + ": expected 3 arguments");
       T s, k;
       if (!linear(A[0], A[1], s) || !term(A[2], k)) return false;
-      const std::string op = f.substr(8);
+      const std::string op = f.substr(f[0] == 'i' ? 8 : 9);
       if (op == "eq") out = F::make_eq(s, k);
       else if (op == "ne") out = F::make_neq(s, k);
       else if (op == "le") out = F::make_leq(s, k);
