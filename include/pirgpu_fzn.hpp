@@ -839,6 +839,17 @@ inline bool compile(const std::string &text, Model &m, IDiagnostics &diag) {
       P.skip_to(';');
       continue;
     }
+    if (P.accept("predicate")) {
+      // predicate name(params); -- a declaration a solver's library adds; nothing to compile
+      std::string name;
+      if (!P.ident(name) || !P.peek("(")) {
+        P.fail("predicate name and parameters expected");
+        break;
+      }
+      P.skip_parens();
+      if (!P.expect(";")) break;
+      continue;
+    }
     if (P.accept("array")) {
       // array [1..n] of [var] T: name [ann] = [ ... ];
       detail::Expr range;

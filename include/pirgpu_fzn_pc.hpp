@@ -605,6 +605,17 @@ inline bool compile_pc(const std::string &text, PcModel &m, IDiagnostics &diag) 
       P.skip_to(';');
       continue;
     }
+    if (P.accept("predicate")) {
+      // predicate name(params); -- a declaration a solver's library adds; nothing to compile
+      std::string name;
+      if (!P.ident(name) || !P.peek("(")) {
+        P.fail("predicate name and parameters expected");
+        break;
+      }
+      P.skip_parens();
+      if (!P.expect(";")) break;
+      continue;
+    }
     if (P.accept("array")) {
       detail::Expr range;
       if (!P.expect("[") || !P.expr(range) || !P.expect("]") || !P.expect("of")) break;

@@ -56,6 +56,28 @@ def test_kat_user_bounds_oracle(case, fzn, oracle):
         assert got == [tuple(e) for e in expect[k]], (name, k)
 
 
+def test_minizinc_output_items(fzn, oracle):
+    """What MiniZinc writes around the constraints: predicate declarations,
+    annotations on variables, arrays, constraints and the solve item."""
+    text = """
+    predicate fzn_all_different_int(array [int] of var int: x);
+    var 1..3: x :: output_var;
+    var 1..3: y :: output_var;
+    var 2..6: s :: is_defined_var;
+    array [1..2] of var int: xs :: output_array([1..2]) = [x, y];
+    array [1..2] of int: cs = [1, 1];
+    constraint int_lin_eq(cs, xs, 6) :: domain;
+    constraint int_plus(x, y, s) :: defines_var(s);
+    solve :: int_search(xs, input_order, indomain_min, complete) satisfy;
+    """
+    dom, props, names = fzn(text)
+    rc, s = _oracle_fix(oracle, dom, props)
+    assert rc == oracle.OK
+    assert tuple(s[names["x"]]) == (3, 3) and tuple(s[names["y"]]) == (3, 3) and tuple(s[names["s"]]) == (6, 6)
+    with pytest.raises(ValueError, match="predicate name"):
+        fzn("predicate ;")
+
+
 def test_errors_are_reported(fzn):
     with pytest.raises(ValueError, match="unsupported constraint"):
         fzn("var int: x; constraint no_such_thing(x);")

@@ -242,3 +242,21 @@ def test_fzn_builtins_by_assignment(case, make_fzn, oracle):
             pytest.skip("not in the PC front end's subset: %s" % e)
         raise
     assert n > 0
+
+
+def test_fzn_minizinc_output_items(make_fzn, oracle):
+    """The PC front end reads what MiniZinc writes around the constraints."""
+    m = make_fzn()
+    d = m.compile("""
+    predicate fzn_all_different_int(array [int] of var int: x);
+    var 1..3: x :: output_var;
+    var 1..3: y :: output_var;
+    array [1..2] of var int: xs :: output_array([1..2]) = [x, y];
+    constraint int_lin_eq([1, 1], xs, 6) :: domain;
+    solve satisfy;
+    """)
+    store = np.ascontiguousarray(np.array(d["newvars"], np.int32).reshape(-1, 2))
+    rc, _ = oracle.pc_fixpoint(d["tape"], oracle.pc_order(d["tape"], d["roots"]), store)
+    names = {n: i for i, n in enumerate(d["names"])}
+    assert rc == oracle.OK
+    assert tuple(store[names["x"]]) == (3, 3) and tuple(store[names["y"]]) == (3, 3)
