@@ -21,7 +21,8 @@
 //   bool_clause bool2int array_bool_and array_bool_or array_bool_xor
 //   (+ bool_*_reif), set_in set_in_reif, array_int_element
 //   array_var_int_element array_bool_element array_var_bool_element; every
-//   reifiable one also half-reified, f_imp(args..., r): r -> f(args...).
+//   reifiable one also half-reified, f_imp(args..., r): r -> f(args...);
+//   fzn_all_different_int / all_different_int as pairwise !=.
 // Decompositions: x < y is 0 = (y <= x); x != y is 0 = (x == y);
 // x = y - z is y = x + z; -x is 0 = t + x; |x| = max(x, -x); integer
 // modulo m of y by z is q = y div z, p = q * z, y = p + m; a linear sum is a
@@ -662,6 +663,16 @@ class Compiler {
         acc = t;
       }
       out = m;
+      return true;
+    }
+    if (g == "fzn_all_different_int" || g == "all_different_int") {
+      // pairwise x_i != x_j (left to the solver by MiniZinc when it declares the predicate)
+      if (r != IMPOSE) return error(f + " cannot be reified");
+      std::vector<int> xs;
+      if (!arity(1) || !values(A[0], xs)) return false;
+      for (size_t i = 0; i < xs.size(); ++i)
+        for (size_t j = i + 1; j < xs.size(); ++j) cmp_ne(xs[i], xs[j], -1);
+      out = -1;
       return true;
     }
     if (g == "array_bool_xor") {

@@ -24,6 +24,7 @@
 //                              (pc.hpp:278-297)
 //   bool_lin_eq bool_lin_le:   as int_lin_*
 //   array_int_maximum array_int_minimum: m == max (min) chain of the terms
+//   fzn_all_different_int all_different_int: a conjunction of pairwise !=
 //   bool_and bool_or bool_xor bool_not, array_bool_and array_bool_or,
 //   array_bool_xor, bool_clause: connectives, clauses as right-nested
 //                              disjunctions of literals (binarize, pc.hpp:467-476)
@@ -443,6 +444,18 @@ class PcCompiler {
         r = F::make_xor(l, r);
       }
       out = r;
+      return true;
+    }
+    if (f == "fzn_all_different_int" || f == "all_different_int") {  // pairwise !=, as one conjunction
+      std::vector<Expr> xs;
+      if (A.size() != 1 || !elements(A[0], xs)) return error(f + ": an array");
+      std::vector<T> ts(xs.size());
+      for (size_t k = 0; k < xs.size(); ++k)
+        if (!term(xs[k], ts[k])) return false;
+      std::vector<F> ne;
+      for (size_t i = 0; i < ts.size(); ++i)
+        for (size_t j = i + 1; j < ts.size(); ++j) ne.push_back(F::make_neq(ts[i], ts[j]));
+      out = ne.empty() ? F::make_true() : conjunction(ne);
       return true;
     }
     if (f == "array_int_maximum" || f == "array_int_minimum") {  // m == max (min) of xs

@@ -230,6 +230,8 @@ BUILTINS = [
                  ("bool_or", lambda a, b: bool(a or b)), ("bool_xor", lambda a, b: a != b))
     for reif in (False, True)
 ] + [
+    ("all_different_int", "var 1..3: x; var 1..3: y; var 1..4: z; constraint fzn_all_different_int([x, y, z]);",
+     "x y z", lambda x, y, z: len({x, y, z}) == 3),
     ("bool_not", "var bool: a; var bool: b; constraint bool_not(a, b);", "a b", lambda a, b: b == 1 - a),
     ("bool2int", "var bool: a; var 0..3: i; constraint bool2int(a, i);", "a i", lambda a, i: i == a),
     ("bool_clause", "var bool: a; var bool: b; var bool: c; constraint bool_clause([a, b], [c]);", "a b c",
