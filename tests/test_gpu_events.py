@@ -59,7 +59,7 @@ def test_events_chain_and_random(local, chase, P, oracle):
     assert rc == orc == oracle.OK
     np.testing.assert_array_equal(g, o)
     if chase < 0:
-        assert st["rounds"] >= 2900
+        assert st["rounds"] >= 2500  # about one link per round
         # far fewer executions than AC-1 sweeps of every propagator
         assert st["executions"] < st["rounds"] * inst.nprops // 20
     else:
