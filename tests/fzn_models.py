@@ -58,3 +58,18 @@ KATS = [
     ("MinConstraint1", ["var 0..4: x; var 2..5: y; var 0..10: z; constraint int_min(x, y, z);"],
      ["x", "y", "z"], [[(0, 4), (2, 5), (0, 4)]]),
 ]
+
+
+def magic_square3():
+    """The 3 x 3 magic square: the numbers 1..9, every row, column and
+    diagonal summing to 15.  It has 8 solutions (the rotations and
+    reflections of one square).  Returns (FlatZinc text, cell names)."""
+    cells = ["m%d%d" % (i, j) for i in range(3) for j in range(3)]
+    lines = ["var 1..9: %s :: output_var;" % c for c in cells]
+    lines.append("constraint fzn_all_different_int([%s]);" % ", ".join(cells))
+    lines_of = [[(i, j) for j in range(3)] for i in range(3)] + [[(i, j) for i in range(3)] for j in range(3)]
+    lines_of += [[(k, k) for k in range(3)], [(k, 2 - k) for k in range(3)]]
+    for ln in lines_of:
+        lines.append("constraint int_lin_eq([1, 1, 1], [%s], 15);" % ", ".join("m%d%d" % ij for ij in ln))
+    lines.append("solve satisfy;")
+    return "\n".join(lines), cells

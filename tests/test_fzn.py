@@ -116,6 +116,17 @@ def test_queens_oracle(fzn, oracle):
     assert rc == oracle.OK and info["solutions"] == 92
 
 
+def test_magic_square_oracle(fzn, oracle):
+    text, cells = M.magic_square3()
+    dom, props, names = fzn(text)
+    rc, sols, info = _search_oracle(oracle, dom, props, [names[c] for c in cells])
+    assert rc == oracle.OK and info["solutions"] == 8
+    for sol in sols:
+        g = np.array(sol).reshape(3, 3)
+        assert sorted(sol) == list(range(1, 10))
+        assert all(g.sum(0) == 15) and all(g.sum(1) == 15) and np.trace(g) == 15 and np.trace(g[::-1]) == 15
+
+
 # ------------------------------------------------------------------- GPU ----
 
 def _gpu_ctx(dom, props):
@@ -309,3 +320,16 @@ def test_builtin_solutions_match_brute_force_gpu(case, fzn):
     assert status == pirgpu.OK
     got = sorted(tuple(int(v) for v in row) for row in sols)
     assert got == want, name
+
+
+@pytest.mark.gpu
+def test_magic_square_gpu(fzn):
+    import pirgpu
+    text, cells = M.magic_square3()
+    dom, props, names = fzn(text)
+    ctx = _gpu_ctx(dom, props)
+    status, sols, st = ctx.search([names[c] for c in cells], max_solutions=100)
+    assert status == pirgpu.OK and st["solutions"] == 8
+    for sol in sols:
+        g = np.array(sol).reshape(3, 3)
+        assert sorted(sol) == list(range(1, 10)) and all(g.sum(0) == 15) and all(g.sum(1) == 15)
