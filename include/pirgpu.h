@@ -242,8 +242,9 @@ typedef struct pir_search_stats {
  * (its values go to row k of out_solutions, max_solutions x ndec); otherwise
  * the branching variable's interval [l, u] is bisected into [l, m] (explored
  * first) and [m + 1, u], m = l + (u - l) / 2.  Up to opts->batch open nodes
- * are propagated per launch (pir_fixpoint_nodes_watch), so with batch > 1 the
- * solutions come in the order of the batches.  The decision variables must
+ * are propagated per launch (as pir_fixpoint_nodes_watch does; each batch is
+ * written into pinned staging the context owns and runs as one CUDA graph),
+ * so with batch > 1 the solutions come in the order of the batches.  The decision variables must
  * determine the others (typically: all variables).  The loop a solver runs
  * around lala-pc's PIR with snapshot / restore (pir.hpp:857-870); the context
  * keeps its store (brought to its fixpoint). */
