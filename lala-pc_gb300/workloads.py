@@ -31,6 +31,8 @@ Two variants of the random part:
   The reified targets are drawn from the variables whose domain holds [0, 1]
   and whose hidden value is 0 or 1.
 """
+import decimal
+
 import numpy as np
 
 ADD, MUL, TDIV, FDIV, CDIV, EDIV, MIN, MAX, EQ, LEQ = range(10)
@@ -334,13 +336,23 @@ def nodes(base_vars=100_000, base_props=400_000, nnodes=4096, seed=0, kmax=64, b
     return base, off, var.astype(np.int32), tl.astype(np.int32), tu.astype(np.int32)
 
 
+def uneven_sizes(ninst, pmin, pmax, seed):
+    """The uneven workload's propagator counts before the modulo decomposition:
+    floor(exp(ln pmin + u (ln pmax - ln pmin))), u uniform in [0, 1), in
+    decimal arithmetic (software, correctly rounded), so the sizes are the same
+    on every machine; numpy's exp / log come from the platform's libm."""
+    u = Rng(seed, 202).random(ninst)
+    c = decimal.Context(prec=50)
+    lo, hi = c.ln(decimal.Decimal(pmin)), c.ln(decimal.Decimal(pmax))
+    return np.array([int(c.exp(c.add(lo, c.multiply(decimal.Decimal(float(x)), c.subtract(hi, lo))))
+                         .to_integral_value(rounding=decimal.ROUND_FLOOR)) for x in u], np.int64)
+
+
 def uneven(ninst=512, pmin=1_000, pmax=200_000, seed=0, variant="planted"):
     """Independent instances with log-uniform propagator counts in
     [pmin, pmax], vars = props / 4, the mix with truncating division and
     modulo.  Returns a list of Instances."""
-    rng = Rng(seed, 202)
-    u = rng.random(ninst)
-    props = np.floor(np.exp(np.log(pmin) + u * (np.log(pmax) - np.log(pmin)))).astype(np.int64)
+    props = uneven_sizes(ninst, pmin, pmax, seed)
     out = []
     for j, p in enumerate(props):
         nv = max(int(p) // 4, 8)
