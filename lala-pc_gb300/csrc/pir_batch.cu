@@ -1225,8 +1225,7 @@ int nodes_run_staged(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nw
   a.out_store = nullptr;
   a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
   void *kargs[] = {&a};
-  cudaKernelNodeParams kp;
-  std::memset(&kp, 0, sizeof(kp));
+  cudaKernelNodeParams kp{};
   kp.func = const_cast<void *>(plan.kfn);
   kp.gridDim = dim3(plan.grid);
   kp.blockDim = dim3(plan.block);
@@ -1468,8 +1467,7 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
     ca.out = b->d_iout;
     ca.max_rounds = a.max_rounds;
     PIR_CK(cudaFuncSetAttribute(k_instances_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, clu_cap));
-    cudaLaunchConfig_t cfg;
-    std::memset(&cfg, 0, sizeof(cfg));
+    cudaLaunchConfig_t cfg{};
     const int nclusters = std::max(1, std::min(nbig, ctx->num_sms / CLU));
     cfg.gridDim = dim3(nclusters * CLU);
     cfg.blockDim = dim3(CLU_BLOCK);

@@ -368,7 +368,7 @@ int pir_ctx_create(pirgpu_ctx **out, int device) {
   }
   ctx->num_sms = prop.multiProcessorCount;
   ctx->smem_optin = (int)prop.sharedMemPerBlockOptin;
-  snprintf(ctx->dev_name, sizeof(ctx->dev_name), "%s", prop.name);
+  snprintf(ctx->dev_name, sizeof(ctx->dev_name), "%.*s", (int)sizeof(ctx->dev_name) - 1, prop.name);
   *out = ctx;
   return PIR_OK;
 }
