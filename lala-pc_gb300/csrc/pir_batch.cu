@@ -19,6 +19,7 @@
 
 #include <cooperative_groups.h>
 
+#include "pir_csr.h"
 #include "pir_engine.h"
 
 namespace cg = cooperative_groups;
@@ -865,19 +866,13 @@ int ensure_events_graph(pirgpu_ctx *ctx, BatchState *b) {
   const int nv = ctx->nvars;
   std::vector<int4> bc4((size_t)n);
   std::vector<int> ptr((size_t)nv + 1, 0), adj((size_t)n * 3);
-  for (long long p = 0; p < n; ++p) {
-    bc4[p] = make_int4(ctx->h_op[p], ctx->h_x[p], ctx->h_y[p], ctx->h_z[p]);
-    ++ptr[ctx->h_x[p] + 1];
-    ++ptr[ctx->h_y[p] + 1];
-    ++ptr[ctx->h_z[p] + 1];
-  }
-  for (int v = 0; v < nv; ++v) ptr[v + 1] += ptr[v];
-  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
-  for (long long p = 0; p < n; ++p) {
-    adj[fill[ctx->h_x[p]]++] = (int)p;
-    adj[fill[ctx->h_y[p]]++] = (int)p;
-    adj[fill[ctx->h_z[p]]++] = (int)p;
-  }
+  // on the host's threads (4M propagators: 0.38 s on one core)
+  const int T = adjacency_threads(n);
+  run_threads(T, [&](int t) {
+    for (long long p = n * t / T; p < n * (t + 1) / T; ++p)
+      bc4[(size_t)p] = make_int4(ctx->h_op[(size_t)p], ctx->h_x[(size_t)p], ctx->h_y[(size_t)p], ctx->h_z[(size_t)p]);
+  });
+  build_adjacency(n, nv, ctx->h_x.data(), ctx->h_y.data(), ctx->h_z.data(), ptr.data(), adj.data(), T);
   void *ptrs[] = {b->d_bc4, b->d_adj_ptr, b->d_adj};
   for (void *q : ptrs)
     if (q) cudaFree(q);
