@@ -15,6 +15,8 @@
 #include <thread>
 #include <vector>
 
+#include "../../include/pirgpu.h"  // enum pc_kind
+
 namespace pirgpu {
 
 // Runs fn(t) for t = 0 .. nthreads - 1, one std::thread each (t = 0 on the
@@ -82,6 +84,84 @@ inline void build_adjacency(long long n, int nv, const int32_t *x, const int32_t
       adj[c[(size_t)x[p]]++] = (int32_t)p;
       adj[c[(size_t)y[p]]++] = (int32_t)p;
       adj[c[(size_t)z[p]]++] = (int32_t)p;
+    }
+  });
+}
+
+// The PC event schedule's variable -> formula adjacency: adj[ptr[v] ..
+// ptr[v + 1]) lists, in increasing order, the formulas i (roots[i] in a tape
+// of 4-int nodes {kind, a, b, c}, the kinds of enum pc_kind) with variable v
+// among their leaves (variable terms, variable literals, store items), each
+// formula once.  ptr: nv + 1 entries; adj is resized to the entry count.
+// Each thread walks a contiguous chunk of formulas (their distinct variables
+// sorted, which the adjacency does not see), then counts, cursors and fills
+// as build_adjacency does: the arrays equal a sequential build's.
+inline void build_formula_adjacency(int np, const int32_t *roots, const int32_t *tape, int nv, int32_t *ptr,
+                                    std::vector<int32_t> &adj, int nthreads) {
+  const int T = std::max(1, nthreads);
+  std::vector<long long> lo(T + 1);
+  for (int t = 0; t <= T; ++t) lo[t] = (long long)np * t / T;
+  std::vector<std::vector<int32_t>> vars((size_t)T), start((size_t)T), cnt((size_t)T);
+  run_threads(T, [&](int t) {
+    std::vector<int32_t> &vs = vars[(size_t)t], &st = start[(size_t)t], &c = cnt[(size_t)t];
+    c.assign((size_t)nv, 0);
+    st.reserve((size_t)(lo[t + 1] - lo[t]) + 1);
+    vs.reserve((size_t)(lo[t + 1] - lo[t]) * 4);
+    std::vector<int32_t> todo;
+    todo.reserve(64);
+    for (long long i = lo[t]; i < lo[t + 1]; ++i) {
+      st.push_back((int32_t)vs.size());
+      const size_t first = vs.size();
+      todo.assign(1, roots[i]);
+      while (!todo.empty()) {
+        const int32_t *d = tape + 4 * (size_t)todo.back();
+        todo.pop_back();
+        const int k = d[0];
+        if (k == PC_VAR || k == PC_PVAR || k == PC_NVAR || (k >= PC_TELL && k <= PC_NASK_OUT)) {
+          vs.push_back(d[1]);
+        } else if (k == PC_AE || k == PC_NADD || k == PC_NMUL) {
+          for (int j = 0; j < d[2]; ++j) todo.push_back(d[1] + j);
+        } else if (k == PC_FORMULA || k == PC_NEG || k == PC_ABS || k == PC_ARG) {
+          todo.push_back(d[1]);
+        } else if ((k >= PC_ADD && k <= PC_MAX) || (k >= PC_LEQ && k <= PC_XOR)) {
+          todo.push_back(d[1]);
+          todo.push_back(d[2]);
+        }
+      }
+      std::sort(vs.begin() + (long)first, vs.end());
+      vs.erase(std::unique(vs.begin() + (long)first, vs.end()), vs.end());
+      for (size_t q = first; q < vs.size(); ++q) ++c[(size_t)vs[q]];
+    }
+    st.push_back((int32_t)vs.size());
+  });
+  std::vector<long long> vlo(T + 1), part(T + 1, 0);
+  for (int t = 0; t <= T; ++t) vlo[t] = (long long)nv * t / T;
+  run_threads(T, [&](int t) {
+    long long s = 0;
+    for (long long v = vlo[t]; v < vlo[t + 1]; ++v)
+      for (int u = 0; u < T; ++u) s += cnt[(size_t)u][(size_t)v];
+    part[t + 1] = s;
+  });
+  for (int t = 0; t < T; ++t) part[t + 1] += part[t];
+  ptr[0] = 0;
+  run_threads(T, [&](int t) {
+    long long s = part[t];
+    for (long long v = vlo[t]; v < vlo[t + 1]; ++v) {
+      for (int u = 0; u < T; ++u) {
+        const int32_t k = cnt[(size_t)u][(size_t)v];
+        cnt[(size_t)u][(size_t)v] = (int32_t)s;
+        s += k;
+      }
+      ptr[v + 1] = (int32_t)s;
+    }
+  });
+  adj.resize((size_t)part[T]);
+  run_threads(T, [&](int t) {
+    const std::vector<int32_t> &vs = vars[(size_t)t], &st = start[(size_t)t];
+    std::vector<int32_t> &c = cnt[(size_t)t];
+    for (long long i = lo[t]; i < lo[t + 1]; ++i) {
+      const size_t r = (size_t)(i - lo[t]);
+      for (int32_t q = st[r]; q < st[r + 1]; ++q) adj[(size_t)c[(size_t)vs[(size_t)q]]++] = (int32_t)i;
     }
   });
 }

@@ -39,6 +39,7 @@
 #include <numeric>
 #include <vector>
 
+#include "pir_csr.h"
 #include "pir_engine.h"
 
 namespace pirgpu {
@@ -1194,40 +1195,10 @@ int tree_base_of(PcState *s, int root) {
 // engine order): the distinct variable leaves of every formula.
 int pc_build_csr(pirgpu_ctx *ctx, PcState *s) {
   const int nv = ctx->nvars, np = (int)s->roots.size();
-  std::vector<int> deg((size_t)nv + 1, 0), seen((size_t)nv, -1), vars, todo;
-  std::vector<int> start((size_t)np + 1, 0);
-  vars.reserve((size_t)np * 6);
-  for (int i = 0; i < np; ++i) {
-    start[(size_t)i] = (int)vars.size();
-    todo.assign(1, s->roots[(size_t)i]);
-    while (!todo.empty()) {
-      const int n = todo.back();
-      todo.pop_back();
-      const int4 d = s->tape[(size_t)n];
-      const int k = d.x;
-      if (k == K_VAR || k == K_PVAR || k == K_NVAR || item_kind(k)) {
-        if (seen[(size_t)d.y] != i) {
-          seen[(size_t)d.y] = i;
-          vars.push_back(d.y);
-        }
-      } else if (k == K_AE) {
-        for (int j = 0; j < d.z; ++j) todo.push_back(d.y + j);
-      } else if (k == K_FORMULA || k == K_NEG || k == K_ABS || k == K_ARG) {
-        todo.push_back(d.y);
-      } else if (k == K_NADD || k == K_NMUL) {
-        for (int j = 0; j < d.z; ++j) todo.push_back(d.y + j);
-      } else if ((k >= K_ADD && k <= K_MAX) || (k >= K_LEQ && k <= K_XOR)) {
-        todo.push_back(d.y);
-        todo.push_back(d.z);
-      }
-    }
-  }
-  start[(size_t)np] = (int)vars.size();
-  for (int v : vars) ++deg[(size_t)v + 1];
-  for (int v = 0; v < nv; ++v) deg[(size_t)v + 1] += deg[(size_t)v];
-  std::vector<int> adj(vars.size()), fill(deg.begin(), deg.end() - 1);
-  for (int i = 0; i < np; ++i)
-    for (int q = start[(size_t)i]; q < start[(size_t)i + 1]; ++q) adj[(size_t)fill[(size_t)vars[(size_t)q]]++] = i;
+  // on the host's threads; the same arrays as a sequential walk
+  std::vector<int> deg((size_t)nv + 1, 0), adj;
+  build_formula_adjacency(np, s->roots.data(), reinterpret_cast<const int32_t *>(s->tape.data()), nv, deg.data(), adj,
+                          adjacency_threads((long long)s->tape.size()));
   int r;
   if ((r = ensure(ctx, (void **)&s->d_adj_ptr, &s->cap_adj_ptr, deg.size() * sizeof(int)))) return r;
   if ((r = ensure(ctx, (void **)&s->d_adj, &s->cap_adj, std::max<size_t>(adj.size(), 1) * sizeof(int)))) return r;

@@ -32,6 +32,7 @@ def csr(tmp_path_factory):
         lib.csr_build(n, nv, p(x), p(y), p(z), p(ptr), p(adj), threads)
         return ptr, adj
     build.threads = lib.csr_threads
+    build.lib_path = out
     return build
 
 
@@ -61,3 +62,63 @@ def test_thread_choice(csr):
     assert csr.threads(1 << 20, 8) == 8
     assert csr.threads(1 << 20, 64) == 16        # capped
     assert 1 <= csr.threads(1 << 20, 0) <= 16
+
+
+def _pc_reference(tape, roots, nv):
+    """Variable -> formula adjacency by walking every formula in Python."""
+    import pc as P
+    lists = [[] for _ in range(nv)]
+    for i, r in enumerate(roots):
+        seen, todo = set(), [int(r)]
+        while todo:
+            k, a, b, _ = (int(v) for v in tape[todo.pop()])
+            if k in (P.VAR, P.PVAR, P.NVAR) or P.TELL <= k <= P.NASK_OUT:
+                seen.add(a)
+            elif k in (P.AE, P.NADD, P.NMUL):
+                todo += list(range(a, a + b))
+            elif k in (P.FORMULA, P.NEG, P.ABS, P.ARG):
+                todo.append(a)
+            elif P.ADD <= k <= P.MAX or P.LEQ <= k <= P.XOR:
+                todo += [a, b]
+        for v in seen:
+            lists[v].append(i)
+    ptr = np.concatenate([[0], np.cumsum([len(l) for l in lists])]).astype(np.int32)
+    adj = np.array([i for l in lists for i in l], np.int32)
+    return ptr, adj
+
+
+def _pc_tapes():
+    import pc as P
+    import workloads as W
+    tape, roots, lb, _, _ = W.pc_mix(3000, 2000, seed=2)
+    yield "pc_mix", tape, roots, len(lb)
+    t = P.Tape()
+    x = [t.var(v) for v in range(6)]
+    t.prop(t.leq(t.nadd([x[0], x[1], x[2], x[0]]), t.constant(5)))
+    t.prop(t.disj(t.eq(t.mul(x[3], x[3]), t.constant(4)), t.pvar(5)))
+    t.prop(t.abstract_element(tell=[(1, 0, 3)], ask=[(2, 1, 1)], not_ask=[(4, 0, 0)]))
+    t.prop(t.true())
+    t.prop(t.imply(t.gt(t.abs(x[4]), t.neg(x[1])), t.nvar(0)))
+    tape, roots = t.arrays()
+    yield "mixed", tape, roots, 8
+
+
+@pytest.mark.parametrize("threads", [1, 2, 5, 16])
+def test_formula_adjacency_matches_reference(csr, threads):
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "lala-pc_gb300"))
+    lib = ctypes.CDLL(str(csr.lib_path))
+    P_ = ctypes.POINTER(ctypes.c_int)
+    lib.pc_adjacency.argtypes = [ctypes.c_int, P_, P_, ctypes.c_int, P_, P_, ctypes.c_int, ctypes.c_int]
+    lib.pc_adjacency.restype = ctypes.c_int
+    for name, tape, roots, nv in _pc_tapes():
+        tape = np.ascontiguousarray(tape, np.int32)
+        roots = np.ascontiguousarray(roots, np.int32)
+        ptr = np.full(nv + 1, -7, np.int32)
+        adj = np.full(8 * len(tape) + 1, -7, np.int32)
+        p = lambda a: a.ctypes.data_as(P_)
+        k = lib.pc_adjacency(len(roots), p(roots), p(tape), nv, p(ptr), p(adj), len(adj), threads)
+        rptr, radj = _pc_reference(tape, roots, nv)
+        assert k == len(radj), name
+        np.testing.assert_array_equal(ptr, rptr, err_msg=name)
+        np.testing.assert_array_equal(adj[:k], radj, err_msg=name)
