@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "pir_engine.h"
+#include "pir_sort.h"
 
 using namespace pirgpu;
 
@@ -501,24 +502,28 @@ int pir_tell(pirgpu_ctx *ctx, int32_t n, const int32_t *op, const int32_t *x, co
   std::copy(x, x + n, x2.begin() + old);
   std::copy(y, y + n, y2.begin() + old);
   std::copy(z, z + n, z2.begin() + old);
+  // on the host's threads, the permutation std::stable_sort gives (4M propagators: 0.91 s on one core)
   std::vector<int> perm(tot);
   std::iota(perm.begin(), perm.end(), 0);
-  std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) {
+  const int T = adjacency_threads((long long)tot);
+  parallel_stable_sort(perm, [&](int a, int b) {
     if (o2[a] != o2[b]) return o2[a] < o2[b];
     if (y2[a] != y2[b]) return y2[a] < y2[b];
     if (x2[a] != x2[b]) return x2[a] < x2[b];
     return z2[a] < z2[b];
-  });
+  }, T);
   ctx->h_op.resize(tot);
   ctx->h_x.resize(tot);
   ctx->h_y.resize(tot);
   ctx->h_z.resize(tot);
-  for (size_t i = 0; i < tot; ++i) {
-    ctx->h_op[i] = o2[perm[i]];
-    ctx->h_x[i] = x2[perm[i]];
-    ctx->h_y[i] = y2[perm[i]];
-    ctx->h_z[i] = z2[perm[i]];
-  }
+  run_threads(T, [&](int t) {
+    for (size_t i = tot * (size_t)t / (size_t)T; i < tot * (size_t)(t + 1) / (size_t)T; ++i) {
+      ctx->h_op[i] = o2[(size_t)perm[i]];
+      ctx->h_x[i] = x2[(size_t)perm[i]];
+      ctx->h_y[i] = y2[(size_t)perm[i]];
+      ctx->h_z[i] = z2[(size_t)perm[i]];
+    }
+  });
   ctx->n = (long long)tot;
   ctx->max_var_used = maxv;
   ctx->bytecode_version++;

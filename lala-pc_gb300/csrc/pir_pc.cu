@@ -41,6 +41,7 @@
 
 #include "pir_csr.h"
 #include "pir_engine.h"
+#include "pir_sort.h"
 
 namespace pirgpu {
 
@@ -1370,10 +1371,10 @@ int pc_tell(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *kind, const int32_t 
     s->tree_base[(size_t)(roots[p] + off)] = tree_base_of(s, roots[p] + off);
   }
   const std::vector<int4> &T = s->tape;
-  std::stable_sort(s->roots.begin(), s->roots.end(), [&](int x, int y) {
+  parallel_stable_sort(s->roots, [&](int x, int y) {
     if (T[(size_t)x].x != T[(size_t)y].x) return T[(size_t)x].x < T[(size_t)y].x;
     return s->len[(size_t)x] < s->len[(size_t)y];
-  });
+  }, adjacency_threads((long long)s->roots.size()));
   s->max_var = max_var;
   s->max_depth = max_depth;
   PIR_CK(cudaSetDevice(ctx->device));

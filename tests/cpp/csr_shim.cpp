@@ -17,3 +17,21 @@ extern "C" int pc_adjacency(int np, const int *roots, const int *tape, int nv, i
   std::copy(a.begin(), a.end(), adj);
   return (int)a.size();
 }
+
+#include <numeric>
+
+#include "../../lala-pc_gb300/csrc/pir_sort.h"
+
+// The install order: a permutation of 0 .. n-1 stably sorted by (op, y, x, z).
+extern "C" void install_order(int n, const int *op, const int *x, const int *y, const int *z, int *perm,
+                              int nthreads) {
+  std::vector<int> p((size_t)n);
+  std::iota(p.begin(), p.end(), 0);
+  pirgpu::parallel_stable_sort(p, [&](int a, int b) {
+    if (op[a] != op[b]) return op[a] < op[b];
+    if (y[a] != y[b]) return y[a] < y[b];
+    if (x[a] != x[b]) return x[a] < x[b];
+    return z[a] < z[b];
+  }, nthreads);
+  std::copy(p.begin(), p.end(), perm);
+}

@@ -122,3 +122,22 @@ def test_formula_adjacency_matches_reference(csr, threads):
         assert k == len(radj), name
         np.testing.assert_array_equal(ptr, rptr, err_msg=name)
         np.testing.assert_array_equal(adj[:k], radj, err_msg=name)
+
+
+@pytest.mark.parametrize("threads", [1, 2, 3, 8, 16])
+@pytest.mark.parametrize("shape", [(0, 1), (1, 1), (4095, 3), (5000, 3), (100_000, 40), (300_000, 1000)])
+def test_install_order_is_the_stable_sort(csr, shape, threads):
+    """The parallel stable sort gives numpy's stable sort by (op, y, x, z):
+    ties keep their input order (small variable ranges make many ties)."""
+    lib = ctypes.CDLL(str(csr.lib_path))
+    P_ = ctypes.POINTER(ctypes.c_int)
+    lib.install_order.argtypes = [ctypes.c_int, P_, P_, P_, P_, P_, ctypes.c_int]
+    n, nv = shape
+    rng = np.random.default_rng(n + nv)
+    op = rng.integers(0, 10, n).astype(np.int32)
+    x, y, z = (rng.integers(0, nv, n).astype(np.int32) for _ in range(3))
+    perm = np.full(n, -1, np.int32)
+    p = lambda a: a.ctypes.data_as(P_)
+    lib.install_order(n, p(op), p(x), p(y), p(z), p(perm), threads)
+    want = np.lexsort((z, x, y, op))  # lexsort is stable: the last key is the primary one
+    np.testing.assert_array_equal(perm, want)
