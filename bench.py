@@ -729,9 +729,9 @@ def run_search(args):
                    "device_ms_per_search": dev_s * 1e3 / args.steps},
         "roofline": None,
         "cpu_baseline": cpu,
-        "e2e": {"value": nodes / sum(walls), "unit": "nodes/s", "h2d_bytes_per_step": None,
-                "d2h_bytes_per_step": None, "note": "whole pir_search calls: host bookkeeping, tightenings "
-                                                    "in and watched bounds out per launch"},
+        "e2e": {"value": nodes / sum(walls), "unit": "nodes/s", "h2d_bytes_per_step": st["h2d_bytes"],
+                "d2h_bytes_per_step": st["d2h_bytes"], "note": "whole pir_search calls: host bookkeeping, "
+                                                               "tightenings in and watched bounds out per launch"},
         "gpu_launches": st["launches"] * args.steps, "clocks": clocks,
     }
     print(json.dumps(out), flush=True)

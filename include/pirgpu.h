@@ -235,6 +235,8 @@ typedef struct pir_search_stats {
   int64_t max_depth;  /* deepest node */
   float device_ms;    /* summed device time of the node launches */
   int32_t status;     /* PIR_OK: space exhausted or max_solutions reached; PIR_TIMEOUT: max_nodes reached */
+  int64_t h2d_bytes;  /* bytes copied to the device for the node batches (tightenings, watch list) */
+  int64_t d2h_bytes;  /* bytes copied back (per-node status and counters, watched bounds) */
 } pir_search_stats;
 
 /* Depth-first search over the decision variables `dec` (ndec of them) from the

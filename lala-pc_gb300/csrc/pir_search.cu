@@ -185,6 +185,14 @@ extern "C" int pir_search(pirgpu_ctx *ctx, int32_t ndec, const int32_t *dec, con
                                     wlb.data(), wub.data(), status.data(), nullptr, &ns);
     }
     if (rc != PIR_OK) break;
+    {
+      // the batch's copies: watch list, offsets and tightenings in; counters, per-node status and
+      // watched bounds out
+      int64_t ntight = 0;
+      for (int id : ids) ntight += pool[(size_t)id].depth;
+      st.h2d_bytes += 4 * ((int64_t)ndec + take + 1 + 3 * ntight);
+      st.d2h_bytes += 32 + 8 * take + 8 * take * (int64_t)ndec;
+    }
     // watched bounds of node i, decision k
     auto lo = [&](int64_t i, int k) -> int32_t {
       return staged ? wout[(size_t)i * ndec + k].x : wlb[(size_t)i * ndec + k];

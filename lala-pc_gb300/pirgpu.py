@@ -48,7 +48,7 @@ class SearchOpts(ctypes.Structure):
 class SearchStats(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_int64), ("failures", ctypes.c_int64), ("solutions", ctypes.c_int64),
                 ("launches", ctypes.c_int64), ("max_depth", ctypes.c_int64), ("device_ms", ctypes.c_float),
-                ("status", ctypes.c_int32)]
+                ("status", ctypes.c_int32), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
 
     def asdict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
