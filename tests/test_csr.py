@@ -1,6 +1,9 @@
-"""The event schedules' variable -> propagator adjacency (pir_csr.h), built
-on the host's threads: the same arrays as a sequential counting sort for
-every thread count, on random bytecodes with repeated variables."""
+"""The host-threaded builders of the install (pir_csr.h, pir_sort.h): the
+event schedules' variable -> propagator adjacency (the arrays of a
+sequential counting sort, on random bytecodes with repeated variables), the
+PC event schedule's variable -> formula adjacency (a Python walk of every
+formula) and the install order of the bytecode (numpy's stable sort by
+(op, y, x, z)), for every thread count."""
 import ctypes
 import os
 import subprocess
