@@ -867,7 +867,7 @@ int ensure_events_graph(pirgpu_ctx *ctx, BatchState *b) {
   std::vector<int4> bc4((size_t)n);
   std::vector<int> ptr((size_t)nv + 1, 0), adj((size_t)n * 3);
   // on the host's threads (4M propagators: 0.38 s on one core)
-  const int T = adjacency_threads(n);
+  const int T = adjacency_threads(n, 0, nv);
   run_threads(T, [&](int t) {
     for (long long p = n * t / T; p < n * (t + 1) / T; ++p)
       bc4[(size_t)p] = make_int4(ctx->h_op[(size_t)p], ctx->h_x[(size_t)p], ctx->h_y[(size_t)p], ctx->h_z[(size_t)p]);

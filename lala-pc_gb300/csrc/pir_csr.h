@@ -29,12 +29,14 @@ inline void run_threads(int nthreads, F fn) {
   for (std::thread &th : pool) th.join();
 }
 
-// Threads worth using for n propagators (0: the host's).
-inline int adjacency_threads(long long n, int requested = 0) {
+// Threads worth using for n work items (0 requested: the host's).  With
+// nvars > 0, each thread's per-variable counts (nvars words) stay within the
+// 3 n entries they count.
+inline int adjacency_threads(long long n, int requested = 0, long long nvars = 0) {
   int t = requested > 0 ? requested : (int)std::thread::hardware_concurrency();
   t = std::max(1, std::min(t, 16));
-  // each thread's per-variable counts cost nvars words: not for small inputs
   if (n < (1ll << 16)) t = 1;
+  if (nvars > 0) t = (int)std::max(1ll, std::min((long long)t, 3 * n / nvars));
   return t;
 }
 

@@ -1199,7 +1199,7 @@ int pc_build_csr(pirgpu_ctx *ctx, PcState *s) {
   // on the host's threads; the same arrays as a sequential walk
   std::vector<int> deg((size_t)nv + 1, 0), adj;
   build_formula_adjacency(np, s->roots.data(), reinterpret_cast<const int32_t *>(s->tape.data()), nv, deg.data(), adj,
-                          adjacency_threads((long long)s->tape.size()));
+                          adjacency_threads((long long)s->tape.size(), 0, nv));
   int r;
   if ((r = ensure(ctx, (void **)&s->d_adj_ptr, &s->cap_adj_ptr, deg.size() * sizeof(int)))) return r;
   if ((r = ensure(ctx, (void **)&s->d_adj, &s->cap_adj, std::max<size_t>(adj.size(), 1) * sizeof(int)))) return r;

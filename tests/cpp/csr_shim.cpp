@@ -7,7 +7,9 @@ extern "C" void csr_build(long long n, int nv, const int *x, const int *y, const
   pirgpu::build_adjacency(n, nv, x, y, z, ptr, adj, nthreads);
 }
 
-extern "C" int csr_threads(long long n, int requested) { return pirgpu::adjacency_threads(n, requested); }
+extern "C" int csr_threads(long long n, int requested, long long nvars) {
+  return pirgpu::adjacency_threads(n, requested, nvars);
+}
 
 extern "C" int pc_adjacency(int np, const int *roots, const int *tape, int nv, int *ptr, int *adj, int cap,
                             int nthreads) {

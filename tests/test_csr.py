@@ -23,7 +23,7 @@ def csr(tmp_path_factory):
     lib = ctypes.CDLL(str(out))
     P = ctypes.POINTER(ctypes.c_int)
     lib.csr_build.argtypes = [ctypes.c_longlong, ctypes.c_int, P, P, P, P, P, ctypes.c_int]
-    lib.csr_threads.argtypes = [ctypes.c_longlong, ctypes.c_int]
+    lib.csr_threads.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_longlong]
     lib.csr_threads.restype = ctypes.c_int
 
     def build(nv, x, y, z, threads):
@@ -61,10 +61,13 @@ def test_adjacency_matches_counting_sort(csr, shape, threads):
 
 
 def test_thread_choice(csr):
-    assert csr.threads(1000, 8) == 1             # small inputs stay on one thread
-    assert csr.threads(1 << 20, 8) == 8
-    assert csr.threads(1 << 20, 64) == 16        # capped
-    assert 1 <= csr.threads(1 << 20, 0) <= 16
+    assert csr.threads(1000, 8, 0) == 1             # small inputs stay on one thread
+    assert csr.threads(1 << 20, 8, 0) == 8
+    assert csr.threads(1 << 20, 64, 0) == 16        # capped
+    assert 1 <= csr.threads(1 << 20, 0, 0) <= 16
+    # per-thread counts of nvars words stay within the 3 n entries
+    assert csr.threads(4_000_000, 16, 1_000_000) == 12
+    assert csr.threads(4_000_000, 16, 100_000_000) == 1
 
 
 def _pc_reference(tape, roots, nv):
