@@ -161,19 +161,29 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def profile_fields(name):
+    """The 'key: number' lines of the ncu summary profiles/<name>.md (the
+    figures a bench line quotes from ncu), as a dict of floats."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    out = {}
+    if not os.path.exists(p):
+        return out
+    for line in open(p):
+        t = line.strip()
+        if ":" not in t or t.startswith(("#", "|", "`")) or " " in t.split(":", 1)[0]:
+            continue
+        k, v = t.split(":", 1)
+        try:
+            out[k] = float(v.strip().split()[0])
+        except (ValueError, IndexError):
+            continue
+    return out
+
+
 def ncu_traffic(name):
     """DRAM bytes per launch recorded by the ncu summary profiles/<name>.md
     (line 'traffic_bytes_per_launch: N'), or None."""
-    p = os.path.join(ROOT, "profiles", name + ".md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+    return profile_fields(name).get("traffic_bytes_per_launch")
 
 
 # --------------------------------------------------------------- workloads --
@@ -243,6 +253,199 @@ def cpu_sample(inst, target_s=12.0, min_sweeps=1):
     return (n * inst.nprops) / dt, n + 1, dt + one, (n + 1) * inst.nprops / (dt + one)
 
 
+def cpu_time_to_fixpoint(sec_per_sweep):
+    """The reference loop's time to the fixpoint of the 1M / 4M + chain
+    instance on one host core: its two parts share no variable, so the
+    Gauss-Seidel loop over the whole instance needs the larger of the parts'
+    sweep counts (each part run to its own fixpoint here, on the oracle),
+    each sweep costing the measured seconds of a sweep of the whole instance."""
+    import workloads as W
+    from oracle import oracle as O
+    rnd = W.single_large(0, chain=0)
+    s = rnd.store()
+    t0 = time.perf_counter()
+    rc, info = O.install_and_fixpoint(rnd.op, rnd.x, rnd.y, rnd.z, s)
+    t_rnd = time.perf_counter() - t0
+    empty = W.Instance(np.zeros(0, np.int32), np.zeros(0, np.int32), *(np.zeros(0, np.int32),) * 4)
+    chain = W.add_chain(empty, 20_000, 1_000_000, 0)
+    c = chain.store()
+    t0 = time.perf_counter()
+    rc2, cinfo = O.install_and_fixpoint(chain.op, chain.x, chain.y, chain.z, c)
+    t_chain = time.perf_counter() - t0
+    sweeps = max(info["sweeps"], cinfo["sweeps"])
+    return {"seconds": sweeps * sec_per_sweep, "sweeps": sweeps, "random_part_sweeps": info["sweeps"],
+            "chain_sweeps": cinfo["sweeps"], "seconds_per_sweep": sec_per_sweep, "cores": 1,
+            "method": "sweeps to the fixpoint (the larger of the random part's and the chain's, each run "
+                      "to its fixpoint on the oracle: %.1f s + %.1f s) x the measured seconds of one sweep "
+                      "of the whole instance" % (t_rnd, t_chain)}
+
+
+def out_of_l2_record(cr, hbm):
+    """AC-1 and event fixpoints of a 4,000,000-var / 16,000,000-propagator
+    instance (256 MB of bytecode + 32 MB of store: more than twice the 129 MB
+    L2), where the per-round bytecode stream comes from HBM."""
+    import pirgpu
+    import workloads as W
+    t0 = time.perf_counter()
+    inst = W.plain(4_000_000, 16_000_000, 10**6, 0)
+    gen_s = time.perf_counter() - t0
+    ctx = pirgpu.Context(0)
+    ctx.load_store(inst.lb, inst.ub)
+    t0 = time.perf_counter()
+    ctx.tell(inst.op, inst.x, inst.y, inst.z)
+    tell_s = time.perf_counter() - t0
+    snap = ctx.snapshot()
+    tuned = ctx.autotune(16)
+    runs = []
+    for k in range(4):  # one warm-up, three timed, the L2 flushed before each
+        ctx.restore(snap)
+        cr.flush_l2()
+        rc, st = ctx.fixpoint()
+        if rc != pirgpu.OK:
+            raise RuntimeError("out-of-L2 fixpoint status %s" % pirgpu.STATUS[rc])
+        if k:
+            runs.append(st)
+    ac1_lb, ac1_ub = ctx.read_store()
+    best = min(runs, key=lambda r: r["device_ms"])
+    ctx.restore(snap)
+    cr.flush_l2()
+    rc, ev = ctx.fixpoint(sched=pirgpu.SCHED_EVENTS)
+    ev_lb, ev_ub = ctx.read_store()
+    same = bool(rc == pirgpu.OK and np.array_equal(ac1_lb, ev_lb) and np.array_equal(ac1_ub, ev_ub))
+    alg = best["executions"] * ALG_BYTES_PER_EXEC + best["narrowed"] * ALG_BYTES_PER_JOIN
+    achieved = alg / (best["device_ms"] / 1e3) / 1e9
+    prof = profile_fields("persistent_fixpoint_out_of_l2")
+    rec = {
+        "workload": "4,000,000 vars / 16,000,000 propagators (planted solution, bounds scale 1e6, base mix); "
+                    "bytecode 256 MB + store 32 MB",
+        "value": best["executions"] / (best["device_ms"] / 1e3), "unit": "executions/s",
+        "time_to_fixpoint_ms": best["device_ms"], "rounds": best["rounds"], "executions": best["executions"],
+        "kernel_variant": list(tuned),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "dram_bytes_per_round": prof.get("dram_bytes_per_round"),
+                     "dram_gbs_ncu": prof.get("dram_gbs"),
+                     "bytes_model": "40 B per execution + 4 B per narrowing join"},
+        "events_schedule": {"time_to_fixpoint_ms": ev["device_ms"], "executions": ev["executions"],
+                            "rounds": ev["rounds"], "certify_narrowed": ev["certify_narrowed"],
+                            "store_equal_to_ac1": same},
+        "l2": "flushed before each fixpoint (256 MiB cudaMemset)", "generate_s": gen_s, "tell_s": tell_s,
+    }
+    ctx.close()
+    return rec
+
+
+def _nodes_bit_exact(ctx, base, off, var, lb, ub, m):
+    """Nodes 0 .. m-1 of a batch: GPU stores (pir_fixpoint_nodes, event
+    schedule) against the oracle run node by node on the host's threads."""
+    import pirgpu
+    from oracle import oracle as O
+    o = off[:m + 1]
+    status, olb, oub, _, _ = ctx.fixpoint_nodes(o, var, lb, ub, sched=pirgpu.SCHED_EVENTS)
+    op, x, y, z = ctx.bytecode()
+    bs = np.ascontiguousarray(np.stack(base, 1))
+    ost, ostore, _ = O.fixpoint_nodes(op, x, y, z, bs, o, var, lb, ub, threads=os.cpu_count() or 1)
+    eq = 0
+    for j in range(m):
+        if status[j] == ost[j] and (ost[j] != O.OK or (np.array_equal(olb[j], ostore[j, :, 0]) and
+                                                       np.array_equal(oub[j], ostore[j, :, 1]))):
+            eq += 1
+    return {"nodes_checked": m, "nodes_equal": eq, "failed_nodes": int((ost == O.FAILED).sum())}
+
+
+def _nodes_sequential(ctx, snap, off, var, lb, ub, sample, sched):
+    """The plain single-instance GPU loop, node after node: restore the base,
+    embed the node's tightenings, pir_fixpoint (AC-1 rounds or the event
+    schedule with its certifying sweep)."""
+    import pirgpu
+    dev, ex, t0 = 0.0, 0, time.perf_counter()
+    for j in range(sample):
+        ctx.restore(snap)
+        ctx.embed_many(var[off[j]:off[j + 1]], lb[off[j]:off[j + 1]], ub[off[j]:off[j + 1]])
+        rc, st = ctx.fixpoint(sched=sched)
+        dev += st["device_ms"] / 1e3
+        ex += st["executions"]
+    wall = time.perf_counter() - t0
+    ctx.restore(snap)
+    return {"nodes_per_s_device": sample / dev, "nodes_per_s_wall": sample / wall, "sample_nodes": sample,
+            "executions_per_node": ex / sample}
+
+
+def nodes_record(cr, args):
+    """The batched-search-node workload (4,096 nodes over a 100,000-var /
+    400,000-propagator base at its fixpoint) measured beside the default
+    line: batched device nodes/s, the plain single-instance GPU loop node
+    after node under both schedules, end to end through the C ABI, and an
+    inline bit-exact check of a sample of nodes against the oracle."""
+    import pirgpu
+    ctx, base, (blb, bub), off, var, lb, ub = _nodes_workload()
+    nn = len(off) - 1
+    tuned = ctx.autotune_nodes(off, var, lb, ub)
+    for _ in range(3):
+        ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=pirgpu.SCHED_EVENTS)
+        cr.flush_l2()
+    runs = []
+    for _ in range(5):
+        status, _, _, rounds, st = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=pirgpu.SCHED_EVENTS)
+        runs.append(st)
+        cr.flush_l2()
+    dev_ms = float(np.median([r["device_ms"] for r in runs]))
+    value = nn / (dev_ms / 1e3)
+    st = runs[0]
+    _, _, _, _, st_ac1 = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=pirgpu.SCHED_AC1)
+    snap = ctx.snapshot()
+    ctx.autotune(8)
+    ctx.restore(snap)
+    seq_ac1 = _nodes_sequential(ctx, snap, off, var, lb, ub, args.seq_nodes, pirgpu.SCHED_AC1)
+    seq_ev = _nodes_sequential(ctx, snap, off, var, lb, ub, args.seq_nodes, pirgpu.SCHED_EVENTS)
+    p_off, p_var, p_lb, p_ub = (cr.pinned(len(a)) for a in (off, var, lb, ub))
+    p_off[:], p_var[:], p_lb[:], p_ub[:] = off, var, lb, ub
+    ts = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        ctx.fixpoint_nodes(p_off, p_var, p_lb, p_ub, want_stores=False, sched=pirgpu.SCHED_EVENTS)
+        ts.append(time.perf_counter() - t0)
+    e2e_t = float(np.median(ts))
+    # end to end through the staged batches (pir_nodes_stage: the batch written
+    # into the context's pinned staging, one CUDA graph per batch), the call a
+    # solver's own search loop makes; per node its status out
+    nt = int(off[-1])
+    ts = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        buf = ctx.nodes_stage(nn, nt, 0)
+        buf[:nn + 1] = off
+        buf[nn + 1:nn + 1 + nt] = var
+        buf[nn + 1 + nt:nn + 1 + 2 * nt] = lb
+        buf[nn + 1 + 2 * nt:] = ub
+        ctx.fixpoint_nodes_staged(nn, nt, 0)
+        ts.append(time.perf_counter() - t0)
+    staged_t = float(np.median(ts))
+    exact = _nodes_bit_exact(ctx, (blb, bub), off, var, lb, ub, min(nn, args.cpu_nodes))
+    rec = {
+        "workload": "nodes: 100,000 vars / 400,000 propagators (bounds scale 1e6) at its fixpoint, 4,096 nodes, "
+                    "k ~ U[1,64] bisections of unfixed vars",
+        "value": value, "unit": "nodes/s", "ms_per_batch": dev_ms, "schedule": "events (certified)",
+        "node_kernel_variant": list(tuned), "executions_per_batch": st["executions"],
+        "certify": {"executions": st["certify_executions"], "narrowed": st["certify_narrowed"]},
+        "max_rounds": int(rounds.max()), "nodes_failed": int((status == pirgpu.FAILED).sum()),
+        "batched_ac1": {"ms_per_batch": st_ac1["device_ms"], "nodes_per_s": nn / (st_ac1["device_ms"] / 1e3),
+                        "executions_per_batch": st_ac1["executions"]},
+        "sequential_ac1": seq_ac1, "sequential_events": seq_ev,
+        "batched_over_sequential_ac1": value / seq_ac1["nodes_per_s_device"],
+        "batched_over_sequential_events": value / seq_ev["nodes_per_s_device"],
+        "e2e": {"value": nn / e2e_t, "unit": "nodes/s", "h2d_bytes_per_step": int(len(var) * 12 + len(off) * 4),
+                "d2h_bytes_per_step": int(nn * 8),
+                "over_sequential_events_wall": (nn / e2e_t) / seq_ev["nodes_per_s_wall"],
+                "staged_graph": {"value": nn / staged_t, "unit": "nodes/s",
+                                 "note": "pir_nodes_stage + pir_fixpoint_nodes_staged: the batch written into "
+                                         "pinned staging, one updated CUDA graph per batch"}},
+        "bit_exact": exact,
+        "l2": "flushed between batches (256 MiB cudaMemset); median of 5 batches, CUDA events",
+    }
+    ctx.close()
+    return rec
+
+
 # ------------------------------------------------------------------- ours ---
 def run_ours(args):
     import pirgpu
@@ -294,6 +497,7 @@ def run_ours(args):
     t_max = dist_max(dist, dev_ms / 1e3)
     execs_all = dist_sum(dist, execs)
     value = execs_all / t_max
+    ac1_store = ctx.read_store() if args.max_rounds == 0 else None
 
     # end to end through the C ABI: pinned host store in, fixpoint, store out
     lb_h = cr.pinned(inst.nvars)
@@ -323,29 +527,56 @@ def run_ours(args):
     ev = None
     if args.mode in (0, 1) and args.max_rounds == 0 and not args.no_events:
         ev_runs = []
-        for _ in range(2):
+        for _ in range(3):
             ctx.restore(snap)
+            cr.flush_l2()
             rc, st = ctx.fixpoint(sched=pirgpu.SCHED_EVENTS)
             if rc != pirgpu.OK:
                 raise RuntimeError("event fixpoint status %s" % pirgpu.STATUS[rc])
             ev_runs.append(st)
-            cr.flush_l2()
-        st = min(ev_runs, key=lambda s: s["device_ms"])
+        ev_store = ctx.read_store()
+        st = sorted(ev_runs, key=lambda s: s["device_ms"])[1]  # median of 3
         ev = {"time_to_fixpoint_ms": st["device_ms"], "executions": st["executions"], "rounds": st["rounds"],
+              "certify_executions": st["certify_executions"], "certify_narrowed": st["certify_narrowed"],
               "ac1_over_events_time": (dev_ms / args.steps) / st["device_ms"],
               "ac1_over_events_executions": (execs / args.steps) / max(st["executions"], 1),
-              "fixpoint": "identical to AC-1 (bit-exact tests)"}
+              "store_equal_to_ac1": bool(np.array_equal(ev_store[0], ac1_store[0]) and
+                                         np.array_equal(ev_store[1], ac1_store[1])),
+              "fixpoint": "certified by a final sweep of every propagator; bit-exact vs the oracle in tests"}
     if rank != 0:
         return
     hbm, hbm_src = peaks()
     achieved = (execs * ALG_BYTES_PER_EXEC + joins * ALG_BYTES_PER_JOIN) / (dev_ms / 1e3) / 1e9
-    traffic = ncu_traffic("persistent_fixpoint_" + args.workload)
+    prof = profile_fields("persistent_fixpoint_" + args.workload)
+    traffic = prof.get("traffic_bytes_per_launch")
     cpu = None
-    if ws == 1 and not args.no_cpu:
+    cpu_fix = None
+    extras = ws == 1 and not args.no_cpu
+    if extras:
         v, sw, secs, _ = cpu_sample(inst, args.cpu_seconds)
         cpu = {"value": v, "unit": "executions/s", "cores": 1, "kind": "port",
                "sample": "%d Gauss-Seidel sweeps (%d executions) of the same instance from its "
                          "initial store, %.1f s, 1 host thread" % (sw, sw * nprops, secs)}
+        if args.workload == "single_large":
+            cpu_fix = cpu_time_to_fixpoint(secs / sw)
+            cpu_fix["over_gpu_ac1"] = cpu_fix["seconds"] / (dev_ms / args.steps / 1e3)
+            if ev:
+                cpu_fix["over_gpu_events"] = cpu_fix["seconds"] / (ev["time_to_fixpoint_ms"] / 1e3)
+    l2_resident = args.workload == "single_large"
+    roofline = {"bound": "l2" if l2_resident else "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": traffic,
+                "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                "bytes_model": "40 B per execution + 4 B per narrowing join"}
+    if l2_resident:
+        roofline["note"] = ("the 64 MB bytecode and 8.3 MB store stay in the 129 MB L2 across rounds: DRAM traffic "
+                            "is the 'traffic' figure; frac is against the HBM copy peak, the only measured "
+                            "memory peak; the ncu L2 figures are in 'l2'")
+        roofline["l2"] = {k: prof.get(k) for k in ("l2_hit_rate_pct", "lts_throughput_pct", "l1tex_throughput_pct",
+                                                   "issue_active_pct", "dram_bytes_per_round")}
+    more = {}
+    if ws == 1 and args.workload == "single_large" and not args.no_extras:
+        more["out_of_l2"] = out_of_l2_record(cr, hbm)
+        more["nodes"] = nodes_record(cr, args)
     out = {
         "metric": "propagator executions/sec", "value": value, "unit": "executions/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -358,10 +589,7 @@ def run_ours(args):
                    "l2": "flushed between steps (256 MiB cudaMemset); step timed with CUDA events",
                    "rounds_per_step": rounds[0], "fixpoint": "bit-exact vs CPU oracle in tests",
                    "kernel_variant": list(tuned) if tuned else args.variant},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic,
-                     "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "bytes_model": "40 B per execution + 4 B per narrowing join"},
+        "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "executions/s",
                 "h2d_bytes_per_step": int(inst.nvars * 8), "d2h_bytes_per_step": int(inst.nvars * 8),
@@ -370,8 +598,10 @@ def run_ours(args):
         "clocks": clocks,
         "time_to_fixpoint_ms": dev_ms / args.steps,
         "events_schedule": ev,
+        "cpu_time_to_fixpoint": cpu_fix,
         "wall_s": wall,
     }
+    out.update(more)
     print(json.dumps(out), flush=True)
 
 
@@ -446,22 +676,15 @@ def run_nodes(args):
         cr.flush_l2()
         _, _, _, _, st_first = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=sched)
         first_ms = st_first["device_ms"]
-    # the plain single-instance GPU loop, node after node (sample)
+    # the plain single-instance GPU loop, node after node (sample), under
+    # AC-1 rounds and under the event schedule
     sample = min(nn, args.seq_nodes) if extras else 0
-    seq_dev_rate = seq_wall_rate = None
+    seq_ac1 = seq_ev = None
     if sample:
         ctx.autotune(8)
         ctx.restore(snap)
-        seq_dev, t0 = 0.0, time.perf_counter()
-        for j in range(sample):
-            ctx.restore(snap)
-            ctx.embed_many(var[off[j]:off[j + 1]], lb[off[j]:off[j + 1]], ub[off[j]:off[j + 1]])
-            rc, st = ctx.fixpoint()
-            seq_dev += st["device_ms"] / 1e3
-        seq_wall = time.perf_counter() - t0
-        ctx.restore(snap)
-        seq_dev_rate = sample / seq_dev
-        seq_wall_rate = sample / seq_wall
+        seq_ac1 = _nodes_sequential(ctx, snap, off, var, lb, ub, sample, pirgpu.SCHED_AC1)
+        seq_ev = _nodes_sequential(ctx, snap, off, var, lb, ub, sample, pirgpu.SCHED_EVENTS)
     # end to end through the C ABI: host tightenings in, per-node status and
     # rounds out (what a search driver reads; the sequential loop reads the
     # same), and separately with every node's store downloaded as well
@@ -482,8 +705,10 @@ def run_nodes(args):
     hbm, hbm_src = peaks()
     achieved = (execs * ALG_BYTES_PER_EXEC + joins * ALG_BYTES_PER_JOIN) / dev_s / 1e9
     cpu = None
+    exact = None
     if extras and not args.no_cpu:
         from oracle import oracle as O
+        exact = _nodes_bit_exact(ctx, (blb, bub), off, var, lb, ub, min(nn, args.cpu_nodes))
         op, x, y, z = ctx.bytecode()
         bs = np.ascontiguousarray(np.stack([blb, bub], 1))
         m = min(nn, args.cpu_nodes)
@@ -507,11 +732,11 @@ def run_nodes(args):
                    "node_kernel_variant": list(tuned) if tuned else None,
                    "batched_ac1_ms": st_ac1["device_ms"], "batched_ac1_executions": st_ac1["executions"],
                    "first_batch_on_new_base_ms": first_ms},
-        "plain_sequential": {"nodes_per_s_device": seq_dev_rate, "nodes_per_s_wall": seq_wall_rate,
-                             "sample_nodes": sample,
-                             "batched_over_sequential_device": value / seq_dev_rate if seq_dev_rate else None,
-                             "batched_over_sequential_wall": (nn_all / e2e_t) / seq_wall_rate
-                             if (seq_wall_rate and e2e_t) else None},
+        "sequential_ac1": seq_ac1, "sequential_events": seq_ev,
+        "batched_over_sequential_ac1": value / seq_ac1["nodes_per_s_device"] if seq_ac1 else None,
+        "batched_over_sequential_events": value / seq_ev["nodes_per_s_device"] if seq_ev else None,
+        "certify": {"executions": runs[0]["certify_executions"], "narrowed": runs[0]["certify_narrowed"]},
+        "bit_exact": exact,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": ncu_traffic("nodes_events_4096_nodes"),
                      "peak_source": hbm_src},
@@ -960,6 +1185,8 @@ def main():
     ap.add_argument("--variant", type=int, default=0, help="persistent kernel variant, 0: autotuned")
     ap.add_argument("--no-events", action="store_true", help="skip the event-schedule run of the single instance")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload: skip the out-of-L2 and batched-node records")
     ap.add_argument("--seq-nodes", type=int, default=128, help="nodes timed in the sequential loop")
     ap.add_argument("--cpu-nodes", type=int, default=256)
     ap.add_argument("--cpu-instances", type=int, default=128)

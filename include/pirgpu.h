@@ -84,7 +84,16 @@ typedef struct pir_opts {
   int32_t chase;              /* event schedule: propagators of narrowed small variables a thread runs at once,
                                  per frontier entry (0: 64; at most 256; < 0: none, everything waits for the next
                                  round) */
-  int32_t reserved[4];
+  int32_t certify;            /* event schedules (pir_fixpoint, pir_fixpoint_nodes, pir_search): 0 or > 0 end the
+                                 run with a certifying sweep (pir_fixpoint: every propagator once; a node: every
+                                 propagator of a variable the node narrowed that is not entailed at the base
+                                 store, whose other propagators see the base store, a fixpoint); a sweep that
+                                 narrows something resumes the rounds, so the result is always a fixpoint;
+                                 < 0: none */
+  int32_t segments;           /* pir_fixpoint's event schedule: 0 or > 0 run the propagators of paths joined by
+                                 variables with two occurrences as segments (a warp sweeps up to 64 of them in
+                                 shared memory); < 0: every propagator on its own */
+  int32_t reserved[2];
 } pir_opts;
 
 typedef struct pir_stats {
@@ -93,6 +102,9 @@ typedef struct pir_stats {
   int64_t narrowed;    /* bounds narrowed (atomic joins that changed the store) */
   float device_ms;     /* device time of the fixpoint (CUDA events on the context stream) */
   int32_t status;      /* pir_status of the run */
+  int64_t certify_executions; /* executions of the certifying sweeps (part of executions) */
+  int64_t certify_narrowed;   /* bounds the certifying sweeps narrowed: 0 unless the schedule stopped short of
+                                 the fixpoint (then the rounds resumed from those narrowings) */
 } pir_stats;
 
 typedef struct pirgpu_ctx pirgpu_ctx;
@@ -190,9 +202,10 @@ int pir_fixpoint_nodes(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off, cons
                        int32_t *out_lb, int32_t *out_ub, int32_t *out_status,
                        int32_t *out_rounds, pir_stats *stats);
 
-/* Number of event node kernel variants (threads per CTA x resident CTAs per
- * SM) that pir_autotune_nodes chooses from; opts.variant of the node calls. */
-#define PIR_NODE_VARIANTS 7
+/* Number of event node kernel variants (one node per CTA or one per warp x
+ * threads per CTA x resident CTAs per SM) that pir_autotune_nodes chooses
+ * from; opts.variant of the node calls. */
+#define PIR_NODE_VARIANTS 10
 
 /* Autotuner of the batched search nodes (event schedule): runs the batch with
  * every node kernel variant (twice, keeping the faster run) and keeps the
@@ -212,6 +225,33 @@ int pir_fixpoint_nodes_watch(pirgpu_ctx *ctx, int32_t nnodes, const int32_t *off
                              const int32_t *lb, const int32_t *ub, const pir_opts *opts, int32_t nwatch,
                              const int32_t *watch, int32_t *out_wlb, int32_t *out_wub, int32_t *out_status,
                              int32_t *out_rounds, pir_stats *stats);
+
+/* Repeated batches of search nodes as CUDA graphs.  A solver that runs its
+ * own search loop around the batched nodes (the per-node shared copies of
+ * pir.hpp:182-195, the snapshot / embed / fixpoint / restore loop of
+ * tests/bound_consistency_test.hpp:175-196) writes each batch into pinned
+ * host memory the context owns, and the batch then runs as one CUDA graph
+ * (clear the counters, copy in, node kernel, copy out) whose copy sizes and
+ * kernel arguments are updated in place from batch to batch; the graph is
+ * rebuilt only when a staging buffer has to grow or the kernel variant
+ * changes.
+ *
+ * pir_nodes_stage returns in *in the staging of a batch of nnodes nodes with
+ * ntight tightenings in all and nwatch watched variables, as int32:
+ * watch[nwatch] | off[nnodes + 1] | var[ntight] | lb[ntight] | ub[ntight]
+ * (the arguments of pir_fixpoint_nodes_watch, back to back).  It stays valid
+ * until the next pir_nodes_stage call on the context. */
+int pir_nodes_stage(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch, int32_t **in);
+/* Runs the staged batch (sizes as given to pir_nodes_stage): the event node
+ * kernel with its certifying sweeps, as pir_fixpoint_nodes_watch does (the
+ * context's store is first brought to its fixpoint when it is not known to be
+ * one).  out_status[j], out_rounds[j] (may be NULL) and the watched bounds
+ * out_wlb / out_wub (nnodes x nwatch, node-major) as pir_fixpoint_nodes_watch
+ * returns them.  The staged input is checked first (offsets, variable
+ * indices): PIR_EINVAL runs nothing. */
+int pir_fixpoint_nodes_staged(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch,
+                              const pir_opts *opts, int32_t *out_status, int32_t *out_rounds,
+                              int32_t *out_wlb, int32_t *out_wub, pir_stats *stats);
 
 /* Branching order of pir_search. */
 enum pir_order {
@@ -284,7 +324,8 @@ int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int64_t *prop_o
  * device looks up the scratch address (cudaGetSymbolAddress) and should come
  * before any stream capture.  Calls share the scratch: calls that overlap on
  * the GPU race and must not be issued.  stream may be NULL (default stream);
- * the call returns once the fixpoint is done, with the status and stats. */
+ * the call waits for the stream (it reads the outcome back) and returns once
+ * the fixpoint is done, with the status and stats. */
 int pir_fixpoint_static(const int32_t *d_op, const int32_t *d_x, const int32_t *d_y,
                         const int32_t *d_z, int64_t n, int32_t *d_store, int32_t nvars,
                         const pir_opts *opts, pir_stats *stats, void *stream);

@@ -21,6 +21,7 @@
 
 #include "pir_csr.h"
 #include "pir_engine.h"
+#include "pir_segments.h"
 
 namespace cg = cooperative_groups;
 
@@ -59,8 +60,17 @@ struct BatchState {
   size_t cap_nio = 0;
   // event-driven nodes: AoS bytecode, variable -> propagator adjacency, per-CTA scratch
   long long ev_version = -1;
+  int ev_graph_nvars = -1;
   int4 *d_bc4 = nullptr;
   int *d_adj_ptr = nullptr, *d_adj = nullptr;
+  std::vector<int> h_adj_ptr, h_adj;  // host copy of the adjacency (the segment builder reads it)
+  // path segments of the single-instance event schedule (pir_segments.h)
+  long long seg_version = -1;
+  int seg_nvars = -1;
+  int nseg = 0;
+  int *d_uptr = nullptr, *d_uadj = nullptr, *d_seg_pptr = nullptr, *d_seg_code = nullptr, *d_seg_vptr = nullptr;
+  unsigned *d_seg_var = nullptr, *d_in_seg = nullptr;
+  unsigned long long *d_seg_umask = nullptr;
   int ev_slots = 0, ev_nvars = 0;  // per-CTA scratch slots allocated (grid <= slots)
   long long ev_n = 0;
   void *d_ev = nullptr;  // per-CTA scratch block
@@ -98,9 +108,10 @@ void destroy_batch_state(pirgpu_ctx *ctx) {
   if (b->sg) cudaGraphDestroy(b->sg);
   if (b->h_sin) cudaFreeHost(b->h_sin);
   if (b->h_sout) cudaFreeHost(b->h_sout);
-  void *ptrs[] = {b->d_bc, b->d_off,    b->d_store, b->d_aux,     b->d_iout, b->d_nstore, b->d_tight,
+  void *ptrs[] = {b->d_bc,    b->d_off,    b->d_store, b->d_aux,     b->d_iout, b->d_nstore, b->d_tight,
                   b->d_nout, b->d_nio, b->d_bc4, b->d_adj_ptr, b->d_adj, b->d_ev, b->d_ent, b->d_watch,
-                  b->d_sin, b->d_sout};
+                  b->d_sin, b->d_sout, b->d_uptr, b->d_uadj, b->d_seg_pptr, b->d_seg_code, b->d_seg_vptr,
+                  b->d_seg_var, b->d_in_seg, b->d_seg_umask};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete b;
@@ -562,7 +573,9 @@ struct EvArgs {
   unsigned *epochs;  // grid
   NodeOut *out;
   unsigned long long *execs, *narrowed;
+  unsigned long long *cert;  // certifying sweeps: [0] executions, [1] bounds narrowed
   long long max_rounds;
+  int certify;  // end every node with a certifying sweep
 };
 
 // Insert `key` into the shared-memory set tab[1 << LOG] (-1 = free): 1 newly
@@ -686,7 +699,7 @@ __global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
   unsigned *pstamp = a.pstamp + blockIdx.x * (size_t)a.n;
   int *cand = a.cand + blockIdx.x * (size_t)a.n;
   unsigned epoch = a.epochs[blockIdx.x];
-  unsigned long long execs = 0, narrowed = 0;
+  unsigned long long execs = 0, narrowed = 0, cert_execs = 0, cert_narrowed = 0;
   for (int i = tid; i < a.bitmap_words; i += blockDim.x) s_dyn[i] = 0u;  // then cleared word by word
   __syncthreads();
   for (;;) {
@@ -718,8 +731,17 @@ __global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
     int cur = 0;
     long long round = 0;
     int status = PIR_OK;
+    // Certifying sweep: when a round lists nothing, one more round runs every
+    // non-entailed propagator of every variable the node narrowed (the touched
+    // list), whatever the wake lists, stamps and sets recorded.  A propagator
+    // none of whose variables the node narrowed reads the base store, which is
+    // a fixpoint, so a sweep without narrowing proves the node's store a
+    // fixpoint; a sweep that narrows lists as any round does and the rounds go
+    // on (and end with another sweep).
+    bool certified = !a.certify;
     while (!failed) {
-      if (s_nd[cur] == 0) break;
+      const bool certifying = s_nd[cur] == 0;
+      if (certifying && certified) break;
       if (a.max_rounds > 0 && round >= a.max_rounds) {
         status = PIR_TIMEOUT;
         break;
@@ -734,13 +756,15 @@ __global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
       set_clear<CHG_LOG>(s_chg_set);
       __syncthreads();
       // candidates: the non-entailed propagators adjacent to the variables
-      // changed last round, the adjacency spread over the CTA
-      const int nd = s_nd[cur];
+      // changed last round (certifying: to every variable the node narrowed),
+      // the adjacency spread over the CTA
+      const int nd = certifying ? s_nt : s_nd[cur];
+      const int *src = certifying ? touched : (cur ? dl1 : dl0);
       for (int c0 = 0; c0 < nd; c0 += blockDim.x) {
         const int i = c0 + tid;
         int beg = 0, deg = 0;
         if (i < nd) {
-          const int v = (cur ? dl1 : dl0)[i];
+          const int v = src[i];
           beg = __ldg(a.adj_ptr + v);
           deg = __ldg(a.adj_ptr + v + 1) - beg;
         }
@@ -768,15 +792,22 @@ __global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
       NodeEvStore rs{ws, a.base, bits, vmark, tmark, cur ? dl0 : dl1, touched, &s_nd[cur ^ 1], &s_nt, s_chg_set,
                      s_touch_set, epoch, tag};
       const int nc = s_ncand;
-      int f2 = 0;
+      int f2 = 0, ch = 0;
       for (int i = tid; i < nc; i += blockDim.x) {
         const int4 b = __ldg(a.bc + cand[i]);
         const Itv ia = rs.load(b.y), ib = rs.load(b.z), ic = rs.load(b.w);
-        narrowed += deduce_loaded(b.x, b.y, b.z, b.w, ia, ib, ic, rs, f2);
+        ch += deduce_loaded(b.x, b.y, b.z, b.w, ia, ib, ic, rs, f2);
         ++execs;
+      }
+      narrowed += ch;
+      if (certifying) {
+        cert_narrowed += ch;
+        if (tid == 0) cert_execs += nc;
       }
       failed = __syncthreads_or(f2);
       cur ^= 1;
+      // a sweep that narrowed nothing certifies; one that narrowed resumes the rounds
+      if (certifying) certified = s_nd[cur] == 0;
     }
     if (failed) status = PIR_FAILED;
     if (tid == 0) {
@@ -808,9 +839,242 @@ __global__ void __launch_bounds__(NB, MINB) k_nodes_events(EvArgs a) {
   if (tid == 0) a.epochs[blockIdx.x] = epoch;
   execs = warp_sum64(execs);
   narrowed = warp_sum64(narrowed);
+  cert_narrowed = warp_sum64(cert_narrowed);
   if ((tid & 31) == 0) {
     if (execs) atomicAdd(a.execs, execs);
     if (narrowed) atomicAdd(a.narrowed, narrowed);
+    if (cert_narrowed) atomicAdd(a.cert + 1, cert_narrowed);
+  }
+  if (tid == 0 && cert_execs) atomicAdd(a.cert, cert_execs);
+}
+
+// ------------------------------------------------- one warp per node -------
+//
+// The same node rounds as k_nodes_events on one warp instead of one CTA:
+// __syncwarp instead of block barriers, a warp scan of the degrees for the
+// adjacency expansion, and about 6 KB of shared memory per node in flight,
+// so an SM holds several times more nodes (a node's frontier is a few hundred
+// propagators: a CTA's warps spent most of each round at its barriers).  The
+// narrowed-variable bitmap is hashed (variable v sets bit v mod WBITS): a
+// false positive only costs a read of the overlay, and the touched list takes
+// each variable once through its global stamp (tmark), not through the bit.
+constexpr int WCAND_LOG = 10, WCHG_LOG = 9, WBITS_LOG = 13;
+
+struct WarpNodeShared {
+  int cand_set[1 << WCAND_LOG];
+  int chg_set[1 << WCHG_LOG];
+  unsigned bits[(1 << WBITS_LOG) / 32];
+  int beg[32], end[32];
+  int ncand, nd[2], nt;
+};
+
+template <int LOG>
+__device__ __forceinline__ void warp_set_clear(int *tab) {
+  for (int i = threadIdx.x & 31; i < (1 << LOG); i += 32) tab[i] = -1;
+}
+
+// The node store of a warp: base meet overlay, the overlay read only where
+// the hashed bitmap says the node may have narrowed.
+struct WarpNodeStore {
+  int2 *ws;
+  const int2 *base;
+  unsigned *bits;
+  unsigned *vmark, *tmark;
+  int *dnext, *touched;
+  int *nd, *nt;
+  int *chg_set;
+  unsigned epoch, tag;
+  __device__ __forceinline__ bool maybe(int v) const {
+    const unsigned h = (unsigned)v & ((1u << WBITS_LOG) - 1u);
+    return (bits[h >> 5] >> (h & 31)) & 1u;
+  }
+  __device__ __forceinline__ Itv load(int v) const {
+    const int2 b = __ldg(base + v);
+    if (!maybe(v)) return mk(b.x, b.y);
+    const int2 t = __ldcg(ws + v);
+    return mk(max(b.x, t.x), min(b.y, t.y));
+  }
+  __device__ __forceinline__ void note(int v) const {
+    int c = set_insert<WCHG_LOG>(chg_set, v);
+    if (c < 0) c = atomicMax(vmark + v, epoch) < epoch ? 1 : 0;
+    if (c > 0) dnext[atomicAdd(nd, 1)] = v;
+    if (atomicExch(tmark + v, tag) != tag) touched[atomicAdd(nt, 1)] = v;
+  }
+  __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
+    int n = 0;
+    if (r.l > seen.l) {
+      asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(&ws[v].x), "r"(r.l) : "memory");
+      ++n;
+    }
+    if (r.u < seen.u) {
+      asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(&ws[v].y), "r"(r.u) : "memory");
+      ++n;
+    }
+    if (n) {
+      const unsigned h = (unsigned)v & ((1u << WBITS_LOG) - 1u);
+      atomicOr(bits + (h >> 5), 1u << (h & 31));
+      note(v);
+      if (is_bot(mk(max(seen.l, r.l), min(seen.u, r.u)))) failed = 1;
+    }
+    return n;
+  }
+};
+
+// WPB warps per CTA, each running nodes one after the other (work stealing);
+// per-node scratch slots are per warp (slot = CTA * WPB + warp).
+template <int WPB, int MINB>
+__global__ void __launch_bounds__(WPB * 32, MINB) k_nodes_warp(EvArgs a) {
+  extern __shared__ unsigned long long s_dyn_w[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WarpNodeShared &sh = reinterpret_cast<WarpNodeShared *>(s_dyn_w)[warp];
+  const size_t nv = (size_t)a.nvars;
+  const size_t slot = (size_t)blockIdx.x * WPB + warp;
+  int2 *ws = a.ws + slot * nv;
+  unsigned *vmark = a.vmark + slot * nv, *tmark = a.tmark + slot * nv;
+  int *const dl0 = a.lists + slot * 3 * nv, *const dl1 = dl0 + nv;  // changed lists
+  int *touched = dl0 + 2 * nv;
+  unsigned *pstamp = a.pstamp + slot * (size_t)a.n;
+  int *cand = a.cand + slot * (size_t)a.n;
+  unsigned epoch = a.epochs[slot];
+  unsigned long long execs = 0, narrowed = 0, cert_execs = 0, cert_narrowed = 0;
+  for (int i = lane; i < (1 << WBITS_LOG) / 32; i += 32) sh.bits[i] = 0u;
+  __syncwarp();
+  for (;;) {
+    int node = 0;
+    if (lane == 0) node = atomicAdd(a.next, 1);
+    node = __shfl_sync(0xFFFFFFFFu, node, 0);
+    if (node >= a.nnodes) break;
+    if (lane == 0) {
+      sh.nd[0] = sh.nd[1] = 0;
+      sh.nt = 0;
+    }
+    warp_set_clear<WCHG_LOG>(sh.chg_set);
+    __syncwarp();
+    ++epoch;
+    const unsigned tag = epoch;
+    WarpNodeStore st{ws, a.base, sh.bits, vmark, tmark, dl0, touched, &sh.nd[0], &sh.nt, sh.chg_set, epoch, tag};
+    const int k0 = a.off[node], k1 = a.off[node + 1];
+    for (int k = k0 + lane; k < k1; k += 32) {
+      const int v = a.var[k];
+      int dummy = 0;
+      st.embed(v, st.load(v), mk(a.lb[k], a.ub[k]), dummy);
+    }
+    __syncwarp();
+    int f = 0;
+    for (int k = k0 + lane; k < k1; k += 32) f |= is_bot(st.load(a.var[k]));
+    int failed = __any_sync(0xFFFFFFFFu, f) ? 1 : 0;
+    int cur = 0;
+    long long round = 0;
+    int status = PIR_OK;
+    // the certifying sweep of k_nodes_events: when a round lists nothing, one
+    // more round over the propagators of every variable the node narrowed
+    bool certified = !a.certify;
+    while (!failed) {
+      __syncwarp();
+      const bool certifying = sh.nd[cur] == 0;
+      if (certifying && certified) break;
+      if (a.max_rounds > 0 && round >= a.max_rounds) {
+        status = PIR_TIMEOUT;
+        break;
+      }
+      ++round;
+      ++epoch;
+      const int nd = certifying ? sh.nt : sh.nd[cur];
+      const int *src = certifying ? touched : (cur ? dl1 : dl0);
+      __syncwarp();
+      if (lane == 0) {
+        sh.ncand = 0;
+        sh.nd[cur ^ 1] = 0;
+      }
+      warp_set_clear<WCAND_LOG>(sh.cand_set);
+      warp_set_clear<WCHG_LOG>(sh.chg_set);
+      __syncwarp();
+      for (int c0 = 0; c0 < nd; c0 += 32) {
+        const int i = c0 + lane;
+        int beg = 0, deg = 0;
+        if (i < nd) {
+          const int v = src[i];
+          beg = __ldg(a.adj_ptr + v);
+          deg = __ldg(a.adj_ptr + v + 1) - beg;
+        }
+        int incl = deg;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        sh.beg[lane] = beg;
+        sh.end[lane] = incl;
+        __syncwarp();
+        const int total = sh.end[31];
+        for (int j = lane; j < total; j += 32) {
+          int lo = 0, hi = 31;
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (sh.end[mid] > j) hi = mid;
+            else lo = mid + 1;
+          }
+          const int first = lo ? sh.end[lo - 1] : 0;
+          const int p = __ldg(a.adj + sh.beg[lo] + (j - first));
+          if (a.ent && a.ent[p]) continue;
+          int c = set_insert<WCAND_LOG>(sh.cand_set, p);
+          if (c < 0) c = atomicMax(pstamp + p, epoch) < epoch ? 1 : 0;
+          if (c > 0) cand[atomicAdd(&sh.ncand, 1)] = p;
+        }
+        __syncwarp();
+      }
+      WarpNodeStore rs{ws, a.base, sh.bits, vmark, tmark, cur ? dl0 : dl1, touched, &sh.nd[cur ^ 1], &sh.nt,
+                       sh.chg_set, epoch, tag};
+      const int nc = sh.ncand;
+      int f2 = 0, ch = 0;
+      for (int i = lane; i < nc; i += 32) {
+        const int4 b = __ldg(a.bc + cand[i]);
+        const Itv ia = rs.load(b.y), ib = rs.load(b.z), ic = rs.load(b.w);
+        ch += deduce_loaded(b.x, b.y, b.z, b.w, ia, ib, ic, rs, f2);
+        ++execs;
+      }
+      narrowed += ch;
+      if (certifying) {
+        cert_narrowed += ch;
+        if (lane == 0) cert_execs += nc;
+      }
+      failed = __any_sync(0xFFFFFFFFu, f2) ? 1 : 0;
+      __syncwarp();
+      cur ^= 1;
+      if (certifying) certified = sh.nd[cur] == 0;
+    }
+    if (failed) status = PIR_FAILED;
+    if (lane == 0) {
+      a.out[node].status = status;
+      a.out[node].rounds = (int)round;
+    }
+    if (a.out_store) {
+      int2 *dst = a.out_store + (size_t)node * nv;
+      for (size_t v = lane; v < nv; v += 32) {
+        const Itv t = st.load((int)v);
+        dst[v] = make_int2(t.l, t.u);
+      }
+    }
+    for (int k = lane; k < a.nwatch; k += 32) {
+      const Itv t = st.load(a.watch[k]);
+      a.out_watch[(size_t)node * a.nwatch + k] = make_int2(t.l, t.u);
+    }
+    __syncwarp();
+    // the overlay back to the whole range where this node narrowed, the bitmap cleared
+    const int nt = sh.nt;
+    for (int i = lane; i < nt; i += 32) ws[touched[i]] = make_int2(INT_MIN, INT_MAX);
+    for (int i = lane; i < (1 << WBITS_LOG) / 32; i += 32) sh.bits[i] = 0u;
+    __syncwarp();
+  }
+  if (lane == 0) a.epochs[slot] = epoch;
+  execs = warp_sum64(execs);
+  narrowed = warp_sum64(narrowed);
+  cert_narrowed = warp_sum64(cert_narrowed);
+  if (lane == 0) {
+    if (execs) atomicAdd(a.execs, execs);
+    if (narrowed) atomicAdd(a.narrowed, narrowed);
+    if (cert_narrowed) atomicAdd(a.cert + 1, cert_narrowed);
+    if (cert_execs) atomicAdd(a.cert, cert_execs);
   }
 }
 
@@ -861,9 +1125,11 @@ BatchState *batch(pirgpu_ctx *ctx) {
 // AoS bytecode and the variable -> propagator adjacency of the context's
 // bytecode (engine order), rebuilt when the bytecode changes.
 int ensure_events_graph(pirgpu_ctx *ctx, BatchState *b) {
-  if (b->ev_version == ctx->bytecode_version && b->d_bc4) return PIR_OK;
+  if (b->ev_version == ctx->bytecode_version && b->ev_graph_nvars == ctx->nvars && b->d_bc4) return PIR_OK;
   const long long n = ctx->n;
   const int nv = ctx->nvars;
+  if (!adjacency_fits(3 * n))
+    return set_err(ctx, PIR_EINVAL, "event schedule: %lld propagators need more than 2^31 - 1 adjacency entries", n);
   std::vector<int4> bc4((size_t)n);
   std::vector<int> ptr((size_t)nv + 1, 0), adj((size_t)n * 3);
   // on the host's threads (4M propagators: 0.38 s on one core)
@@ -872,7 +1138,8 @@ int ensure_events_graph(pirgpu_ctx *ctx, BatchState *b) {
     for (long long p = n * t / T; p < n * (t + 1) / T; ++p)
       bc4[(size_t)p] = make_int4(ctx->h_op[(size_t)p], ctx->h_x[(size_t)p], ctx->h_y[(size_t)p], ctx->h_z[(size_t)p]);
   });
-  build_adjacency(n, nv, ctx->h_x.data(), ctx->h_y.data(), ctx->h_z.data(), ptr.data(), adj.data(), T);
+  if (!build_adjacency(n, nv, ctx->h_x.data(), ctx->h_y.data(), ctx->h_z.data(), ptr.data(), adj.data(), T))
+    return set_err(ctx, PIR_EINVAL, "event schedule: adjacency does not fit int32 offsets");
   void *ptrs[] = {b->d_bc4, b->d_adj_ptr, b->d_adj};
   for (void *q : ptrs)
     if (q) cudaFree(q);
@@ -888,17 +1155,81 @@ int ensure_events_graph(pirgpu_ctx *ctx, BatchState *b) {
   PIR_CK(cudaMemcpyAsync(b->d_adj_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   PIR_CK(cudaMemcpyAsync(b->d_adj, adj.data(), adj.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   PIR_CK(cudaStreamSynchronize(ctx->stream));
+  b->h_adj_ptr.swap(ptr);
+  b->h_adj.swap(adj);
   b->ev_version = ctx->bytecode_version;
+  b->ev_graph_nvars = nv;
   return PIR_OK;
 }
 
-int events_graph(pirgpu_ctx *ctx, const int4 **bc, const int **adj_ptr, const int **adj) {
+// Path segments and the variable -> unit adjacency of the context's
+// bytecode, rebuilt with the adjacency.
+static int ensure_segments(pirgpu_ctx *ctx, BatchState *b) {
+  int r;
+  if ((r = ensure_events_graph(ctx, b))) return r;
+  if (b->seg_version == ctx->bytecode_version && b->seg_nvars == ctx->nvars) return PIR_OK;
+  const long long n = ctx->n;
+  const int nv = ctx->nvars;
+  Segments S;
+  if (!build_segments(n, nv, ctx->h_op.data(), ctx->h_x.data(), ctx->h_y.data(), ctx->h_z.data(),
+                      b->h_adj_ptr.data(), b->h_adj.data(), adjacency_threads(n, 0, nv), S))
+    return set_err(ctx, PIR_EINVAL, "event schedule: unit adjacency does not fit int32 offsets");
+  void *old[] = {b->d_uptr, b->d_uadj, b->d_seg_pptr, b->d_seg_code, b->d_seg_vptr, b->d_seg_var, b->d_in_seg,
+                 b->d_seg_umask};
+  for (void *q : old)
+    if (q) cudaFree(q);
+  b->d_uptr = b->d_uadj = b->d_seg_pptr = b->d_seg_code = b->d_seg_vptr = nullptr;
+  b->d_seg_var = b->d_in_seg = nullptr;
+  b->d_seg_umask = nullptr;
+  b->nseg = 0;
+  if (S.nseg > 0) {
+    auto up = [&](void **dst, const void *src, size_t bytes) -> int {
+      if (cudaMalloc(dst, std::max<size_t>(bytes, 4)) != cudaSuccess) {
+        cudaGetLastError();
+        *dst = nullptr;
+        return set_err(ctx, PIR_ENOMEM, "event segments");
+      }
+      if (bytes) PIR_CK(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+      return PIR_OK;
+    };
+    if ((r = up((void **)&b->d_uptr, S.uptr.data(), S.uptr.size() * 4)) ||
+        (r = up((void **)&b->d_uadj, S.uadj.data(), S.uadj.size() * 4)) ||
+        (r = up((void **)&b->d_seg_pptr, S.pptr.data(), S.pptr.size() * 4)) ||
+        (r = up((void **)&b->d_seg_code, S.code.data(), S.code.size() * 4)) ||
+        (r = up((void **)&b->d_seg_vptr, S.vptr.data(), S.vptr.size() * 4)) ||
+        (r = up((void **)&b->d_seg_var, S.var.data(), S.var.size() * 4)) ||
+        (r = up((void **)&b->d_in_seg, S.in_seg.data(), S.in_seg.size() * 4)) ||
+        (r = up((void **)&b->d_seg_umask, S.umask.data(), S.umask.size() * 8)))
+      return r;
+    PIR_CK(cudaStreamSynchronize(ctx->stream));
+    b->nseg = S.nseg;
+  }
+  b->seg_version = ctx->bytecode_version;
+  b->seg_nvars = nv;
+  return PIR_OK;
+}
+
+int events_graph(pirgpu_ctx *ctx, EventsGraph *g, bool segments) {
   BatchState *b = batch(ctx);
-  const int r = ensure_events_graph(ctx, b);
+  const int r = segments ? ensure_segments(ctx, b) : ensure_events_graph(ctx, b);
   if (r) return r;
-  *bc = b->d_bc4;
-  *adj_ptr = b->d_adj_ptr;
-  *adj = b->d_adj;
+  *g = EventsGraph();
+  g->bc = b->d_bc4;
+  g->adj_ptr = b->d_adj_ptr;
+  g->adj = b->d_adj;
+  g->uptr = b->d_adj_ptr;
+  g->uadj = b->d_adj;
+  if (segments && b->nseg > 0) {
+    g->nseg = b->nseg;
+    g->uptr = b->d_uptr;
+    g->uadj = b->d_uadj;
+    g->seg_pptr = b->d_seg_pptr;
+    g->seg_code = b->d_seg_code;
+    g->seg_vptr = b->d_seg_vptr;
+    g->seg_var = b->d_seg_var;
+    g->in_seg = b->d_seg_umask ? b->d_in_seg : nullptr;
+    g->seg_umask = b->d_seg_umask;
+  }
   return PIR_OK;
 }
 
@@ -916,34 +1247,43 @@ struct NodePlan {
 static int plan_nodes(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const pir_opts &opts, NodePlan *plan) {
   int r;
   if ((r = ensure_events_graph(ctx, b))) return r;
-  // variants 1..7: (threads per CTA, resident CTAs per SM the registers are sized for)
+  // variants 1..10: (threads per CTA, nodes per CTA -- 1: one node per CTA,
+  // else one per warp --, resident CTAs per SM the registers are sized for)
   struct NodeVariant {
-    int block;
+    int block, wpb;
     const void *fn;
   };
   static const NodeVariant kNodeVariants[] = {
-      {256, (const void *)k_nodes_events<256, 2>}, {256, (const void *)k_nodes_events<256, 3>},
-      {256, (const void *)k_nodes_events<256, 4>}, {256, (const void *)k_nodes_events<256, 6>},
-      {256, (const void *)k_nodes_events<256, 8>}, {128, (const void *)k_nodes_events<128, 8>},
-      {128, (const void *)k_nodes_events<128, 10>}};
+      {256, 1, (const void *)k_nodes_events<256, 2>}, {256, 1, (const void *)k_nodes_events<256, 3>},
+      {256, 1, (const void *)k_nodes_events<256, 4>}, {256, 1, (const void *)k_nodes_events<256, 6>},
+      {256, 1, (const void *)k_nodes_events<256, 8>}, {128, 1, (const void *)k_nodes_events<128, 8>},
+      {128, 1, (const void *)k_nodes_events<128, 10>}, {256, 8, (const void *)k_nodes_warp<8, 2>},
+      {256, 8, (const void *)k_nodes_warp<8, 3>},      {128, 4, (const void *)k_nodes_warp<4, 6>}};
   static_assert(sizeof(kNodeVariants) / sizeof(kNodeVariants[0]) == PIR_NODE_VARIANTS, "node variant count");
   const int nvar = opts.variant >= 1 && opts.variant <= PIR_NODE_VARIANTS ? opts.variant
                    : (b->node_variant > 0 ? b->node_variant : 6);
-  const int block = kNodeVariants[nvar - 1].block;
+  const int block = kNodeVariants[nvar - 1].block, wpb = kNodeVariants[nvar - 1].wpb;
   const void *kfn = kNodeVariants[nvar - 1].fn;
-  // the bitmap of narrowed variables, in shared memory while it takes at most 32 KB
+  // CTA per node: the bitmap of narrowed variables, in shared memory while it
+  // takes at most 32 KB; warp per node: its shared state
   const int words = (ctx->nvars + 31) / 32;
-  const int bitmap_words = words * 4 <= 32 * 1024 ? words : 0;
-  const size_t dyn_smem = bitmap_words ? (size_t)bitmap_words * 4 : ((size_t)1 << TOUCH_LOG) * sizeof(int);
+  const int bitmap_words = wpb == 1 && words * 4 <= 32 * 1024 ? words : 0;
+  const size_t dyn_smem = wpb > 1 ? (size_t)wpb * sizeof(WarpNodeShared)
+                          : bitmap_words ? (size_t)bitmap_words * 4 : ((size_t)1 << TOUCH_LOG) * sizeof(int);
+  if (dyn_smem > 48 * 1024)
+    PIR_CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem));
   int occ = 0;
   PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, block, dyn_smem));
   occ = std::max(occ, 1);
-  const int grid = std::max(1, std::min(nnodes, ctx->num_sms * (opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ)));
+  const int grid = std::max(1, std::min((nnodes + wpb - 1) / wpb,
+                                        ctx->num_sms * (opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ)));
   const size_t nv = (size_t)ctx->nvars, n = (size_t)std::max<long long>(ctx->n, 1);
-  // per-CTA scratch slots: ws | vmark | tmark | lists(3) | pstamp | cand | epochs
+  // per-node-in-flight scratch slots (a CTA's, or a warp's): ws | vmark |
+  // tmark | lists(3) | pstamp | cand | epochs
   const size_t per_cta = nv * 8 + nv * 4 * 2 + nv * 4 * 3 + n * 4 * 2;
-  if (b->ev_slots < grid || b->ev_nvars != ctx->nvars || b->ev_n != ctx->n) {
-    const int slots = std::max(grid, ctx->num_sms * occ);
+  const int need_slots = grid * wpb;
+  if (b->ev_slots < need_slots || b->ev_nvars != ctx->nvars || b->ev_n != ctx->n) {
+    const int slots = std::max(need_slots, ctx->num_sms * occ * wpb);
     const size_t need = per_cta * (size_t)slots + 64 * (size_t)slots + 256;
     if (b->d_ev) cudaFree(b->d_ev);
     b->d_ev = nullptr;
@@ -1029,7 +1369,7 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
     PIR_CK(cudaMemcpyAsync(d_ub, ub, ntight * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   }
   PIR_CK(cudaMemsetAsync(d_next, 0, 4 * sizeof(int), ctx->stream));
-  PIR_CK(cudaMemsetAsync(d_cnt, 0, 2 * sizeof(unsigned long long), ctx->stream));
+  PIR_CK(cudaMemsetAsync(d_cnt, 0, 4 * sizeof(unsigned long long), ctx->stream));
   int2 *d_out_store = nullptr;
   if (out_lb) {
     if ((r = ensure(ctx, (void **)&b->d_nstore, &b->cap_nstore, (size_t)nnodes * nv * sizeof(int2)))) return r;
@@ -1057,7 +1397,9 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
   a.out = b->d_nout;
   a.execs = d_cnt;
   a.narrowed = d_cnt + 1;
+  a.cert = d_cnt + 2;
   a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
+  a.certify = opts.certify >= 0;
   PIR_CK(cudaEventRecord(ctx->ev0, ctx->stream));
   if (need_ent) {
     k_entailed<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(b->d_bc4, ctx->n, ctx->d_store, b->d_ent);
@@ -1070,7 +1412,7 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
   PIR_CK(cudaGetLastError());
   PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   std::vector<NodeOut> hout(nnodes);
-  unsigned long long hcnt[2] = {0, 0};
+  unsigned long long hcnt[4] = {0, 0, 0, 0};
   PIR_CK(cudaMemcpyAsync(hout.data(), b->d_nout, nnodes * sizeof(NodeOut), cudaMemcpyDeviceToHost, ctx->stream));
   PIR_CK(cudaMemcpyAsync(hcnt, d_cnt, sizeof(hcnt), cudaMemcpyDeviceToHost, ctx->stream));
   std::vector<int2> hw;
@@ -1113,6 +1455,8 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
   }
   st.executions = (int64_t)hcnt[0];
   st.narrowed = (int64_t)hcnt[1];
+  st.certify_executions = (int64_t)hcnt[2];
+  st.certify_narrowed = (int64_t)hcnt[3];
   st.status = worst;
   if (stats) *stats = st;
   return PIR_OK;
@@ -1144,13 +1488,15 @@ static size_t pow2_at_least(size_t bytes) {
 
 // Staged batch layout.  In (int32, host and device alike): watch (nwatch) |
 // off (nnodes + 1) | var | lb | ub (ntight each).  Out (device, copied back
-// whole): execution and narrowing counters (2 x u64) | work counter (4 x
-// int) | NodeOut x nnodes | watched bounds int2 x nnodes x nwatch.
+// whole): counters (4 x u64: executions, narrowings, and the certifying
+// sweeps' executions and narrowings) | work counter (4 x int) | padding to 64
+// bytes | NodeOut x nnodes | watched bounds int2 x nnodes x nwatch.
+constexpr size_t STAGE_HDR = 64;
 static size_t stage_in_bytes(int32_t nnodes, int32_t ntight, int32_t nwatch) {
   return ((size_t)nwatch + (size_t)nnodes + 1 + 3 * (size_t)ntight) * sizeof(int32_t);
 }
 static size_t stage_out_bytes(int32_t nnodes, int32_t nwatch) {
-  return 32 + (size_t)nnodes * sizeof(NodeOut) + (size_t)nnodes * (size_t)nwatch * sizeof(int2);
+  return STAGE_HDR + (size_t)nnodes * sizeof(NodeOut) + (size_t)nnodes * (size_t)nwatch * sizeof(int2);
 }
 
 int nodes_stage(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch, int32_t **in) {
@@ -1174,7 +1520,7 @@ static int build_stage_graph(pirgpu_ctx *ctx, BatchState *b, size_t bytes_in, si
   ms.dst = b->d_sout;
   ms.value = 0;
   ms.elementSize = 4;
-  ms.width = 8;  // the counters: 32 bytes
+  ms.width = STAGE_HDR / 4;  // the counters
   ms.height = 1;
   cudaGraphNode_t clear, e0, e1;
   PIR_CK(cudaGraphAddMemsetNode(&clear, b->sg, nullptr, 0, &ms));
@@ -1193,7 +1539,7 @@ static int build_stage_graph(pirgpu_ctx *ctx, BatchState *b, size_t bytes_in, si
 }
 
 int nodes_run_staged(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch, const pir_opts &opts,
-                     int32_t *out_status, const int2 **wout, pir_stats *stats) {
+                     int32_t *out_status, int32_t *out_rounds, const int2 **wout, pir_stats *stats) {
   BatchState *b = batch(ctx);
   int r;
   NodePlan plan;
@@ -1214,11 +1560,13 @@ int nodes_run_staged(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nw
   a.nnodes = nnodes;
   a.execs = reinterpret_cast<unsigned long long *>(dout);
   a.narrowed = a.execs + 1;
-  a.next = reinterpret_cast<int *>(dout + 16);
-  a.out = reinterpret_cast<NodeOut *>(dout + 32);
-  a.out_watch = nwatch > 0 ? reinterpret_cast<int2 *>(dout + 32 + (size_t)nnodes * sizeof(NodeOut)) : nullptr;
+  a.cert = a.execs + 2;
+  a.next = reinterpret_cast<int *>(dout + 32);
+  a.out = reinterpret_cast<NodeOut *>(dout + STAGE_HDR);
+  a.out_watch = nwatch > 0 ? reinterpret_cast<int2 *>(dout + STAGE_HDR + (size_t)nnodes * sizeof(NodeOut)) : nullptr;
   a.out_store = nullptr;
   a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
+  a.certify = opts.certify >= 0;
   void *kargs[] = {&a};
   cudaKernelNodeParams kp{};
   kp.func = const_cast<void *>(plan.kfn);
@@ -1245,21 +1593,24 @@ int nodes_run_staged(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nw
   b->ent_store_version = ctx->store_version;
   b->ent_bc_version = ctx->bytecode_version;
   const unsigned long long *cnt = reinterpret_cast<const unsigned long long *>(b->h_sout);
-  const NodeOut *no = reinterpret_cast<const NodeOut *>(b->h_sout + 32);
+  const NodeOut *no = reinterpret_cast<const NodeOut *>(b->h_sout + STAGE_HDR);
   pir_stats st;
   std::memset(&st, 0, sizeof(st));
   PIR_CK(cudaEventElapsedTime(&st.device_ms, ctx->ev0, ctx->ev1));
   int worst = PIR_OK;
   for (int j = 0; j < nnodes; ++j) {
     out_status[j] = no[j].status;
+    if (out_rounds) out_rounds[j] = no[j].rounds;
     st.rounds = std::max<int64_t>(st.rounds, no[j].rounds);
     if (no[j].status == PIR_TIMEOUT) worst = PIR_TIMEOUT;
   }
   st.executions = (int64_t)cnt[0];
   st.narrowed = (int64_t)cnt[1];
+  st.certify_executions = (int64_t)cnt[2];
+  st.certify_narrowed = (int64_t)cnt[3];
   st.status = worst;
   if (stats) *stats = st;
-  *wout = reinterpret_cast<const int2 *>(b->h_sout + 32 + (size_t)nnodes * sizeof(NodeOut));
+  *wout = reinterpret_cast<const int2 *>(b->h_sout + STAGE_HDR + (size_t)nnodes * sizeof(NodeOut));
   return PIR_OK;
 }
 

@@ -11,6 +11,7 @@
 #define PIR_CSR_H
 
 #include <algorithm>
+#include <climits>
 #include <cstdint>
 #include <thread>
 #include <vector>
@@ -40,9 +41,16 @@ inline int adjacency_threads(long long n, int requested = 0, long long nvars = 0
   return t;
 }
 
+// The adjacency indexes its entries with int32 (ptr, the kernels' cursors):
+// at most INT32_MAX of them.
+inline bool adjacency_fits(long long entries) { return entries >= 0 && entries <= (long long)INT32_MAX; }
+
 // ptr: nv + 1 entries; adj: 3 n entries.  Variables must lie in [0, nv).
-inline void build_adjacency(long long n, int nv, const int32_t *x, const int32_t *y, const int32_t *z,
+// Returns false, writing nothing, when the 3 n entries do not fit int32
+// offsets (n > 715,827,882 propagators).
+inline bool build_adjacency(long long n, int nv, const int32_t *x, const int32_t *y, const int32_t *z,
                             int32_t *ptr, int32_t *adj, int nthreads) {
+  if (n < 0 || !adjacency_fits(3 * n)) return false;
   const int T = std::max(1, nthreads);
   std::vector<long long> lo(T + 1);
   for (int t = 0; t <= T; ++t) lo[t] = n * t / T;
@@ -88,6 +96,7 @@ inline void build_adjacency(long long n, int nv, const int32_t *x, const int32_t
       adj[c[(size_t)z[p]]++] = (int32_t)p;
     }
   });
+  return true;
 }
 
 // The PC event schedule's variable -> formula adjacency: adj[ptr[v] ..
@@ -97,8 +106,9 @@ inline void build_adjacency(long long n, int nv, const int32_t *x, const int32_t
 // formula once.  ptr: nv + 1 entries; adj is resized to the entry count.
 // Each thread walks a contiguous chunk of formulas (their distinct variables
 // sorted, which the adjacency does not see), then counts, cursors and fills
-// as build_adjacency does: the arrays equal a sequential build's.
-inline void build_formula_adjacency(int np, const int32_t *roots, const int32_t *tape, int nv, int32_t *ptr,
+// as build_adjacency does: the arrays equal a sequential build's.  Returns
+// false, writing nothing, when the entries do not fit int32 offsets.
+inline bool build_formula_adjacency(int np, const int32_t *roots, const int32_t *tape, int nv, int32_t *ptr,
                                     std::vector<int32_t> &adj, int nthreads) {
   const int T = std::max(1, nthreads);
   std::vector<long long> lo(T + 1);
@@ -145,6 +155,7 @@ inline void build_formula_adjacency(int np, const int32_t *roots, const int32_t 
     part[t + 1] = s;
   });
   for (int t = 0; t < T; ++t) part[t + 1] += part[t];
+  if (!adjacency_fits(part[T])) return false;
   ptr[0] = 0;
   run_threads(T, [&](int t) {
     long long s = part[t];
@@ -166,6 +177,7 @@ inline void build_formula_adjacency(int np, const int32_t *roots, const int32_t 
       for (int32_t q = st[r]; q < st[r + 1]; ++q) adj[(size_t)c[(size_t)vs[(size_t)q]]++] = (int32_t)i;
     }
   });
+  return true;
 }
 
 }  // namespace pirgpu

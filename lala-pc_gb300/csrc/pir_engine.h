@@ -72,6 +72,23 @@ void destroy_pc_state(pirgpu_ctx *ctx);
 int pc_max_var_used(const pirgpu_ctx *ctx);
 long long pc_count(const pirgpu_ctx *ctx);
 int pc_truncate(pirgpu_ctx *ctx, long long n);
+// The event schedules' view of the context's bytecode (engine order), built
+// on the host's threads once per bytecode version (pir_batch.cu): the AoS
+// bytecode, the variable -> propagator adjacency (CSR) and, for the
+// single-instance event kernel, the path segments with the variable -> unit
+// adjacency (pir_segments.h; equal to the propagator adjacency when there are
+// no segments).
+struct EventsGraph {
+  const int4 *bc = nullptr;
+  const int *adj_ptr = nullptr, *adj = nullptr;
+  int nseg = 0;
+  const int *uptr = nullptr, *uadj = nullptr;
+  const int *seg_pptr = nullptr, *seg_code = nullptr, *seg_vptr = nullptr;
+  const unsigned *seg_var = nullptr, *in_seg = nullptr;
+  const unsigned long long *seg_umask = nullptr;
+};
+int events_graph(pirgpu_ctx *ctx, EventsGraph *g, bool segments);
+
 int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);
 int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);
 // Records variables embedded since the last learned fixpoint (its "just

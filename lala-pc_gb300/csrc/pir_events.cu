@@ -4,54 +4,70 @@
 // lala-pc's driver sweeps every propagator until a sweep changes nothing
 // (GaussSeidelIteration around PIR::deduce(int), tests/pir_test.cpp:60-62);
 // the AC-1 kernels do the same, one sweep per round.  Here a round runs only
-// the propagators that have a variable narrowed in the previous round (the
-// first round runs all of them), found through the variable -> propagator
-// adjacency.  Every propagator of pir.hpp:721-817 reads only its three
-// intervals, so one whose intervals did not change since its last run (which
-// changed nothing) cannot change anything: the run ends at the same fixpoint,
-// or the same failure, as the sweeps, bit for bit (propagators are monotone,
-// so the order of the runs does not matter).
+// the units that have a variable narrowed in the previous round (the first
+// round runs all of them), found through the variable -> unit adjacency.
+// Every propagator of pir.hpp:721-817 reads only its three intervals, so one
+// whose intervals did not change since its last run (which changed nothing)
+// cannot change anything: the run ends at the same fixpoint, or the same
+// failure, as the sweeps, bit for bit (propagators are monotone, so the order
+// of the runs does not matter).  A final full round (the certifying sweep,
+// opts.certify) checks it.
+//
+// Units.  A unit is a propagator, or a segment: up to SEG_MAX propagators of
+// a path joined by link variables (variables with exactly two occurrences,
+// pir_segments.h).  A thread runs a propagator; a warp runs a segment: it
+// stages the segment's variables in shared memory, one lane sweeps the
+// segment's propagators forward and backward until none narrows anything,
+// and the warp joins what changed into the store and lists the units of the
+// changed variables that have occurrences outside the segment.  A segment
+// reached through a link variable is run at once by the same warp (chasing,
+// SEG_CHASE per entry).  A long chain x_{i+1} = x_i + c_i then costs a few
+// shared-memory accesses per link instead of dependent L2 round trips.
 //
 // Rounds with a large frontier run on the whole grid, separated by the grid
-// barrier.  A round whose frontier has at most `local_max` propagators runs
-// on CTA 0 alone, separated by __syncthreads, while the other CTAs wait at
-// the next grid barrier; CTA 0 hands back when the frontier grows or the run
-// ends.  Deep, narrow propagation (a long chain) then costs a block barrier
-// per round instead of a grid barrier.  Within a round, a thread that
-// narrows a variable with few propagators runs them itself at once (see
-// "Chasing" below), so a chain of such variables advances many links per
-// round: on 1M vars / 4M propagators plus a 20,000-link chain whose upper
-// bounds ripple back one link per round, ~20,000 rounds become a few hundred.
+// barrier.  A round whose frontier has at most `local_max` units runs on CTA
+// 0 alone, separated by __syncthreads, while the other CTAs wait at the next
+// grid barrier; CTA 0 hands back when the frontier grows or the run ends.
+// Within a round, a thread that narrows a variable with few units runs its
+// propagators itself at once ("Chasing" below).
 #include <algorithm>
+#include <climits>
 #include <cstring>
 
 #include "pir_engine.h"
 #include "pir_kernels.cuh"
+#include "pir_segments.h"
 
 namespace pirgpu {
-
-// Engine-order AoS bytecode and the variable -> propagator adjacency (CSR),
-// built once per bytecode version (pir_batch.cu).
-int events_graph(pirgpu_ctx *ctx, const int4 **bc, const int **adj_ptr, const int **adj);
 
 namespace {
 
 constexpr int EV_CONTINUE = 0, EV_FIXPOINT = 1, EV_FAILED = 2, EV_CAP = 3, EV_ERROR = 4;
 constexpr int CNT_STRIDE = 32;  // counters one 128-byte line apart
+constexpr int EV_BLOCK = 256, EV_WARPS = EV_BLOCK / 32;
+constexpr int NO_UNIT = INT_MIN;  // an empty slot among units (a segment s is ~s, never INT_MIN)
 
 struct EvFixArgs {
   const int4 *bc;  // {op, x, y, z} per propagator
-  const int *adj_ptr, *adj;
+  const int *adj_ptr, *adj;  // variable -> unit adjacency: propagator p as p, segment s as ~s
   int2 *store;
   unsigned *pstamp;  // per propagator: the last round it is listed for
-  unsigned *vstamp;  // per variable: the last round its propagators were listed for
-  int *list0, *list1;  // frontier of round r: list0 for even r, list1 for odd r
+  unsigned *sstamp;  // per segment: the last round it is listed for
+  unsigned *vstamp;  // per variable: the last round its units were listed for
+  int *list0, *list1;  // frontier (units) of round r: list0 for even r, list1 for odd r
   unsigned *cnt;     // frontier sizes: round r in cnt[(r % 3) * CNT_STRIDE]
   Control *ctl;
   long long n;
   long long max_rounds, timeout_ns;
   unsigned local_max;
   int chase;  // runs chased per frontier entry (0: none)
+  int certify;  // end with a full round (every unit once) that narrows nothing
+  // path segments (nseg = 0: none; pir_segments.h)
+  int nseg;
+  const int *seg_pptr, *seg_code, *seg_vptr;
+  const unsigned *seg_var, *in_seg;
+  const unsigned long long *seg_umask;
+  int *seg_busy;  // per segment: 1 while a warp runs it
 };
 
 __device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
@@ -60,22 +76,26 @@ __device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
   return v;
 }
 
-// Chasing.  A run that narrows a variable with at most CHASE_DEG
-// propagators runs them itself at once (up to `chase` runs per frontier
+// Chasing.  A run that narrows a variable with at most CHASE_DEG units runs
+// the propagators among them itself at once (up to `chase` runs per frontier
 // entry, CHASE_CAP pending, in shared memory) instead of leaving them to the
-// next round; every other narrowed variable has its propagators listed for
-// the next round, and so has whatever is still pending when the runs run
-// out.  A run is first repeated on its own results (up to CLOSE_RUNS runs;
-// past that the propagator is listed), so the propagator that narrowed a
-// variable is not chased with the variable's others.  Every propagator of a
-// narrowed variable thus runs after the narrowing, at once or in the next
-// round, which is all the event schedule needs (the propagators are
-// monotone).  A deep chain of small variables then advances up to `chase`
-// links per round instead of one.
+// next round; every other narrowed variable has its units listed for the
+// next round, and so has whatever is still pending when the runs run out.
+// A run is first repeated on its own results (up to CLOSE_RUNS runs; past
+// that the propagator is listed), so the propagator that narrowed a variable
+// is not chased with the variable's others.  Every unit of a narrowed
+// variable thus runs after the narrowing, at once or in the next round,
+// which is all the event schedule needs (the propagators are monotone).
 // The budget is capped: a chase is dependent L2 round trips (a few us each,
 // more when many chasers narrow the same variables), and the grid's other
 // CTAs wait for the round at a barrier with a time limit.
 constexpr int CHASE_DEG = 4, CHASE_CAP = 8, CLOSE_RUNS = 4, CHASE_DEFAULT = 64, CHASE_MAX = 256, DEFER_CAP = 8;
+
+// Segments: sweeps per run before the rest waits for the next round,
+// segments chased per frontier entry, the chase stack of a warp, and the
+// frontier's segments a CTA queues for its warps per round (more wait for the
+// next round).
+constexpr int SEG_PASSES = 16, SEG_CHASE = 32, SEG_STACK = 8, SEG_QUEUE = 256;
 
 // One run's joins: red to the store as RedStore does, and the run's view of
 // its three variables (the intervals it read, met with what it joined) for
@@ -118,48 +138,49 @@ struct RunView {
 };
 
 // Listing policy of the grid rounds: the first narrowing of a variable in
-// round r lists its propagators for round r + 1 (the round stamps keep every
-// variable expanded, and every propagator listed, at most once per round).
-// The adjacency is walked EXPAND entries at a time: their loads and stamp
+// round r lists its units for round r + 1 (the round stamps keep every
+// variable expanded, and every unit listed, at most once per round).  The
+// adjacency is walked EXPAND entries at a time: their loads and stamp
 // atomics are independent (one memory round trip each per batch, not per
 // entry), and the batch takes its list slots with one atomic.
 constexpr int EXPAND = 8;
 
 struct EvSched {
   const int *adj;
-  unsigned *pstamp, *vstamp;
+  unsigned *pstamp, *sstamp, *vstamp;
   int *next;
   unsigned *next_cnt;
   unsigned next_round;
-  __device__ __forceinline__ void list_prop(int q) const {
-    if (atomicMax(pstamp + q, next_round) < next_round) next[atomicAdd(next_cnt, 1u)] = q;
+  __device__ __forceinline__ bool claim(int u) const {
+    return atomicMax(u >= 0 ? pstamp + u : sstamp + ~u, next_round) < next_round;
   }
-  // Lists the cnt (<= DEFER_CAP) propagators buf[0], buf[stride], ...
+  __device__ __forceinline__ void list_unit(int u) const {
+    if (claim(u)) next[atomicAdd(next_cnt, 1u)] = u;
+  }
+  // Lists the cnt (<= DEFER_CAP) units buf[0], buf[stride], ...
   __device__ __forceinline__ void list_batch(const int *buf, int cnt, int stride) const {
     int q[DEFER_CAP];
     unsigned take = 0;
 #pragma unroll
-    for (int j = 0; j < DEFER_CAP; ++j) q[j] = j < cnt ? buf[j * stride] : -1;
+    for (int j = 0; j < DEFER_CAP; ++j) q[j] = j < cnt ? buf[j * stride] : NO_UNIT;
 #pragma unroll
     for (int j = 0; j < DEFER_CAP; ++j)
-      if (q[j] >= 0 && atomicMax(pstamp + q[j], next_round) < next_round) take |= 1u << j;
+      if (q[j] != NO_UNIT && claim(q[j])) take |= 1u << j;
     if (!take) return;
     unsigned slot = atomicAdd(next_cnt, (unsigned)__popc(take));
 #pragma unroll
     for (int j = 0; j < DEFER_CAP; ++j)
       if (take & (1u << j)) next[slot++] = q[j];
   }
-  // Lists v's propagators (adjacency range r) for the next round.
-  __device__ __forceinline__ void schedule(int v, int2 r) const {
-    if (atomicMax(vstamp + v, next_round) >= next_round) return;
+  __device__ __forceinline__ void expand(int2 r, int skip) const {
     for (int k0 = r.x; k0 < r.y; k0 += EXPAND) {
       int q[EXPAND];
 #pragma unroll
-      for (int j = 0; j < EXPAND; ++j) q[j] = k0 + j < r.y ? __ldg(adj + k0 + j) : -1;
+      for (int j = 0; j < EXPAND; ++j) q[j] = k0 + j < r.y ? __ldg(adj + k0 + j) : NO_UNIT;
       unsigned take = 0;
 #pragma unroll
       for (int j = 0; j < EXPAND; ++j)
-        if (q[j] >= 0 && atomicMax(pstamp + q[j], next_round) < next_round) take |= 1u << j;
+        if (q[j] != NO_UNIT && q[j] != skip && claim(q[j])) take |= 1u << j;
       if (!take) continue;
       unsigned slot = atomicAdd(next_cnt, (unsigned)__popc(take));
 #pragma unroll
@@ -167,12 +188,22 @@ struct EvSched {
         if (take & (1u << j)) next[slot++] = q[j];
     }
   }
+  // Lists v's units (adjacency range r) for the next round.
+  __device__ __forceinline__ void schedule(int v, int2 r) const {
+    if (atomicMax(vstamp + v, next_round) >= next_round) return;
+    expand(r, NO_UNIT);
+  }
+  // The same for a variable a segment narrowed, without the segment itself
+  // (it left its variables at its own fixpoint), and without the variable's
+  // stamp: a later narrowing of v in this round must still list the segment.
+  __device__ __forceinline__ void schedule_but(int v, int2 r, int skip) const { expand(r, skip); }
 };
 
 __device__ __forceinline__ EvSched ev_sched(const EvFixArgs &a, long long round) {
   EvSched sc;
   sc.adj = a.adj;
   sc.pstamp = a.pstamp;
+  sc.sstamp = a.sstamp;
   sc.vstamp = a.vstamp;
   sc.next = ((round + 1) & 1) ? a.list1 : a.list0;
   sc.next_cnt = a.cnt + ((round + 1) % 3) * CNT_STRIDE;
@@ -180,13 +211,14 @@ __device__ __forceinline__ EvSched ev_sched(const EvFixArgs &a, long long round)
   return sc;
 }
 
-// Runs frontier entry q and what it chases (stack: this thread's CHASE_CAP
-// slots, blockDim.x apart; defer: its DEFER_CAP slots).  Returns the bounds
-// narrowed.  A run whose variable is chased is itself listed for the next
-// round: its repeat on its own results does not see what a concurrent run of
-// the same propagator joined, and the next round reads the store after the
-// barrier.  Those listings wait in `defer` and go out DEFER_CAP at a time
-// (their stamp atomics in flight together), off the chase's critical path.
+// Runs frontier propagator q and what it chases (stack: this thread's
+// CHASE_CAP slots, blockDim.x apart; defer: its DEFER_CAP slots).  Returns
+// the bounds narrowed.  A run whose variable is chased is itself listed for
+// the next round: its repeat on its own results does not see what a
+// concurrent run of the same propagator joined, and the next round reads the
+// store after the barrier.  Those listings wait in `defer` and go out
+// DEFER_CAP at a time (their stamp atomics in flight together), off the
+// chase's critical path.  Segments met on the way are listed.
 template <class Sched>
 __device__ __forceinline__ int run_entry(int q, const EvFixArgs &a, const Sched &sc, int *stack, int *defer,
                                          int budget, unsigned long long &execs, int &failed) {
@@ -220,7 +252,7 @@ __device__ __forceinline__ int run_entry(int q, const EvFixArgs &a, const Sched 
       o2 = w.n[2];
     }
     if (failed) return changed;  // the round fails
-    if (k == close) sc.list_prop(q);
+    if (k == close) sc.list_unit(q);
     bool chased = false;
     // each distinct variable once (a hit marks every slot of its variable)
     if (b.z == b.y) hit &= ~2u;
@@ -235,8 +267,13 @@ __device__ __forceinline__ int run_entry(int q, const EvFixArgs &a, const Sched 
 #pragma unroll
         for (int j = 0; j < CHASE_DEG; ++j) e[j] = j < deg ? __ldg(a.adj + r.x + j) : q;
 #pragma unroll
-        for (int j = 0; j < CHASE_DEG; ++j)
-          if (e[j] != q) stack[(sp++) * stride] = e[j];
+        for (int j = 0; j < CHASE_DEG; ++j) {
+          if (e[j] == q) continue;
+          if (e[j] >= 0)
+            stack[(sp++) * stride] = e[j];
+          else
+            sc.list_unit(e[j]);  // a segment: a warp runs it next round
+        }
         chased = true;
       } else {
         sc.schedule(v, r);
@@ -251,7 +288,7 @@ __device__ __forceinline__ int run_entry(int q, const EvFixArgs &a, const Sched 
     }
     if (sp == 0) break;
     if (budget <= 0) {
-      while (sp > 0) sc.list_prop(stack[(--sp) * stride]);
+      while (sp > 0) sc.list_unit(stack[(--sp) * stride]);
       break;
     }
     q = stack[(--sp) * stride];
@@ -261,38 +298,255 @@ __device__ __forceinline__ int run_entry(int q, const EvFixArgs &a, const Sched 
   return changed;
 }
 
+// ------------------------------------------------------------- segments ----
+
+// A warp's shared-memory workspace for one segment.
+struct SegWork {
+  int2 iv[SEG_VARS];                   // the segment's intervals, as its sweeps leave them
+  int2 orig[SEG_VARS];                 // as read from the store
+  unsigned long long umask[SEG_VARS];  // per local variable: the segment's propagators using it
+  unsigned var[SEG_VARS];              // global variable | SEG_BOUNDARY
+  int code[SEG_MAX];                   // op | slot_x << 8 | slot_y << 16 | slot_z << 24
+  int stack[SEG_STACK];                // segments to chase
+  int sp;
+};
+
+// The frontier segments a CTA queues in a round for its warps (one queue per
+// round parity: the other is reset while this one is in use).
+struct SegQueue {
+  int q[SEG_QUEUE];
+  int n, head;
+};
+
+// The sweeps' store: the segment's intervals in shared memory (one lane).  A
+// narrowing meets into the current interval and marks the propagators of
+// the segment that use the variable (the narrowing one too: a propagator
+// need not be idempotent) for another run.
+struct SegStore {
+  int2 *iv;
+  const unsigned long long *umask;
+  unsigned long long dirty;
+  __device__ __forceinline__ Itv load(int i) const {
+    const int2 t = iv[i];
+    return mk(t.x, t.y);
+  }
+  __device__ __forceinline__ int embed(int i, Itv, Itv r, int &failed) {
+    const int2 t = iv[i];
+    const int nl = max(t.x, r.l), nu = min(t.y, r.u);
+    const int c = (nl != t.x) + (nu != t.y);
+    if (c) {
+      iv[i] = make_int2(nl, nu);
+      dirty |= umask[i];
+      if (is_bot(mk(nl, nu))) failed = 1;
+    }
+    return c;
+  }
+};
+
+__device__ __forceinline__ void seg_run_one(const SegWork &w, SegStore &st, int k, int &failed) {
+  const unsigned c = (unsigned)w.code[k];
+  st.dirty &= ~(1ull << k);
+  deduce((int)(c & 0xFFu), (int)((c >> 8) & 0xFFu), (int)((c >> 16) & 0xFFu), (int)(c >> 24), st, failed);
+}
+
+// Runs segment s on the calling warp (all 32 lanes): stage, sweep, join, and
+// list (or push on the warp's chase stack, when `chase`) the units of the
+// changed variables that have occurrences outside the segment.  Returns this
+// lane's count of bounds narrowed in the store.
+template <class Sched>
+__device__ int run_segment(const EvFixArgs &a, const Sched &sc, int s, SegWork &w, bool chase,
+                           unsigned long long &execs, int &failed) {
+  const int lane = threadIdx.x & 31;
+  int got = 0;
+  if (lane == 0) got = atomicCAS(a.seg_busy + s, 0, 1) == 0;
+  got = __shfl_sync(0xFFFFFFFFu, got, 0);
+  if (!got) {  // another warp runs it: it runs again next round
+    if (lane == 0) sc.list_unit(~s);
+    return 0;
+  }
+  const int p0 = __ldg(a.seg_pptr + s), np = __ldg(a.seg_pptr + s + 1) - p0;
+  const int v0 = __ldg(a.seg_vptr + s), nl = __ldg(a.seg_vptr + s + 1) - v0;
+  for (int i = lane; i < nl; i += 32) {
+    const unsigned gv = __ldg(a.seg_var + v0 + i);
+    const int2 t = __ldcg(a.store + (int)(gv & ~SEG_BOUNDARY));
+    w.var[i] = gv;
+    w.iv[i] = t;
+    w.orig[i] = t;
+    w.umask[i] = __ldg(a.seg_umask + v0 + i);
+  }
+  for (int k = lane; k < np; k += 32) w.code[k] = __ldg(a.seg_code + p0 + k);
+  __syncwarp();
+  int fl = 0, conv = 1;
+  if (lane == 0) {
+    SegStore st{w.iv, w.umask, np >= 64 ? ~0ull : ((1ull << np) - 1ull)};
+    unsigned long long ex = 0;
+    for (int pass = 0; st.dirty && !fl && pass < SEG_PASSES; ++pass) {
+      for (int k = 0; k < np && !fl; ++k)
+        if ((st.dirty >> k) & 1ull) {
+          seg_run_one(w, st, k, fl);
+          ++ex;
+        }
+      for (int k = np - 1; k >= 0 && !fl; --k)
+        if ((st.dirty >> k) & 1ull) {
+          seg_run_one(w, st, k, fl);
+          ++ex;
+        }
+    }
+    conv = st.dirty == 0ull;
+    execs += ex;
+  }
+  __syncwarp();
+  fl = __shfl_sync(0xFFFFFFFFu, fl, 0);
+  conv = __shfl_sync(0xFFFFFFFFu, conv, 0);
+  int changed = 0;
+  for (int i = lane; i < nl; i += 32) {
+    const int2 o = w.orig[i], t = w.iv[i];
+    const bool lo = t.x > o.x, hi = t.y < o.y;
+    if (!lo && !hi) continue;
+    const unsigned gv = w.var[i];
+    const int v = (int)(gv & ~SEG_BOUNDARY);
+    if (lo) asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(&a.store[v].x), "r"(t.x) : "memory");
+    if (hi) asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(&a.store[v].y), "r"(t.y) : "memory");
+    changed += (int)lo + (int)hi;
+    if (!(gv & SEG_BOUNDARY) || fl) continue;
+    const int2 r = make_int2(__ldg(a.adj_ptr + v), __ldg(a.adj_ptr + v + 1));
+    if (r.y - r.x == 2) {
+      // a link variable: the one other unit
+      const int u0 = __ldg(a.adj + r.x), u1 = __ldg(a.adj + r.x + 1);
+      const int other = u0 == ~s ? u1 : u0;
+      if (chase && other < 0) {
+        const int k = atomicAdd(&w.sp, 1);
+        if (k < SEG_STACK) {
+          w.stack[k] = ~other;
+          continue;
+        }
+      }
+      sc.list_unit(other);
+    } else {
+      sc.schedule_but(v, r, ~s);
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    __threadfence();
+    atomicExch(a.seg_busy + s, 0);
+    if (!conv && !fl) sc.list_unit(~s);  // sweeps left over: the rest next round
+  }
+  failed |= fl;
+  return changed;
+}
+
+// Runs segment s and the segments it chases (SEG_CHASE per entry, none
+// when chasing is off) on the calling warp.
+template <class Sched>
+__device__ int run_segment_chain(const EvFixArgs &a, const Sched &sc, int s, SegWork &w,
+                                 unsigned long long &execs, int &failed) {
+  const int lane = threadIdx.x & 31;
+  int budget = a.chase > 0 ? SEG_CHASE : 0, changed = 0;
+  if (lane == 0) w.sp = 0;
+  __syncwarp();
+  for (;;) {
+    changed += run_segment(a, sc, s, w, budget > 0, execs, failed);
+    __syncwarp();
+    const int sp = min(w.sp, SEG_STACK);
+    if (sp == 0 || failed) break;
+    if (budget <= 0) {
+      for (int i = lane; i < sp; i += 32) sc.list_unit(~w.stack[i]);
+      break;
+    }
+    --budget;
+    s = w.stack[sp - 1];
+    __syncwarp();
+    if (lane == 0) w.sp = sp - 1;
+    __syncwarp();
+  }
+  return changed;
+}
+
+// The warp phase of a round: a full round runs every segment (warps of the
+// grid strided), another round the segments its CTA queued.
+template <class Sched>
+__device__ int run_segment_phase(const EvFixArgs &a, const Sched &sc, bool full, long long first_warp,
+                                 long long nwarps, SegQueue &q, SegWork *work, unsigned long long &execs,
+                                 int &failed) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  SegWork &w = work[warp];
+  int changed = 0;
+  // the lanes' own failures (from their propagators) made warp-uniform: the
+  // segment code below runs on whole warps
+  failed = __any_sync(0xFFFFFFFFu, failed) ? 1 : 0;
+  if (full) {
+    for (long long s = first_warp; s < a.nseg && !failed; s += nwarps)
+      changed += run_segment_chain(a, sc, (int)s, w, execs, failed);
+    return changed;
+  }
+  const int items = min(q.n, SEG_QUEUE);
+  for (;;) {
+    int k = 0;
+    if (lane == 0) k = atomicAdd(&q.head, 1);
+    k = __shfl_sync(0xFFFFFFFFu, k, 0);
+    if (k >= items || failed) break;
+    changed += run_segment_chain(a, sc, q.q[k], w, execs, failed);
+  }
+  return changed;
+}
+
+// A frontier entry that is a segment: queued for the CTA's warps this round,
+// or, with the queue full, listed for the next.
+template <class Sched>
+__device__ __forceinline__ void queue_segment(int u, SegQueue &q, const Sched &sc) {
+  const int k = atomicAdd(&q.n, 1);
+  if (k < SEG_QUEUE)
+    q.q[k] = ~u;
+  else
+    sc.list_unit(u);
+}
+
+__device__ __forceinline__ bool in_segment(const EvFixArgs &a, long long p) {
+  return a.nseg && ((__ldg(a.in_seg + (p >> 5)) >> (p & 31)) & 1u);
+}
+
 // Runs the frontier entries i = first, first + stride, ... < items of round
-// `round` (round 0: every propagator).  Returns the bounds narrowed.
-__device__ __forceinline__ int run_frontier(const EvFixArgs &a, long long round, long long items, long long first,
-                                            long long stride, int *stack, int *defer, unsigned long long &execs,
-                                            int &failed) {
+// `round` (a full round, such as round 0: every propagator that is not in a
+// segment; segments go to the queue).  Returns the bounds narrowed.
+__device__ __forceinline__ int run_frontier(const EvFixArgs &a, long long round, bool full, long long items,
+                                            long long first, long long stride, int *stack, int *defer,
+                                            SegQueue &sq, unsigned long long &execs, int &failed) {
   const EvSched sc = ev_sched(a, round);
   const int *cur = (round & 1) ? a.list1 : a.list0;
   int changed = 0;
   for (long long i = first; i < items && !failed; i += stride) {
-    const int q = round == 0 ? (int)i : __ldcg(cur + i);
-    changed += run_entry(q, a, sc, stack, defer, a.chase, execs, failed);
+    if (full) {
+      if (in_segment(a, i)) continue;
+      changed += run_entry((int)i, a, sc, stack, defer, a.chase, execs, failed);
+    } else {
+      const int u = __ldcg(cur + i);
+      if (u < 0)
+        queue_segment(u, sq, sc);
+      else
+        changed += run_entry(u, a, sc, stack, defer, a.chase, execs, failed);
+    }
   }
   return changed;
 }
 
 // Rounds run by CTA 0 alone keep their bookkeeping in shared memory: the
 // frontier's first LOCAL_CAP entries, the list counters, and the round's
-// sets of expanded variables and listed propagators (open addressing, at
-// most L_PROBE probes).  Every listed propagator's index also goes to the
-// global list (a store nobody waits on), so a round whose frontier outgrows
-// local_max hands over to the grid as it is.  A key that finds no free slot
-// in its probe window falls back to the global round stamps; since slots
-// only fill during a round, every thread that meets that key takes the same
-// route, and each propagator is still listed at most once per round.  The
-// stamps hold round numbers, which only grow, so the rounds run here leave
-// them valid for later rounds.
+// sets of expanded variables and listed units (open addressing, at most
+// L_PROBE probes).  Every listed unit also goes to the global list (a store
+// nobody waits on), so a round whose frontier outgrows local_max hands over
+// to the grid as it is.  A key that finds no free slot in its probe window
+// falls back to the global round stamps; since slots only fill during a
+// round, every thread that meets that key takes the same route, and each
+// unit is still listed at most once per round.  The stamps hold round
+// numbers, which only grow, so the rounds run here leave them valid for later
+// rounds.
 constexpr int LOCAL_CAP = 256, LV_LOG = 10, LP_LOG = 11, L_PROBE = 16;
 
 struct LocalShared {
   int q[2][LOCAL_CAP];       // frontier, by round parity
   int vset[2][1 << LV_LOG];  // variables expanded, by round parity
-  int pset[2][1 << LP_LOG];  // propagators listed, by round parity
+  int pset[2][1 << LP_LOG];  // units listed, by round parity
   unsigned cnt[3], bits[3];  // list sizes and changed | failed bits, round % 3
 };
 
@@ -313,38 +567,36 @@ __device__ __forceinline__ int local_insert(int *tab, int key) {
 // the list head in shared memory.
 struct LocalSched {
   const int *adj;
-  unsigned *pstamp, *vstamp;
+  unsigned *pstamp, *sstamp, *vstamp;
   int *next;           // global list of the next round
   int *next_q;         // its first LOCAL_CAP entries (shared)
   unsigned *next_cnt;  // shared
   int *vset, *pset;    // this round's sets (shared)
   unsigned next_round;
-  __device__ __forceinline__ bool claim(int q) const {
-    const int t = local_insert<LP_LOG>(pset, q);
-    return t > 0 || (t < 0 && atomicMax(pstamp + q, next_round) < next_round);
+  int n;               // propagators: segment s has the set key n + s
+  __device__ __forceinline__ bool claim(int u) const {
+    const int t = local_insert<LP_LOG>(pset, u >= 0 ? u : n + ~u);
+    return t > 0 || (t < 0 && atomicMax(u >= 0 ? pstamp + u : sstamp + ~u, next_round) < next_round);
   }
-  __device__ __forceinline__ void append(int q, unsigned slot) const {
-    next[slot] = q;
-    if (slot < (unsigned)LOCAL_CAP) next_q[slot] = q;
+  __device__ __forceinline__ void append(int u, unsigned slot) const {
+    next[slot] = u;
+    if (slot < (unsigned)LOCAL_CAP) next_q[slot] = u;
   }
-  __device__ __forceinline__ void list_prop(int q) const {
-    if (claim(q)) append(q, atomicAdd(next_cnt, 1u));
+  __device__ __forceinline__ void list_unit(int u) const {
+    if (claim(u)) append(u, atomicAdd(next_cnt, 1u));
   }
   __device__ __forceinline__ void list_batch(const int *buf, int cnt, int stride) const {
-    for (int j = 0; j < cnt; ++j) list_prop(buf[j * stride]);
+    for (int j = 0; j < cnt; ++j) list_unit(buf[j * stride]);
   }
-  __device__ __forceinline__ void schedule(int v, int2 r) const {
-    const int fresh = local_insert<LV_LOG>(vset, v);
-    if (fresh == 0) return;
-    if (fresh < 0 && atomicMax(vstamp + v, next_round) >= next_round) return;
+  __device__ __forceinline__ void expand(int2 r, int skip) const {
     for (int k0 = r.x; k0 < r.y; k0 += EXPAND) {
       int q[EXPAND];
 #pragma unroll
-      for (int j = 0; j < EXPAND; ++j) q[j] = k0 + j < r.y ? __ldg(adj + k0 + j) : -1;
+      for (int j = 0; j < EXPAND; ++j) q[j] = k0 + j < r.y ? __ldg(adj + k0 + j) : NO_UNIT;
       unsigned take = 0;
 #pragma unroll
       for (int j = 0; j < EXPAND; ++j)
-        if (q[j] >= 0 && claim(q[j])) take |= 1u << j;
+        if (q[j] != NO_UNIT && q[j] != skip && claim(q[j])) take |= 1u << j;
       if (!take) continue;
       unsigned slot = atomicAdd(next_cnt, (unsigned)__popc(take));
 #pragma unroll
@@ -352,6 +604,13 @@ struct LocalSched {
         if (take & (1u << j)) append(q[j], slot++);
     }
   }
+  __device__ __forceinline__ void schedule(int v, int2 r) const {
+    const int fresh = local_insert<LV_LOG>(vset, v);
+    if (fresh == 0) return;
+    if (fresh < 0 && atomicMax(vstamp + v, next_round) >= next_round) return;
+    expand(r, NO_UNIT);
+  }
+  __device__ __forceinline__ void schedule_but(int v, int2 r, int skip) const { expand(r, skip); }
 };
 
 // CTA 0 alone: rounds separated by one __syncthreads each while the frontier
@@ -360,8 +619,8 @@ struct LocalSched {
 // the outcome to the control block, and on a hand-over the frontier size to
 // the global counter (thread 0; the writes precede its release at the next
 // grid barrier).
-__device__ void run_local(const EvFixArgs &a, long long round, int *stack, int *defer, unsigned long long &execs,
-                          unsigned long long &narrowed) {
+__device__ void run_local(const EvFixArgs &a, long long round, int *stack, int *defer, SegQueue *sq, SegWork *work,
+                          unsigned long long &execs, unsigned long long &narrowed) {
   __shared__ LocalShared sh;
   const int tid = threadIdx.x;
   for (int i = tid; i < (1 << LV_LOG); i += blockDim.x) sh.vset[0][i] = sh.vset[1][i] = -1;
@@ -385,17 +644,20 @@ __device__ void run_local(const EvFixArgs &a, long long round, int *stack, int *
     const int p = (int)(round & 1), r3 = (int)(round % 3), n3 = (int)((round + 1) % 3), c3 = (int)((round + 2) % 3);
     const unsigned items = sh.cnt[r3];
     if (items > a.local_max) break;
-    // the parity p ^ 1 sets served round - 1; counter c3 was read before the
-    // last barrier, bits n3 (round - 2's) right after the one before it
+    // the parity p ^ 1 sets and segment queue served round - 1; counter c3
+    // was read before the last barrier, bits n3 (round - 2's) right after the
+    // one before it
     for (int i = tid; i < (1 << LV_LOG); i += blockDim.x) sh.vset[p ^ 1][i] = -1;
     for (int i = tid; i < (1 << LP_LOG); i += blockDim.x) sh.pset[p ^ 1][i] = -1;
     if (tid == 0) {
       sh.cnt[c3] = 0u;
       sh.bits[n3] = 0u;
+      sq[p ^ 1].n = sq[p ^ 1].head = 0;
     }
     LocalSched sc;
     sc.adj = a.adj;
     sc.pstamp = a.pstamp;
+    sc.sstamp = a.sstamp;
     sc.vstamp = a.vstamp;
     sc.next = ((round + 1) & 1) ? a.list1 : a.list0;
     sc.next_q = sh.q[p ^ 1];
@@ -403,11 +665,19 @@ __device__ void run_local(const EvFixArgs &a, long long round, int *stack, int *
     sc.vset = sh.vset[p];
     sc.pset = sh.pset[p];
     sc.next_round = (unsigned)(round + 1);
+    sc.n = (int)a.n;
     const int *cur = p ? a.list1 : a.list0;
     int failed = 0, changed = 0;
     for (unsigned i = tid; i < items && !failed; i += blockDim.x) {
-      const int q = i < (unsigned)LOCAL_CAP ? sh.q[p][i] : __ldcg(cur + i);
-      changed += run_entry(q, a, sc, stack, defer, a.chase, execs, failed);
+      const int u = i < (unsigned)LOCAL_CAP ? sh.q[p][i] : __ldcg(cur + i);
+      if (u < 0)
+        queue_segment(u, sq[p], sc);
+      else
+        changed += run_entry(u, a, sc, stack, defer, a.chase, execs, failed);
+    }
+    if (a.nseg) {
+      __syncthreads();
+      changed += run_segment_phase(a, sc, false, 0, 0, sq[p], work, execs, failed);
     }
     narrowed += changed;
     const unsigned bits = __reduce_or_sync(0xFFFFFFFFu, (changed ? 1u : 0u) | (failed ? 2u : 0u));
@@ -430,35 +700,54 @@ __device__ void run_local(const EvFixArgs &a, long long round, int *stack, int *
     }
   }
   if (tid == 0) {
-    if (state == EV_CONTINUE) {
-      // the grid runs round `round` from the global list
-      a.cnt[(round % 3) * CNT_STRIDE] = sh.cnt[round % 3];
-      a.cnt[((round + 1) % 3) * CNT_STRIDE] = 0u;
-    }
+    // the grid runs round `round` from the global list (or, after a fixpoint,
+    // a full certifying round); it lists into the counter of round + 1
+    if (state == EV_CONTINUE) a.cnt[(round % 3) * CNT_STRIDE] = sh.cnt[round % 3];
+    a.cnt[((round + 1) % 3) * CNT_STRIDE] = 0u;
     a.ctl->ev_round = round;
     a.ctl->ev_state = state;
   }
 }
 
-__global__ void __launch_bounds__(256, 2) k_fixpoint_events(EvFixArgs a) {
+// Dynamic shared memory: one segment workspace per warp (only when the
+// bytecode has segments).
+__global__ void __launch_bounds__(EV_BLOCK, 2) k_fixpoint_events(EvFixArgs a) {
   __shared__ unsigned s_bits[2], s_word[2];
-  __shared__ int s_stack[CHASE_CAP * 256], s_defer[DEFER_CAP * 256];
+  __shared__ int s_stack[CHASE_CAP * EV_BLOCK], s_defer[DEFER_CAP * EV_BLOCK];
+  __shared__ SegQueue s_sq[2];
+  extern __shared__ unsigned long long s_dyn_ev[];
+  SegWork *work = reinterpret_cast<SegWork *>(s_dyn_ev);
   const int tid = threadIdx.x;
   const long long gtid = blockIdx.x * (long long)blockDim.x + tid;
   const long long gstride = (long long)gridDim.x * blockDim.x;
-  unsigned long long execs = 0, narrowed = 0;
+  const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
+  unsigned long long execs = 0, narrowed = 0, cert_execs = 0, cert_narrowed = 0;
   long long round = 0, nbar = 0;
+  // Certifying round: when a round changes nothing, one more round runs every
+  // unit once, whatever the frontier lists, stamps and chases recorded.  If
+  // it narrows nothing the store is a fixpoint of every propagator; if it
+  // narrows, it lists as any round does and the rounds go on.  full_round is
+  // the last round that ran every unit (round 0 is one).
+  long long full_round = 0;
   int state = EV_CONTINUE;
-  if (tid == 0) s_bits[0] = s_bits[1] = 0u;
+  if (tid == 0) {
+    s_bits[0] = s_bits[1] = 0u;
+    s_sq[0].n = s_sq[0].head = s_sq[1].n = s_sq[1].head = 0;
+  }
   __syncthreads();
   for (;;) {
-    const long long items = round == 0 ? a.n : (long long)ld_relaxed(a.cnt + (round % 3) * CNT_STRIDE);
-    const int p = (int)(nbar & 1);
-    if (round > 0 && items <= (long long)a.local_max) {
+    const bool full = round == full_round;
+    const long long items = full ? a.n : (long long)ld_relaxed(a.cnt + (round % 3) * CNT_STRIDE);
+    const int p = (int)(nbar & 1), rp = (int)(round & 1);
+    if (!full && items <= (long long)a.local_max) {
       // small frontier: CTA 0 runs the rounds, everyone meets at the next grid barrier
-      if (blockIdx.x == 0) run_local(a, round, s_stack + tid, s_defer + tid, execs, narrowed);
+      if (blockIdx.x == 0) run_local(a, round, s_stack + tid, s_defer + tid, s_sq, work, execs, narrowed);
       __syncthreads();
-      if (tid == 0) s_word[p] = grid_sync_rot(a.ctl, gridDim.x, nbar, 0, 0, a.timeout_ns, &a.ctl->hb);
+      if (tid == 0) {
+        // whatever round comes next starts with empty segment queues
+        s_sq[0].n = s_sq[0].head = s_sq[1].n = s_sq[1].head = 0;
+        s_word[p] = grid_sync_rot(a.ctl, gridDim.x, nbar, 0, 0, a.timeout_ns, &a.ctl->hb);
+      }
       __syncthreads();
       ++nbar;
       if (s_word[p] & BIT_ERROR) {
@@ -467,20 +756,45 @@ __global__ void __launch_bounds__(256, 2) k_fixpoint_events(EvFixArgs a) {
       }
       round = __ldcg(&a.ctl->ev_round);
       state = __ldcg(&a.ctl->ev_state);
+      if (state == EV_FIXPOINT && a.certify) {
+        if (a.max_rounds > 0 && round >= a.max_rounds) {
+          state = EV_CAP;  // no round left for the certifying one
+          break;
+        }
+        full_round = round;
+        state = EV_CONTINUE;
+        continue;
+      }
       if (state != EV_CONTINUE) break;
       continue;
     }
-    // the counter of round + 2 was last read in round - 1
+    // the counter of round + 2 was last read in round - 1; the other
+    // segment queue was last used in round - 1
     if (blockIdx.x == 0 && tid == 0) a.cnt[((round + 2) % 3) * CNT_STRIDE] = 0u;
+    if (tid == 0) s_sq[rp ^ 1].n = s_sq[rp ^ 1].head = 0;
     int failed = 0;
-    const int changed = run_frontier(a, round, items, gtid, gstride, s_stack + tid, s_defer + tid, execs, failed);
+    const unsigned long long execs0 = execs;
+    int changed =
+        run_frontier(a, round, full, items, gtid, gstride, s_stack + tid, s_defer + tid, s_sq[rp], execs, failed);
+    if (a.nseg) {
+      __syncthreads();
+      changed += run_segment_phase(a, ev_sched(a, round), full, gwarp, nwarps, s_sq[rp], work, execs, failed);
+    }
     narrowed += changed;
+    if (full && round > 0) {
+      cert_execs += execs - execs0;
+      cert_narrowed += changed;
+    }
     const unsigned bits = __reduce_or_sync(0xFFFFFFFFu, (changed ? 1u : 0u) | (failed ? 2u : 0u));
     if ((tid & 31) == 0 && bits) atomicOr(&s_bits[p], bits);
     __syncthreads();
     if (tid == 0) {
+      // read and clear: the next grid round with this parity may come after
+      // a local phase, which advances nbar without a grid round of the other
+      // parity (a stale changed bit would then report a change that did not
+      // happen, and certifying rounds would follow one another for ever)
       const unsigned b = s_bits[p];
-      s_bits[p ^ 1] = 0u;
+      s_bits[p] = 0u;
       s_word[p] = grid_sync_rot(a.ctl, gridDim.x, nbar, b & 1u, b & 2u, a.timeout_ns);
     }
     __syncthreads();
@@ -495,20 +809,28 @@ __global__ void __launch_bounds__(256, 2) k_fixpoint_events(EvFixArgs a) {
       state = EV_FAILED;
       break;
     }
-    if (!(w & BIT_CHANGED)) {
-      state = EV_FIXPOINT;
+    if (a.max_rounds > 0 && round >= a.max_rounds && (w & BIT_CHANGED || (a.certify && !full))) {
+      state = EV_CAP;  // still changing, or no round left for the certifying one
       break;
     }
-    if (a.max_rounds > 0 && round >= a.max_rounds) {
-      state = EV_CAP;
+    if (!(w & BIT_CHANGED)) {
+      if (a.certify && !full) {
+        full_round = round;
+        continue;
+      }
+      state = EV_FIXPOINT;
       break;
     }
   }
   execs = warp_sum64(execs);
   narrowed = warp_sum64(narrowed);
+  cert_execs = warp_sum64(cert_execs);
+  cert_narrowed = warp_sum64(cert_narrowed);
   if ((tid & 31) == 0) {
     if (execs) atomicAdd(&a.ctl->executions, execs);
     if (narrowed) atomicAdd(&a.ctl->narrowed, narrowed);
+    if (cert_execs) atomicAdd(&a.ctl->cert_execs, cert_execs);
+    if (cert_narrowed) atomicAdd(&a.ctl->cert_narrowed, cert_narrowed);
   }
   if (blockIdx.x == 0 && tid == 0) {
     a.ctl->rounds = round;
@@ -524,24 +846,26 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   pir_stats st;
   std::memset(&st, 0, sizeof(st));
-  const int4 *bc = nullptr;
-  const int *adj_ptr = nullptr, *adj = nullptr;
+  EventsGraph g;
   int r;
-  if ((r = events_graph(ctx, &bc, &adj_ptr, &adj))) return r;
-  const size_t n = (size_t)ctx->n, nv = (size_t)ctx->nvars;
-  // scratch: pstamp | vstamp | counters (cleared each run) | list 0 | list 1
-  const size_t o_v = align256(n * 4), o_c = o_v + align256(nv * 4), o_l0 = o_c + 3 * CNT_STRIDE * 4,
-               o_l1 = o_l0 + align256(n * 4), bytes = o_l1 + align256(n * 4);
+  if ((r = events_graph(ctx, &g, opts.segments >= 0))) return r;
+  const size_t n = (size_t)ctx->n, nv = (size_t)ctx->nvars, ns = (size_t)g.nseg;
+  // scratch: pstamp | sstamp | busy | vstamp | counters (cleared each run) | list 0 | list 1
+  const size_t o_s = align256(n * 4), o_b = o_s + align256(ns * 4), o_v = o_b + align256(ns * 4),
+               o_c = o_v + align256(nv * 4), o_l0 = o_c + 3 * CNT_STRIDE * 4, o_l1 = o_l0 + align256(n * 4),
+               bytes = o_l1 + align256(n * 4);
   if ((r = ensure(ctx, &ctx->d_scratch, &ctx->cap_scratch, bytes))) return r;
   char *base = (char *)ctx->d_scratch;
   PIR_CK(cudaMemsetAsync(base, 0, o_l0, ctx->stream));
   if ((r = reset_control(ctx))) return r;
   EvFixArgs a;
-  a.bc = bc;
-  a.adj_ptr = adj_ptr;
-  a.adj = adj;
+  a.bc = g.bc;
+  a.adj_ptr = g.uptr;
+  a.adj = g.uadj;
   a.store = ctx->d_store;
   a.pstamp = (unsigned *)base;
+  a.sstamp = (unsigned *)(base + o_s);
+  a.seg_busy = (int *)(base + o_b);
   a.vstamp = (unsigned *)(base + o_v);
   a.cnt = (unsigned *)(base + o_c);
   a.list0 = (int *)(base + o_l0);
@@ -552,14 +876,26 @@ int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   a.timeout_ns = opts.barrier_timeout_ns > 0 ? opts.barrier_timeout_ns : 2000000000ll;
   a.local_max = opts.local_frontier > 0 ? (unsigned)opts.local_frontier : 256u;
   a.chase = opts.chase > 0 ? std::min(opts.chase, CHASE_MAX) : (opts.chase < 0 ? 0 : CHASE_DEFAULT);
+  a.certify = opts.certify >= 0;
+  a.nseg = g.nseg;
+  a.seg_pptr = g.seg_pptr;
+  a.seg_code = g.seg_code;
+  a.seg_vptr = g.seg_vptr;
+  a.seg_var = g.seg_var;
+  a.in_seg = g.in_seg;
+  a.seg_umask = g.seg_umask;
+  const size_t dyn = g.nseg ? (size_t)EV_WARPS * sizeof(SegWork) : 0;
+  if (dyn) PIR_CK(cudaFuncSetAttribute(k_fixpoint_events, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   int occ = 0;
-  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fixpoint_events, 256, 0));
+  PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fixpoint_events, EV_BLOCK, dyn));
   if (occ < 1) return set_err(ctx, PIR_ECUDA, "event kernel does not fit on an SM");
   const int per_sm = opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ;
-  const int grid = std::max(1, std::min(ctx->num_sms * per_sm, (int)std::min<size_t>((n + 255) / 256, 1 << 20)));
+  const int grid =
+      std::max(1, std::min(ctx->num_sms * per_sm, (int)std::min<size_t>((n + EV_BLOCK - 1) / EV_BLOCK, 1 << 20)));
   void *args[] = {&a};
   PIR_CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  PIR_CK(cudaLaunchCooperativeKernel((const void *)k_fixpoint_events, dim3(grid), dim3(256), args, 0, ctx->stream));
+  PIR_CK(cudaLaunchCooperativeKernel((const void *)k_fixpoint_events, dim3(grid), dim3(EV_BLOCK), args, dyn,
+                                     ctx->stream));
   PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   Control h;
   if ((r = read_control(ctx, &h))) return r;
@@ -567,6 +903,8 @@ int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   st.rounds = h.rounds;
   st.executions = (int64_t)h.executions;
   st.narrowed = (int64_t)h.narrowed;
+  st.certify_executions = (int64_t)h.cert_execs;
+  st.certify_narrowed = (int64_t)h.cert_narrowed;
   int status;
   if (h.status) status = h.status;
   else if (h.failed) status = PIR_FAILED;

@@ -29,7 +29,9 @@ struct Control {
   long long ev_round;
   int ev_state;
   int pad_i;
-  unsigned long long pad[7];
+  // certifying sweeps: their executions and the bounds they narrowed
+  unsigned long long cert_execs, cert_narrowed;
+  unsigned long long pad[5];
 };
 
 constexpr unsigned BIT_CHANGED = 1u << 29;

@@ -1198,8 +1198,9 @@ int pc_build_csr(pirgpu_ctx *ctx, PcState *s) {
   const int nv = ctx->nvars, np = (int)s->roots.size();
   // on the host's threads; the same arrays as a sequential walk
   std::vector<int> deg((size_t)nv + 1, 0), adj;
-  build_formula_adjacency(np, s->roots.data(), reinterpret_cast<const int32_t *>(s->tape.data()), nv, deg.data(), adj,
-                          adjacency_threads((long long)s->tape.size(), 0, nv));
+  if (!build_formula_adjacency(np, s->roots.data(), reinterpret_cast<const int32_t *>(s->tape.data()), nv, deg.data(),
+                               adj, adjacency_threads((long long)s->tape.size(), 0, nv)))
+    return set_err(ctx, PIR_EINVAL, "PC event schedule: more than 2^31 - 1 adjacency entries");
   int r;
   if ((r = ensure(ctx, (void **)&s->d_adj_ptr, &s->cap_adj_ptr, deg.size() * sizeof(int)))) return r;
   if ((r = ensure(ctx, (void **)&s->d_adj, &s->cap_adj, std::max<size_t>(adj.size(), 1) * sizeof(int)))) return r;

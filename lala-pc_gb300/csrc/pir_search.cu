@@ -25,7 +25,7 @@ int fixpoint_nodes_events(pirgpu_ctx *ctx, BatchState *b, int32_t nnodes, const 
 // launch per batch, outputs read from pinned memory.
 int nodes_stage(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch, int32_t **in);
 int nodes_run_staged(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch, const pir_opts &opts,
-                     int32_t *out_status, const int2 **wout, pir_stats *stats);
+                     int32_t *out_status, int32_t *out_rounds, const int2 **wout, pir_stats *stats);
 }  // namespace pirgpu
 
 using namespace pirgpu;
@@ -85,6 +85,56 @@ extern "C" int pir_fixpoint_nodes_watch(pirgpu_ctx *ctx, int32_t nnodes, const i
   PIR_CK(cudaSetDevice(ctx->device));
   return fixpoint_nodes_events(ctx, batch(ctx), nnodes, off, var, lb, ub, opts, nullptr, nullptr, out_status,
                                out_rounds, stats, nwatch, watch, out_wlb, out_wub);
+}
+
+extern "C" int pir_nodes_stage(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch, int32_t **in) {
+  if (!ctx || !in) return PIR_EINVAL;
+  *in = nullptr;
+  if (nnodes < 0 || ntight < 0 || nwatch < 0) return set_err(ctx, PIR_EINVAL, "negative batch size");
+  PIR_CK(cudaSetDevice(ctx->device));
+  return nodes_stage(ctx, nnodes, ntight, nwatch, in);
+}
+
+extern "C" int pir_fixpoint_nodes_staged(pirgpu_ctx *ctx, int32_t nnodes, int32_t ntight, int32_t nwatch,
+                                         const pir_opts *opts_in, int32_t *out_status, int32_t *out_rounds,
+                                         int32_t *out_wlb, int32_t *out_wub, pir_stats *stats) {
+  if (!ctx) return PIR_EINVAL;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (nnodes < 0 || ntight < 0 || nwatch < 0) return set_err(ctx, PIR_EINVAL, "negative batch size");
+  if (nnodes == 0) return PIR_OK;
+  if (!out_status || (nwatch > 0 && (!out_wlb || !out_wub))) return set_err(ctx, PIR_EINVAL, "null output");
+  int32_t *in = nullptr;
+  int r;
+  // the staging the caller wrote (pir_nodes_stage with these sizes returns the same buffer)
+  if ((r = pir_nodes_stage(ctx, nnodes, ntight, nwatch, &in))) return r;
+  const int32_t *watch = in, *off = in + nwatch, *var = off + nnodes + 1, *lb = var + ntight, *ub = lb + ntight;
+  if (off[0] != 0 || off[nnodes] != ntight) return set_err(ctx, PIR_EINVAL, "offsets must run from 0 to ntight");
+  for (int j = 0; j < nnodes; ++j)
+    if (off[j + 1] < off[j]) return set_err(ctx, PIR_EINVAL, "node %d: offsets decrease", j);
+  for (int k = 0; k < ntight; ++k)
+    if (var[k] < 0 || var[k] >= ctx->nvars) return set_err(ctx, PIR_EINVAL, "tightening %d: var out of range", k);
+  for (int k = 0; k < nwatch; ++k)
+    if (watch[k] < 0 || watch[k] >= ctx->nvars) return set_err(ctx, PIR_EINVAL, "watch %d: var out of range", k);
+  pir_opts opts;
+  std::memset(&opts, 0, sizeof(opts));
+  if (opts_in) opts = *opts_in;
+  opts.sched = PIR_SCHED_EVENTS;
+  if (!ctx->failed && ctx->n > 0 && !ctx->at_fixpoint) {
+    pir_opts fo;
+    std::memset(&fo, 0, sizeof(fo));
+    r = pir_fixpoint(ctx, &fo, nullptr);
+    if (r != PIR_OK && r != PIR_FAILED) return r;
+  }
+  if (ctx->failed || ctx->n == 0)  // nothing to propagate: the plain path
+    return pir_fixpoint_nodes_watch(ctx, nnodes, off, var, lb, ub, &opts, nwatch, watch, out_wlb, out_wub,
+                                    out_status, out_rounds, stats);
+  const int2 *wout = nullptr;
+  if ((r = nodes_run_staged(ctx, nnodes, ntight, nwatch, opts, out_status, out_rounds, &wout, stats))) return r;
+  for (size_t k = 0; k < (size_t)nnodes * (size_t)nwatch; ++k) {
+    out_wlb[k] = wout[k].x;
+    out_wub[k] = wout[k].y;
+  }
+  return PIR_OK;
 }
 
 namespace {
@@ -165,7 +215,7 @@ extern "C" int pir_search(pirgpu_ctx *ctx, int32_t ndec, const int32_t *dec, con
         }
         o[i + 1] = (int32_t)t;
       }
-      rc = nodes_run_staged(ctx, (int32_t)take, (int32_t)ntight, ndec, eo, status.data(), &wout, &ns);
+      rc = nodes_run_staged(ctx, (int32_t)take, (int32_t)ntight, ndec, eo, status.data(), nullptr, &wout, &ns);
     } else {
       off.assign(1, 0);
       tv.clear();
@@ -191,7 +241,7 @@ extern "C" int pir_search(pirgpu_ctx *ctx, int32_t ndec, const int32_t *dec, con
       int64_t ntight = 0;
       for (int id : ids) ntight += pool[(size_t)id].depth;
       st.h2d_bytes += 4 * ((int64_t)ndec + take + 1 + 3 * ntight);
-      st.d2h_bytes += 32 + 8 * take + 8 * take * (int64_t)ndec;
+      st.d2h_bytes += 64 + 8 * take + 8 * take * (int64_t)ndec;
     }
     // watched bounds of node i, decision k
     auto lo = [&](int64_t i, int k) -> int32_t {

@@ -11,12 +11,16 @@
 // g_static_scratch below, which every GPU that loads the library holds until
 // the process exits.  The array's device address is looked up once per device
 // with cudaGetSymbolAddress on the first call made on that device, so that
-// first call should come before any stream capture.  All calls share the
-// array: it is cleared at the start of each call, and calls that overlap on the
-// GPU (from different streams or threads) race on it and must not be issued.
+// first call should come before any stream capture; after cudaDeviceReset the
+// address is stale and the process must not call this entry point again on that
+// device.  All calls share the array: it is cleared at the start of each call,
+// and calls that overlap on the GPU (from different streams or threads) race on
+// it and must not be issued.  Every call waits for its stream to finish (it
+// reads the outcome back) before it returns.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 
@@ -46,20 +50,24 @@ static __device__ __align__(256) unsigned char g_static_scratch[sizeof(pirgpu::S
 namespace pirgpu {
 namespace {
 
-// Device address of g_static_scratch, per device, filled on first use.
-StaticScratch *g_scratch_ptr[kStaticMaxDevices] = {nullptr};
+// Device address of g_static_scratch, per device, filled on first use (with
+// that device current).  Host threads making their first calls on one device
+// at once may both look it up; they store the same address.
+std::atomic<StaticScratch *> g_scratch_ptr[kStaticMaxDevices];
 
 int scratch_for_device(int dev, StaticScratch **out) {
   if (dev < 0 || dev >= kStaticMaxDevices) return PIR_EINVAL;
-  if (!g_scratch_ptr[dev]) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p) {
+  StaticScratch *p = g_scratch_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    void *q = nullptr;
+    if (cudaGetSymbolAddress(&q, g_static_scratch) != cudaSuccess || !q) {
       cudaGetLastError();
       return PIR_ECUDA;
     }
-    g_scratch_ptr[dev] = static_cast<StaticScratch *>(p);
+    p = static_cast<StaticScratch *>(q);
+    g_scratch_ptr[dev].store(p, std::memory_order_release);
   }
-  *out = g_scratch_ptr[dev];
+  *out = p;
   return PIR_OK;
 }
 

@@ -20,7 +20,7 @@ STATUS = ["OK", "FAILED", "TIMEOUT", "BARRIER_TIMEOUT", "EINVAL", "ECUDA", "ENOM
 MODE_AUTO, MODE_PERSISTENT, MODE_HOSTLOOP, MODE_SMEM = range(4)
 SCHED_AC1, SCHED_LEARNED, SCHED_EVENTS = range(3)
 PERSISTENT_VARIANTS = 10  # PIR_PERSISTENT_VARIANTS
-NODE_VARIANTS = 7  # PIR_NODE_VARIANTS
+NODE_VARIANTS = 10  # PIR_NODE_VARIANTS
 INF = 2**31 - 1
 MINF = -2**31
 
@@ -37,7 +37,7 @@ class Opts(ctypes.Structure):
                 ("ctas_per_sm", ctypes.c_int32), ("sched", ctypes.c_int32),
                 ("wake_fraction", ctypes.c_float), ("variant", ctypes.c_int32),
                 ("local_frontier", ctypes.c_int32), ("chase", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 4)]
+                ("certify", ctypes.c_int32), ("segments", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
 class SearchOpts(ctypes.Structure):
@@ -60,11 +60,13 @@ ORDER_INPUT, ORDER_MIN_DOMAIN = range(2)
 class Stats(ctypes.Structure):
     _fields_ = [("rounds", ctypes.c_int64), ("executions", ctypes.c_int64),
                 ("narrowed", ctypes.c_int64), ("device_ms", ctypes.c_float),
-                ("status", ctypes.c_int32)]
+                ("status", ctypes.c_int32), ("certify_executions", ctypes.c_int64),
+                ("certify_narrowed", ctypes.c_int64)]
 
     def asdict(self):
         return dict(rounds=self.rounds, executions=self.executions, narrowed=self.narrowed,
-                    device_ms=self.device_ms, status=self.status)
+                    device_ms=self.device_ms, status=self.status,
+                    certify_executions=self.certify_executions, certify_narrowed=self.certify_narrowed)
 
 
 _lib = None
@@ -115,6 +117,11 @@ SIGNATURES = [
                                                 _I32P, _I32P, ctypes.POINTER(Stats)]),
     ("pir_search", ctypes.c_int, [_P, ctypes.c_int32, _I32P, ctypes.POINTER(SearchOpts), _I32P,
                                   ctypes.POINTER(SearchStats)]),
+    ("pir_nodes_stage", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.POINTER(_I32P)]),
+    ("pir_fixpoint_nodes_staged", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                 ctypes.POINTER(Opts), _I32P, _I32P, _I32P, _I32P,
+                                                 ctypes.POINTER(Stats)]),
     ("pir_fixpoint_instances", ctypes.c_int, [_P, ctypes.c_int32, _I64P, _I64P, _I32P, _I32P,
                                               _I32P, _I32P, _I32P, _I32P, ctypes.POINTER(Opts),
                                               _I32P, _I32P, _F32P, ctypes.POINTER(Stats)]),
@@ -165,11 +172,11 @@ def _c32(a):
 
 
 def make_opts(mode=MODE_AUTO, max_rounds=0, barrier_timeout_ns=0, block=0, ctas_per_sm=0,
-              sched=SCHED_AC1, wake_fraction=0.0, variant=0, local_frontier=0, chase=0):
+              sched=SCHED_AC1, wake_fraction=0.0, variant=0, local_frontier=0, chase=0, certify=0, segments=0):
     o = Opts()
     o.max_rounds, o.barrier_timeout_ns, o.mode, o.block = max_rounds, barrier_timeout_ns, mode, block
     o.ctas_per_sm, o.sched, o.wake_fraction, o.variant = ctas_per_sm, sched, wake_fraction, variant
-    o.local_frontier, o.chase = local_frontier, chase
+    o.local_frontier, o.chase, o.certify, o.segments = local_frontier, chase, certify, segments
     return o
 
 
@@ -428,6 +435,28 @@ class Context:
         self._check(self._L.pir_fixpoint_nodes_watch(self.h, nn, _p32(off), _p32(var), _p32(lb), _p32(ub),
                                                      ctypes.byref(o), nw, _p32(watch), _p32(wl), _p32(wu),
                                                      _p32(status), _p32(rounds), ctypes.byref(s)))
+        return status, wl, wu, rounds, s.asdict()
+
+    def nodes_stage(self, nnodes, ntight, nwatch):
+        """The context's pinned staging of a node batch, as an int32 array:
+        watch[nwatch] | off[nnodes + 1] | var | lb | ub (ntight each).  Valid
+        until the next nodes_stage call."""
+        p = _I32P()
+        self._check(self._L.pir_nodes_stage(self.h, nnodes, ntight, nwatch, ctypes.byref(p)))
+        return np.ctypeslib.as_array(p, shape=(nwatch + nnodes + 1 + 3 * ntight,))
+
+    def fixpoint_nodes_staged(self, nnodes, ntight, nwatch, **kw):
+        """Runs the staged batch as one CUDA graph: (status, watched lb, watched
+        ub (nnodes x nwatch), rounds, stats)."""
+        status = np.empty(nnodes, np.int32)
+        rounds = np.empty(nnodes, np.int32)
+        wl = np.empty((nnodes, nwatch), np.int32)
+        wu = np.empty((nnodes, nwatch), np.int32)
+        o = make_opts(**kw)
+        s = Stats()
+        self._check(self._L.pir_fixpoint_nodes_staged(self.h, nnodes, ntight, nwatch, ctypes.byref(o),
+                                                      _p32(status), _p32(rounds), _p32(wl), _p32(wu),
+                                                      ctypes.byref(s)))
         return status, wl, wu, rounds, s.asdict()
 
     def search(self, dec, max_solutions=0, max_nodes=0, batch=0, order=ORDER_INPUT):

@@ -23,6 +23,7 @@ def csr(tmp_path_factory):
     lib = ctypes.CDLL(str(out))
     P = ctypes.POINTER(ctypes.c_int)
     lib.csr_build.argtypes = [ctypes.c_longlong, ctypes.c_int, P, P, P, P, P, ctypes.c_int]
+    lib.csr_build.restype = ctypes.c_int
     lib.csr_threads.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_longlong]
     lib.csr_threads.restype = ctypes.c_int
 
@@ -32,9 +33,10 @@ def csr(tmp_path_factory):
         ptr = np.full(nv + 1, -7, np.int32)
         adj = np.full(3 * n, -7, np.int32)
         p = lambda a: a.ctypes.data_as(P)
-        lib.csr_build(n, nv, p(x), p(y), p(z), p(ptr), p(adj), threads)
+        assert lib.csr_build(n, nv, p(x), p(y), p(z), p(ptr), p(adj), threads) == 1
         return ptr, adj
     build.threads = lib.csr_threads
+    build.lib = lib
     build.lib_path = out
     return build
 
@@ -58,6 +60,21 @@ def test_adjacency_matches_counting_sort(csr, shape, threads):
     rptr, radj = _reference(nv, x, y, z)
     np.testing.assert_array_equal(ptr, rptr)
     np.testing.assert_array_equal(adj, radj)
+
+
+def test_adjacency_rejects_int32_overflow(csr):
+    """3 n adjacency entries beyond INT32_MAX (n > 715,827,882 propagators,
+    which fit a GB300's memory) would wrap the int32 offsets: the builder
+    refuses before touching anything (the bytecode arrays are never read,
+    so a fake n with one-element arrays is safe)."""
+    P = ctypes.POINTER(ctypes.c_int)
+    one = np.zeros(1, np.int32)
+    ptr = np.full(2, -7, np.int32)
+    adj = np.full(1, -7, np.int32)
+    p = lambda a: a.ctypes.data_as(P)
+    for n in ((2**31 - 1) // 3 + 1, 2**31, 2**40):
+        assert csr.lib.csr_build(n, 1, p(one), p(one), p(one), p(ptr), p(adj), 4) == 0
+    assert np.all(ptr == -7) and np.all(adj == -7)
 
 
 def test_thread_choice(csr):

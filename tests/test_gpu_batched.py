@@ -141,12 +141,19 @@ def test_nodes_events_parity(seed, P, oracle):
     np.testing.assert_array_equal(l2[ok], olb[ok])
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("variant", list(range(1, 11)))
 def test_nodes_events_variants(variant, P, oracle):
-    """The event node kernel: 256 threads sized for 2, 3, 4, 6 and 8 resident
-    CTAs per SM, 128 threads for 8 and 10."""
+    """The event node kernel: one node per CTA with 256 threads sized for 2,
+    3, 4, 6 and 8 resident CTAs per SM, 128 threads for 8 and 10; one node per
+    warp with 8 warps per CTA sized for 2 and 3 CTAs per SM, 4 warps for 6.
+    Twice in a row: the second launch finds the scratch as the first left it."""
     ctx, (blb, bub), off, var, lb, ub = _nodes_setup(P, seed=4, nnodes=300)
-    status, olb, oub, _, _ = ctx.fixpoint_nodes(off, var, lb, ub, sched=P.SCHED_EVENTS, variant=variant)
+    status, olb, oub, _, st = ctx.fixpoint_nodes(off, var, lb, ub, sched=P.SCHED_EVENTS, variant=variant)
+    assert st["certify_narrowed"] == 0
+    s2, l2, u2, _, _ = ctx.fixpoint_nodes(off, var, lb, ub, sched=P.SCHED_EVENTS, variant=variant)
+    np.testing.assert_array_equal(s2, status)
+    np.testing.assert_array_equal(l2, olb)
+    np.testing.assert_array_equal(u2, oub)
     op, x, y, z = ctx.bytecode()
     base = np.ascontiguousarray(np.stack([blb, bub], 1))
     ostatus, ostore, _ = oracle.fixpoint_nodes(op, x, y, z, base, off, var, lb, ub)
@@ -263,3 +270,33 @@ def test_instances_reject_bad_bytecode(P):
         with pytest.raises(P.PirError, match=msg):
             ctx.fixpoint_instances(prop_off, var_off, arrs["op"], arrs["x"], arrs["y"], arrs["z"], lb, ub)
         np.testing.assert_array_equal(lb, lb0)
+
+
+def test_nodes_staged_graph_matches_watch(P):
+    """pir_nodes_stage + pir_fixpoint_nodes_staged (each batch one CUDA graph,
+    updated in place, rebuilt when the staging grows) give what
+    pir_fixpoint_nodes_watch gives, batch after batch; a bad variable in the
+    staging is rejected before anything runs."""
+    ctx, (blb, bub), off, var, lb, ub = _nodes_setup(P, nnodes=200, seed=7)
+    watch = np.arange(0, 5000, 7, dtype=np.int32)
+    for j0, j1 in ((0, 60), (60, 120), (120, 200), (0, 30)):
+        o = (off[j0:j1 + 1] - off[j0]).astype(np.int32)
+        sl = slice(off[j0], off[j1])
+        ws, wl, wu, wr, _ = ctx.fixpoint_nodes_watch(o, var[sl], lb[sl], ub[sl], watch)
+        nn, nt, nw = j1 - j0, int(o[-1]), len(watch)
+        buf = ctx.nodes_stage(nn, nt, nw)
+        buf[:nw] = watch
+        buf[nw:nw + nn + 1] = o
+        buf[nw + nn + 1:nw + nn + 1 + nt] = var[sl]
+        buf[nw + nn + 1 + nt:nw + nn + 1 + 2 * nt] = lb[sl]
+        buf[nw + nn + 1 + 2 * nt:] = ub[sl]
+        ss, sl_, su, sr, st = ctx.fixpoint_nodes_staged(nn, nt, nw)
+        np.testing.assert_array_equal(ss, ws)
+        np.testing.assert_array_equal(sr, wr)
+        np.testing.assert_array_equal(sl_, wl)
+        np.testing.assert_array_equal(su, wu)
+        assert st["certify_narrowed"] == 0
+    buf = ctx.nodes_stage(2, 1, 0)
+    buf[:] = [0, 1, 1, 5000, 0, 0]  # off 0, 1, 1; var 5000 is out of range
+    with pytest.raises(P.PirError):
+        ctx.fixpoint_nodes_staged(2, 1, 0)

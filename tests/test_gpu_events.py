@@ -50,12 +50,12 @@ def test_events_spec_fails(seed, P, oracle):
 @pytest.mark.parametrize("chase", [-1, 0])
 @pytest.mark.parametrize("local", [0, 1])
 def test_events_chain_and_random(local, chase, P, oracle):
-    """100k vars / 400k propagators plus a 3,000-link chain: without chasing
-    the deep part takes a round per link, mostly small-frontier rounds; with
-    it, a few dozen rounds."""
+    """100k vars / 400k propagators plus a 3,000-link chain, every propagator
+    on its own (no segments): without chasing the deep part takes a round per
+    link, mostly small-frontier rounds; with it, a few dozen rounds."""
     import workloads as W
     inst = W.add_chain(W.plain(100_000, 400_000, 10**6, 7), 3000, 10**6, 7)
-    rc, g, st, orc, o, info = _both(P, oracle, inst, local_frontier=local, chase=chase)
+    rc, g, st, orc, o, info = _both(P, oracle, inst, local_frontier=local, chase=chase, segments=-1)
     assert rc == orc == oracle.OK
     np.testing.assert_array_equal(g, o)
     if chase < 0:
@@ -67,9 +67,10 @@ def test_events_chain_and_random(local, chase, P, oracle):
         assert st["executions"] < 20 * inst.nprops
 
 
+@pytest.mark.parametrize("segments", [0, -1])
 @pytest.mark.parametrize("chase", [-1, 0])
 @pytest.mark.parametrize("local", [0, 300, 1 << 30])
-def test_events_hub_overflow(local, chase, P, oracle):
+def test_events_hub_overflow(local, chase, segments, P, oracle):
     """A 300-link chain whose middle variable feeds 3,000 more propagators
     y_j = x_150 + c_j: the round that narrows x_150 lists more propagators
     than a round on one CTA keeps in shared memory (256) and than its dedupe
@@ -84,12 +85,14 @@ def test_events_hub_overflow(local, chase, P, oracle):
                       np.concatenate([chain.ub, np.full(k, 10**6), c]),
                       np.concatenate([chain.op, np.full(k, W.ADD)]), np.concatenate([chain.x, ys]),
                       np.concatenate([chain.y, np.full(k, hub)]), np.concatenate([chain.z, cs]))
-    rc, g, st, orc, o, info = _both(P, oracle, inst, local_frontier=local, chase=chase)
+    rc, g, st, orc, o, info = _both(P, oracle, inst, local_frontier=local, chase=chase, segments=segments)
     assert rc == orc == oracle.OK
     np.testing.assert_array_equal(g, o)
+    assert st["certify_narrowed"] == 0
     # (a round may read bounds joined earlier in the same round, so the waves
-    # can move faster than one link per round)
-    assert st["rounds"] >= (100 if chase < 0 else 2)
+    # can move faster than one link per round; segments move 64 links a round)
+    if segments < 0:
+        assert st["rounds"] >= (100 if chase < 0 else 2)
     # x_150 narrows in about 150 rounds, each listing its 3,002 propagators
     # (once each): fewer executions than the oracle's 301 sweeps
     assert st["executions"] < info["execs"]
@@ -99,10 +102,11 @@ def test_events_hub_overflow(local, chase, P, oracle):
 @pytest.mark.parametrize("local", [1, 256, 1 << 30])
 def test_events_chase(chase, local, P, oracle):
     """The chase budget (runs of small variables' propagators done at once by
-    the narrowing thread; -1: none) changes the rounds, never the fixpoint."""
+    the narrowing thread; -1: none) changes the rounds, never the fixpoint
+    (every propagator on its own, no segments)."""
     import workloads as W
     inst = W.add_chain(W.plain(30_000, 120_000, 10**6, 11), 2000, 10**6, 11)
-    rc, g, st, orc, o, _ = _both(P, oracle, inst, local_frontier=local, chase=chase)
+    rc, g, st, orc, o, _ = _both(P, oracle, inst, local_frontier=local, chase=chase, segments=-1)
     assert rc == orc == oracle.OK
     np.testing.assert_array_equal(g, o)
     if chase < 0:
@@ -142,15 +146,17 @@ def _mixed_chain(L, seed):
     return W.Instance(lb, ub, op, X, Y, Z)
 
 
+@pytest.mark.parametrize("segments", [0, -1])
 @pytest.mark.parametrize("chase", [-1, 0, 1, 256])
 @pytest.mark.parametrize("seed", range(6))
-def test_events_chase_mixed_chains(seed, chase, P, oracle):
+def test_events_chase_mixed_chains(seed, chase, segments, P, oracle):
     inst = _mixed_chain(1500, seed)
     for local in (0, 1 << 30):
-        rc, g, _, orc, o, _ = _both(P, oracle, inst, local_frontier=local, chase=chase)
+        rc, g, st, orc, o, _ = _both(P, oracle, inst, local_frontier=local, chase=chase, segments=segments)
         assert rc == orc
         if orc == oracle.OK:
             np.testing.assert_array_equal(g, o)
+            assert st["certify_narrowed"] == 0
 
 
 def test_events_long_chain_capped_chase(P):
@@ -168,7 +174,7 @@ def test_events_long_chain_capped_chase(P):
     ctx = P.Context(0)
     ctx.load_store(inst.lb, inst.ub)
     ctx.tell(inst.op, inst.x, inst.y, inst.z)
-    rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS, chase=1 << 30)
+    rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS, chase=1 << 30, segments=-1)
     assert rc == P.OK
     lb, ub = ctx.read_store()
     np.testing.assert_array_equal(lb[:L + 1], want_lb)
@@ -177,6 +183,15 @@ def test_events_long_chain_capped_chase(P):
     # that starts late inside what the front already updated can carry it
     # past 256 links in a round, so not L / 256 exactly)
     assert st["rounds"] >= L // 1024
+    # as segments of at most 64 links, a warp chasing at most 32 of them per
+    # entry: the same store
+    ctx.load_store(inst.lb, inst.ub)
+    rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS)
+    assert rc == P.OK and st["certify_narrowed"] == 0
+    lb, ub = ctx.read_store()
+    np.testing.assert_array_equal(lb[:L + 1], want_lb)
+    np.testing.assert_array_equal(ub[:L + 1], want_ub)
+    assert st["rounds"] < L // 64 + 100
 
 
 @pytest.mark.parametrize("chase", [-1, 0, 2])
@@ -215,11 +230,13 @@ def test_events_round_cap(P, oracle):
     import workloads as W
     empty = W.Instance(np.zeros(0, np.int32), np.zeros(0, np.int32), *(np.zeros(0, np.int32),) * 4)
     inst = W.add_chain(empty, 2000, 10**6, 1)
-    for local, chase, cap in ((0, -1, 100), (1, -1, 100), (0, 0, 2), (1, 0, 2)):
+    for local, chase, cap, segs in ((0, -1, 100, -1), (1, -1, 100, -1), (0, 0, 2, -1), (1, 0, 2, -1),
+                                    (0, -1, 10, 0), (1, -1, 10, 0)):
         ctx = P.Context(0)
         ctx.load_store(inst.lb, inst.ub)
         ctx.tell(inst.op, inst.x, inst.y, inst.z)
-        rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS, max_rounds=cap, local_frontier=local, chase=chase)
+        rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS, max_rounds=cap, local_frontier=local, chase=chase,
+                              segments=segs)
         assert rc == P.TIMEOUT and st["rounds"] == cap
         rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS)
         assert rc == P.OK
@@ -227,6 +244,77 @@ def test_events_round_cap(P, oracle):
         s = inst.store()
         orc, _ = oracle.install_and_fixpoint(inst.op, inst.x, inst.y, inst.z, s)
         np.testing.assert_array_equal(np.stack([lb, ub], 1), s)
+
+
+@pytest.mark.parametrize("local", [0, 1, 1 << 30])
+def test_events_segments_chain_and_random(local, P, oracle):
+    """100k vars / 400k propagators plus a 3,000-link chain, the chain run as
+    47 segments of at most 64 links: the oracle's fixpoint in far fewer
+    rounds than one link per round, and a certifying sweep that finds
+    nothing."""
+    import workloads as W
+    inst = W.add_chain(W.plain(100_000, 400_000, 10**6, 7), 3000, 10**6, 7)
+    o = inst.store()
+    orc, _ = oracle.install_and_fixpoint(inst.op, inst.x, inst.y, inst.z, o)
+    assert orc == oracle.OK
+    for chase in (0, -1):  # without chasing: segment by segment
+        ctx = P.Context(0)
+        ctx.load_store(inst.lb, inst.ub)
+        ctx.tell(inst.op, inst.x, inst.y, inst.z)
+        rc, st = ctx.fixpoint(sched=P.SCHED_EVENTS, local_frontier=local, chase=chase)
+        assert rc == P.OK
+        np.testing.assert_array_equal(np.stack(ctx.read_store(), 1), o)
+        assert st["certify_narrowed"] == 0 and st["certify_executions"] > 0
+        assert st["rounds"] < (300 if chase == 0 else 3000 // 20)
+
+
+def _rings(nring, length, seed):
+    """nring rings of `length` propagators, x_{i+1} = x_i + 0 or x_{i+1} =
+    max(x_i, c_i) (indices mod length; every x_i occurs twice, so each ring
+    is one cycle of link variables: all its variables equal, at least the
+    largest c_i), with a reified side check on every 7th variable (which
+    breaks the path there)."""
+    import workloads as W
+    rng = np.random.default_rng(seed)
+    lb, ub, op, X, Y, Z = [], [], [], [], [], []
+
+    def var(lo, hi):
+        lb.append(lo)
+        ub.append(hi)
+        return len(lb) - 1
+
+    for _ in range(nring):
+        xs = [var(-10**5, 10**5) for _ in range(length)]
+        lb[xs[0]], ub[xs[0]] = 0, 50
+        for i in range(length):
+            mx = rng.integers(0, 4) == 0
+            c = int(rng.integers(0, 41)) if mx else 0
+            op.append(W.MAX if mx else W.ADD)
+            X.append(xs[(i + 1) % length]), Y.append(xs[i]), Z.append(var(c, c))
+            if i % 7 == 3:
+                t = int(rng.integers(0, 80))
+                op.append(W.LEQ)
+                X.append(var(0, 1)), Y.append(xs[i]), Z.append(var(t, t))
+    return W.Instance(lb, ub, op, X, Y, Z)
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_events_segments_rings_and_failure(seed, P, oracle):
+    """Cycles of link variables (cut once each), and a chain whose last link
+    is cut below the sum of its increments, so a segment fails."""
+    import workloads as W
+    inst = _rings(40, 150, seed)
+    rc, g, st, orc, o, _ = _both(P, oracle, inst)
+    assert rc == orc
+    if orc == oracle.OK:
+        np.testing.assert_array_equal(g, o)
+        assert st["certify_narrowed"] == 0
+    empty = W.Instance(np.zeros(0, np.int32), np.zeros(0, np.int32), *(np.zeros(0, np.int32),) * 4)
+    chain = W.add_chain(empty, 500, 10**6, seed)
+    chain.lb[0], chain.ub[0] = 0, 0
+    chain.ub[500] = 400  # the increments are at least 1 each: x_500 >= 500
+    rc, _, _, orc, _, _ = _both(P, oracle, chain)
+    assert rc == orc == oracle.FAILED
 
 
 @pytest.mark.parametrize("case", K.CASES, ids=[c.name for c in K.CASES])
