@@ -8,7 +8,7 @@ x_{i+1} = x_i + c_i (c_i ~ U[1, 5]) that keeps changing one bound per round
 for ~20,000 rounds.  Metric: propagator executions per second.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload single_large|single_small|nodes|uneven|learned]
+                  [--workload single_large|single_small|out_of_l2|nodes|uneven|learned|search|pc]
 
 --impl reference times the reference algorithm's CPU path (the C++
 restatement of lala-pc's PIR::deduce driven by the Gauss-Seidel loop) on
@@ -196,6 +196,10 @@ def make_workload(name):
     elif name == "single_small":
         inst = W.single_small(0)
         desc = "1,000 vars / 3,000 propagators (planted solution, bounds scale 1e3)"
+    elif name == "out_of_l2":
+        inst = W.plain(4_000_000, 16_000_000, 10**6, 0)
+        desc = ("4,000,000 vars / 16,000,000 propagators (planted solution, bounds scale 1e6, base mix); "
+                "bytecode 256 MB + store 32 MB")
     else:
         raise ValueError(name)
     return inst, desc

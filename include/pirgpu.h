@@ -93,7 +93,13 @@ typedef struct pir_opts {
   int32_t segments;           /* pir_fixpoint's event schedule: 0 or > 0 run the propagators of paths joined by
                                  variables with two occurrences as segments (a warp sweeps up to 64 of them in
                                  shared memory); < 0: every propagator on its own */
-  int32_t reserved[2];
+  int32_t dense;              /* pir_fixpoint's event schedule: a dense round (every propagator once, AC-1
+                                 style, noting only which variables narrowed: one atomic per variable instead
+                                 of listing each narrowed variable's propagators) is followed by another while
+                                 the propagators of the variables it narrowed number at least 1/dense of all
+                                 (0: 1/32) and those variables keep getting fewer; < 0: dense only for the first
+                                 round and the certifying sweep */
+  int32_t reserved[1];
 } pir_opts;
 
 typedef struct pir_stats {

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpirgpu.so")
 SOURCES = ["pir_engine.cu", "pir_batch.cu", "pir_sched.cu", "pir_static.cu", "pir_events.cu", "pir_search.cu",
-           "pir_pc.cu"]
+           "pir_pc.cu", "pir_install.cu"]
 HEADERS = ["pir_device.cuh", "pir_kernels.cuh", "pir_engine.h", "pir_csr.h", "pir_sort.h", "pir_segments.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

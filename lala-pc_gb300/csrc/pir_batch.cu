@@ -68,6 +68,7 @@ struct BatchState {
   long long seg_version = -1;
   int seg_nvars = -1;
   int nseg = 0;
+  long long seg_nvar = 0;
   int *d_uptr = nullptr, *d_uadj = nullptr, *d_seg_pptr = nullptr, *d_seg_code = nullptr, *d_seg_vptr = nullptr;
   unsigned *d_seg_var = nullptr, *d_in_seg = nullptr;
   unsigned long long *d_seg_umask = nullptr;
@@ -1130,16 +1131,7 @@ int ensure_events_graph(pirgpu_ctx *ctx, BatchState *b) {
   const int nv = ctx->nvars;
   if (!adjacency_fits(3 * n))
     return set_err(ctx, PIR_EINVAL, "event schedule: %lld propagators need more than 2^31 - 1 adjacency entries", n);
-  std::vector<int4> bc4((size_t)n);
   std::vector<int> ptr((size_t)nv + 1, 0), adj((size_t)n * 3);
-  // on the host's threads (4M propagators: 0.38 s on one core)
-  const int T = adjacency_threads(n, 0, nv);
-  run_threads(T, [&](int t) {
-    for (long long p = n * t / T; p < n * (t + 1) / T; ++p)
-      bc4[(size_t)p] = make_int4(ctx->h_op[(size_t)p], ctx->h_x[(size_t)p], ctx->h_y[(size_t)p], ctx->h_z[(size_t)p]);
-  });
-  if (!build_adjacency(n, nv, ctx->h_x.data(), ctx->h_y.data(), ctx->h_z.data(), ptr.data(), adj.data(), T))
-    return set_err(ctx, PIR_EINVAL, "event schedule: adjacency does not fit int32 offsets");
   void *ptrs[] = {b->d_bc4, b->d_adj_ptr, b->d_adj};
   for (void *q : ptrs)
     if (q) cudaFree(q);
@@ -1151,10 +1143,29 @@ int ensure_events_graph(pirgpu_ctx *ctx, BatchState *b) {
     cudaGetLastError();
     return set_err(ctx, PIR_ENOMEM, "event graph");
   }
-  PIR_CK(cudaMemcpyAsync(b->d_bc4, bc4.data(), (size_t)n * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
-  PIR_CK(cudaMemcpyAsync(b->d_adj_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-  PIR_CK(cudaMemcpyAsync(b->d_adj, adj.data(), adj.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-  PIR_CK(cudaStreamSynchronize(ctx->stream));
+  if (n >= DEVICE_INSTALL_MIN) {
+    // on the device (pir_install.cu); the host copy of the adjacency for the segment builder
+    int r;
+    if ((r = device_events_graph(ctx, b->d_bc4, b->d_adj_ptr, b->d_adj))) return r;
+    PIR_CK(cudaMemcpyAsync(ptr.data(), b->d_adj_ptr, ptr.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PIR_CK(cudaMemcpyAsync(adj.data(), b->d_adj, adj.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PIR_CK(cudaStreamSynchronize(ctx->stream));
+  } else {
+    // on the host's threads
+    std::vector<int4> bc4((size_t)n);
+    const int T = adjacency_threads(n, 0, nv);
+    run_threads(T, [&](int t) {
+      for (long long p = n * t / T; p < n * (t + 1) / T; ++p)
+        bc4[(size_t)p] =
+            make_int4(ctx->h_op[(size_t)p], ctx->h_x[(size_t)p], ctx->h_y[(size_t)p], ctx->h_z[(size_t)p]);
+    });
+    if (!build_adjacency(n, nv, ctx->h_x.data(), ctx->h_y.data(), ctx->h_z.data(), ptr.data(), adj.data(), T))
+      return set_err(ctx, PIR_EINVAL, "event schedule: adjacency does not fit int32 offsets");
+    PIR_CK(cudaMemcpyAsync(b->d_bc4, bc4.data(), (size_t)n * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
+    PIR_CK(cudaMemcpyAsync(b->d_adj_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    PIR_CK(cudaMemcpyAsync(b->d_adj, adj.data(), adj.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    PIR_CK(cudaStreamSynchronize(ctx->stream));
+  }
   b->h_adj_ptr.swap(ptr);
   b->h_adj.swap(adj);
   b->ev_version = ctx->bytecode_version;
@@ -1203,6 +1214,7 @@ static int ensure_segments(pirgpu_ctx *ctx, BatchState *b) {
       return r;
     PIR_CK(cudaStreamSynchronize(ctx->stream));
     b->nseg = S.nseg;
+    b->seg_nvar = (long long)S.var.size();
   }
   b->seg_version = ctx->bytecode_version;
   b->seg_nvars = nv;
@@ -1221,6 +1233,7 @@ int events_graph(pirgpu_ctx *ctx, EventsGraph *g, bool segments) {
   g->uadj = b->d_adj;
   if (segments && b->nseg > 0) {
     g->nseg = b->nseg;
+    g->seg_nvar = b->seg_nvar;
     g->uptr = b->d_uptr;
     g->uadj = b->d_uadj;
     g->seg_pptr = b->d_seg_pptr;

@@ -378,7 +378,8 @@ void pir_ctx_destroy(pirgpu_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  void *ptrs[] = {ctx->d_store, ctx->d_op, ctx->d_x, ctx->d_y, ctx->d_z, ctx->d_ctl, ctx->d_scratch, ctx->d_io};
+  void *ptrs[] = {ctx->d_store, ctx->d_op, ctx->d_x, ctx->d_y, ctx->d_z, ctx->d_ctl, ctx->d_scratch, ctx->d_io,
+                  ctx->d_install};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   destroy_batch_state(ctx);
@@ -502,6 +503,16 @@ int pir_tell(pirgpu_ctx *ctx, int32_t n, const int32_t *op, const int32_t *x, co
   std::copy(x, x + n, x2.begin() + old);
   std::copy(y, y + n, y2.begin() + old);
   std::copy(z, z + n, z2.begin() + old);
+  if ((long long)tot >= DEVICE_INSTALL_MIN) {
+    // the stable (op, y, x, z) sort on the device (pir_install.cu)
+    if ((r = device_install(ctx, (long long)tot, o2.data(), x2.data(), y2.data(), z2.data()))) return r;
+    ctx->n = (long long)tot;
+    ctx->max_var_used = maxv;
+    ctx->bytecode_version++;
+    ctx->at_fixpoint = false;
+    if (changed) *changed = 1;
+    return PIR_OK;
+  }
   // on the host's threads, the permutation std::stable_sort gives (4M propagators: 0.91 s on one core)
   std::vector<int> perm(tot);
   std::iota(perm.begin(), perm.end(), 0);

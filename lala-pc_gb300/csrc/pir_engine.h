@@ -44,6 +44,8 @@ struct pirgpu_ctx {
   pirgpu::Control *d_ctl = nullptr;
   void *d_scratch = nullptr;
   size_t cap_scratch = 0;
+  void *d_install = nullptr;  // scratch of the device install (radix sorts)
+  size_t cap_install = 0;
   int last_grid = 0;
   int last_mode = 0;
   int last_variant = 0;
@@ -82,12 +84,23 @@ struct EventsGraph {
   const int4 *bc = nullptr;
   const int *adj_ptr = nullptr, *adj = nullptr;
   int nseg = 0;
+  long long seg_nvar = 0;  // local variable slots of all segments
   const int *uptr = nullptr, *uadj = nullptr;
   const int *seg_pptr = nullptr, *seg_code = nullptr, *seg_vptr = nullptr;
   const unsigned *seg_var = nullptr, *in_seg = nullptr;
   const unsigned long long *seg_umask = nullptr;
 };
 int events_graph(pirgpu_ctx *ctx, EventsGraph *g, bool segments);
+
+// Install on the device (pir_install.cu), for bytecodes of at least
+// DEVICE_INSTALL_MIN propagators: device_install sorts the n given
+// propagators (host arrays, any order) into the engine order (op, y, x, z),
+// stably, and writes the padded device SoA and the host copies h_op .. h_z;
+// device_events_graph builds the AoS bytecode and the variable -> propagator
+// adjacency of the context's bytecode into the given device arrays.
+constexpr long long DEVICE_INSTALL_MIN = 1 << 16;
+int device_install(pirgpu_ctx *ctx, long long n, const int *op, const int *x, const int *y, const int *z);
+int device_events_graph(pirgpu_ctx *ctx, int4 *bc, int *adj_ptr, int *adj);
 
 int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);
 int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);

@@ -10,8 +10,10 @@
 // whose intervals did not change since its last run (which changed nothing)
 // cannot change anything: the run ends at the same fixpoint, or the same
 // failure, as the sweeps, bit for bit (propagators are monotone, so the order
-// of the runs does not matter).  A final full round (the certifying sweep,
-// opts.certify) checks it.
+// of the runs does not matter).  While a round narrows many variables the
+// next one is dense (every unit, AC-1 style, noting only the narrowed
+// variables: "Dense rounds" below); a final dense round (the certifying
+// sweep, opts.certify) checks the fixpoint.
 //
 // Units.  A unit is a propagator, or a segment: up to SEG_MAX propagators of
 // a path joined by link variables (variables with exactly two occurrences,
@@ -61,13 +63,24 @@ struct EvFixArgs {
   long long max_rounds, timeout_ns;
   unsigned local_max;
   int chase;  // runs chased per frontier entry (0: none)
-  int certify;  // end with a full round (every unit once) that narrows nothing
+  int certify;  // end with a dense round (every unit once) that narrows nothing
   // path segments (nseg = 0: none; pir_segments.h)
   int nseg;
   const int *seg_pptr, *seg_code, *seg_vptr;
   const unsigned *seg_var, *in_seg;
   const unsigned long long *seg_umask;
-  int *seg_busy;  // per segment: 1 while a warp runs it
+  int *seg_busy;   // per segment: 1 while a warp runs it
+  int2 *seg_last;  // per local slot: its interval when the segment's last run ended at its own fixpoint
+  int *seg_valid;  // per segment: seg_last holds that run's intervals
+  // dense rounds (every unit once, AC-1 style): the variables they narrow
+  unsigned *cstamp;    // per variable: the last dense round (+ 1) that noted it
+  int *cvl0, *cvl1;    // the variables noted by dense round r: cvl0 for even r, cvl1 for odd r
+  unsigned *ccnt;      // their counts: round r in ccnt[(r % 3) * CNT_STRIDE]
+  unsigned *dsum;      // the sum of their unit degrees, likewise
+  unsigned *dflag;     // round r in dflag[(r % 3) * CNT_STRIDE]: a segment has sweeps left, dense again
+  int dense_div;       // a dense round whose noted variables have at least n / dense_div units may be followed
+                       // by another (0: never)
+  int nvars;
 };
 
 __device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
@@ -146,11 +159,13 @@ struct RunView {
 constexpr int EXPAND = 8;
 
 struct EvSched {
+  static constexpr bool kDense = false;
   const int *adj;
   unsigned *pstamp, *sstamp, *vstamp;
   int *next;
   unsigned *next_cnt;
   unsigned next_round;
+  __device__ __forceinline__ void note(int) const {}
   __device__ __forceinline__ bool claim(int u) const {
     return atomicMax(u >= 0 ? pstamp + u : sstamp + ~u, next_round) < next_round;
   }
@@ -320,8 +335,7 @@ struct SegQueue {
 
 // The sweeps' store: the segment's intervals in shared memory (one lane).  A
 // narrowing meets into the current interval and marks the propagators of
-// the segment that use the variable (the narrowing one too: a propagator
-// need not be idempotent) for another run.
+// the segment that use the variable for another run.
 struct SegStore {
   int2 *iv;
   const unsigned long long *umask;
@@ -343,18 +357,30 @@ struct SegStore {
   }
 };
 
+// One propagator of the segment.  ADD, MIN, MAX and the reified EQ / LEQ
+// are idempotent (a second run on what the first left narrows nothing;
+// checked exhaustively against the oracle), so such a propagator over three
+// distinct variables is not marked again by its own narrowings; MUL and the
+// divisions are.
 __device__ __forceinline__ void seg_run_one(const SegWork &w, SegStore &st, int k, int &failed) {
   const unsigned c = (unsigned)w.code[k];
-  st.dirty &= ~(1ull << k);
-  deduce((int)(c & 0xFFu), (int)((c >> 8) & 0xFFu), (int)((c >> 16) & 0xFFu), (int)(c >> 24), st, failed);
+  const int op = (int)(c & 0xFFu), sx = (int)((c >> 8) & 0xFFu), sy = (int)((c >> 16) & 0xFFu), sz = (int)(c >> 24);
+  const unsigned long long bit = 1ull << k;
+  st.dirty &= ~bit;
+  deduce(op, sx, sy, sz, st, failed);
+  const bool idem = op == OP_ADD || op == OP_MIN || op == OP_MAX || op == OP_EQ || op == OP_LEQ;
+  if (idem && sx != sy && sx != sz && sy != sz) st.dirty &= ~bit;
 }
 
 // Runs segment s on the calling warp (all 32 lanes): stage, sweep, join, and
 // list (or push on the warp's chase stack, when `chase`) the units of the
-// changed variables that have occurrences outside the segment.  Returns this
-// lane's count of bounds narrowed in the store.
+// changed variables that have occurrences outside the segment.  The sweeps
+// start from every propagator in a dense round, and otherwise from the
+// propagators of the variables that differ from the segment's snapshot (the
+// intervals its last run left at its own fixpoint: the others are still at
+// their fixpoint).  Returns this lane's count of bounds narrowed in the store.
 template <class Sched>
-__device__ int run_segment(const EvFixArgs &a, const Sched &sc, int s, SegWork &w, bool chase,
+__device__ int run_segment(const EvFixArgs &a, const Sched &sc, int s, SegWork &w, bool chase, bool full,
                            unsigned long long &execs, int &failed) {
   const int lane = threadIdx.x & 31;
   int got = 0;
@@ -366,19 +392,33 @@ __device__ int run_segment(const EvFixArgs &a, const Sched &sc, int s, SegWork &
   }
   const int p0 = __ldg(a.seg_pptr + s), np = __ldg(a.seg_pptr + s + 1) - p0;
   const int v0 = __ldg(a.seg_vptr + s), nl = __ldg(a.seg_vptr + s + 1) - v0;
+  const bool snap = !full && __ldcg(a.seg_valid + s);
+  unsigned long long start = 0ull;
   for (int i = lane; i < nl; i += 32) {
     const unsigned gv = __ldg(a.seg_var + v0 + i);
     const int2 t = __ldcg(a.store + (int)(gv & ~SEG_BOUNDARY));
+    const unsigned long long um = __ldg(a.seg_umask + v0 + i);
     w.var[i] = gv;
     w.iv[i] = t;
     w.orig[i] = t;
-    w.umask[i] = __ldg(a.seg_umask + v0 + i);
+    w.umask[i] = um;
+    if (snap) {
+      const int2 l = __ldcg(a.seg_last + v0 + i);
+      if (l.x != t.x || l.y != t.y) start |= um;
+    }
   }
   for (int k = lane; k < np; k += 32) w.code[k] = __ldg(a.seg_code + p0 + k);
+  if (snap) {
+    const unsigned lo = __reduce_or_sync(0xFFFFFFFFu, (unsigned)start);
+    const unsigned hi = __reduce_or_sync(0xFFFFFFFFu, (unsigned)(start >> 32));
+    start = (unsigned long long)hi << 32 | lo;
+  } else {
+    start = np >= 64 ? ~0ull : ((1ull << np) - 1ull);
+  }
   __syncwarp();
   int fl = 0, conv = 1;
   if (lane == 0) {
-    SegStore st{w.iv, w.umask, np >= 64 ? ~0ull : ((1ull << np) - 1ull)};
+    SegStore st{w.iv, w.umask, start};
     unsigned long long ex = 0;
     for (int pass = 0; st.dirty && !fl && pass < SEG_PASSES; ++pass) {
       for (int k = 0; k < np && !fl; ++k)
@@ -409,6 +449,10 @@ __device__ int run_segment(const EvFixArgs &a, const Sched &sc, int s, SegWork &
     if (hi) asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(&a.store[v].y), "r"(t.y) : "memory");
     changed += (int)lo + (int)hi;
     if (!(gv & SEG_BOUNDARY) || fl) continue;
+    if (Sched::kDense) {
+      sc.note(v);
+      continue;
+    }
     const int2 r = make_int2(__ldg(a.adj_ptr + v), __ldg(a.adj_ptr + v + 1));
     if (r.y - r.x == 2) {
       // a link variable: the one other unit
@@ -426,8 +470,12 @@ __device__ int run_segment(const EvFixArgs &a, const Sched &sc, int s, SegWork &
       sc.schedule_but(v, r, ~s);
     }
   }
+  // the snapshot of this run's own fixpoint (none when it stopped short)
+  if (conv && !fl)
+    for (int i = lane; i < nl; i += 32) a.seg_last[v0 + i] = w.iv[i];
   __syncwarp();
   if (lane == 0) {
+    a.seg_valid[s] = conv && !fl;
     __threadfence();
     atomicExch(a.seg_busy + s, 0);
     if (!conv && !fl) sc.list_unit(~s);  // sweeps left over: the rest next round
@@ -439,14 +487,15 @@ __device__ int run_segment(const EvFixArgs &a, const Sched &sc, int s, SegWork &
 // Runs segment s and the segments it chases (SEG_CHASE per entry, none
 // when chasing is off) on the calling warp.
 template <class Sched>
-__device__ int run_segment_chain(const EvFixArgs &a, const Sched &sc, int s, SegWork &w,
+__device__ int run_segment_chain(const EvFixArgs &a, const Sched &sc, int s, SegWork &w, bool full,
                                  unsigned long long &execs, int &failed) {
   const int lane = threadIdx.x & 31;
   int budget = a.chase > 0 ? SEG_CHASE : 0, changed = 0;
   if (lane == 0) w.sp = 0;
   __syncwarp();
   for (;;) {
-    changed += run_segment(a, sc, s, w, budget > 0, execs, failed);
+    changed += run_segment(a, sc, s, w, budget > 0, full, execs, failed);
+    full = false;  // chased segments start from what changed
     __syncwarp();
     const int sp = min(w.sp, SEG_STACK);
     if (sp == 0 || failed) break;
@@ -463,30 +512,23 @@ __device__ int run_segment_chain(const EvFixArgs &a, const Sched &sc, int s, Seg
   return changed;
 }
 
-// The warp phase of a round: a full round runs every segment (warps of the
-// grid strided), another round the segments its CTA queued.
+// The warp phase of an event round: the segments its CTA queued.
 template <class Sched>
-__device__ int run_segment_phase(const EvFixArgs &a, const Sched &sc, bool full, long long first_warp,
-                                 long long nwarps, SegQueue &q, SegWork *work, unsigned long long &execs,
-                                 int &failed) {
+__device__ int run_segment_phase(const EvFixArgs &a, const Sched &sc, SegQueue &q, SegWork *work,
+                                 unsigned long long &execs, int &failed) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   SegWork &w = work[warp];
   int changed = 0;
   // the lanes' own failures (from their propagators) made warp-uniform: the
   // segment code below runs on whole warps
   failed = __any_sync(0xFFFFFFFFu, failed) ? 1 : 0;
-  if (full) {
-    for (long long s = first_warp; s < a.nseg && !failed; s += nwarps)
-      changed += run_segment_chain(a, sc, (int)s, w, execs, failed);
-    return changed;
-  }
   const int items = min(q.n, SEG_QUEUE);
   for (;;) {
     int k = 0;
     if (lane == 0) k = atomicAdd(&q.head, 1);
     k = __shfl_sync(0xFFFFFFFFu, k, 0);
     if (k >= items || failed) break;
-    changed += run_segment_chain(a, sc, q.q[k], w, execs, failed);
+    changed += run_segment_chain(a, sc, q.q[k], w, false, execs, failed);
   }
   return changed;
 }
@@ -506,26 +548,110 @@ __device__ __forceinline__ bool in_segment(const EvFixArgs &a, long long p) {
   return a.nseg && ((__ldg(a.in_seg + (p >> 5)) >> (p & 31)) & 1u);
 }
 
-// Runs the frontier entries i = first, first + stride, ... < items of round
-// `round` (a full round, such as round 0: every propagator that is not in a
-// segment; segments go to the queue).  Returns the bounds narrowed.
-__device__ __forceinline__ int run_frontier(const EvFixArgs &a, long long round, bool full, long long items,
-                                            long long first, long long stride, int *stack, int *defer,
-                                            SegQueue &sq, unsigned long long &execs, int &failed) {
+// Runs the frontier entries i = first, first + stride, ... < items of event
+// round `round` (segments go to the queue).  Returns the bounds narrowed.
+__device__ __forceinline__ int run_frontier(const EvFixArgs &a, long long round, long long items, long long first,
+                                            long long stride, int *stack, int *defer, SegQueue &sq,
+                                            unsigned long long &execs, int &failed) {
   const EvSched sc = ev_sched(a, round);
   const int *cur = (round & 1) ? a.list1 : a.list0;
   int changed = 0;
   for (long long i = first; i < items && !failed; i += stride) {
-    if (full) {
-      if (in_segment(a, i)) continue;
-      changed += run_entry((int)i, a, sc, stack, defer, a.chase, execs, failed);
-    } else {
-      const int u = __ldcg(cur + i);
-      if (u < 0)
-        queue_segment(u, sq, sc);
-      else
-        changed += run_entry(u, a, sc, stack, defer, a.chase, execs, failed);
+    const int u = __ldcg(cur + i);
+    if (u < 0)
+      queue_segment(u, sq, sc);
+    else
+      changed += run_entry(u, a, sc, stack, defer, a.chase, execs, failed);
+  }
+  return changed;
+}
+
+// ---------------------------------------------------------- dense rounds ----
+//
+// Early rounds narrow a large share of the variables, and listing each
+// narrowed variable's units (a stamp atomic per unit) then costs more than
+// running every unit.  A dense round runs every propagator once (threads,
+// grid-strided, as an AC-1 sweep) and every segment (warps, all of it), and
+// only notes which variables it narrowed: the first narrowing of a variable
+// in the round appends it to the round's list (one atomic per variable).  The
+// next round is dense again while the noted variables' units number at least
+// n / dense_div and the list keeps shrinking (by an eighth over DENSE_WINDOW
+// dense rounds: deep propagation that narrows about the same variables round after
+// round, a long chain, moves faster in event rounds, whose chases dense
+// rounds lack);
+// otherwise an expansion phase lists the units of the noted variables and
+// event rounds go on.  A dense round ran every unit, so one that narrows nothing ends the
+// run at a fixpoint: the first round and the certifying sweep are dense
+// rounds.
+constexpr int DENSE_WINDOW = 16;
+
+struct DenseSched {
+  static constexpr bool kDense = true;
+  const int *adj_ptr;
+  unsigned *cstamp;
+  int *cvl;
+  unsigned *ccnt, *dsum, *dflag;
+  unsigned tag;
+  __device__ __forceinline__ void note(int v) const {
+    if (atomicMax(cstamp + v, tag) < tag) {
+      cvl[atomicAdd(ccnt, 1u)] = v;
+      atomicAdd(dsum, (unsigned)(__ldg(adj_ptr + v + 1) - __ldg(adj_ptr + v)));
     }
+  }
+  // a segment left with sweeps to do: the next round is dense again
+  __device__ __forceinline__ void list_unit(int) const { atomicOr(dflag, 1u); }
+  __device__ __forceinline__ void schedule_but(int v, int2, int) const { note(v); }
+};
+
+__device__ __forceinline__ DenseSched dense_sched(const EvFixArgs &a, long long round) {
+  DenseSched d;
+  d.adj_ptr = a.adj_ptr;
+  d.cstamp = a.cstamp;
+  d.cvl = (round & 1) ? a.cvl1 : a.cvl0;
+  d.ccnt = a.ccnt + (round % 3) * CNT_STRIDE;
+  d.dsum = a.dsum + (round % 3) * CNT_STRIDE;
+  d.dflag = a.dflag + (round % 3) * CNT_STRIDE;
+  d.tag = (unsigned)(round + 1);
+  return d;
+}
+
+// RedStore's joins, noting the narrowed variables.
+struct DenseStore {
+  int2 *s;
+  const DenseSched *sc;
+  __device__ __forceinline__ Itv load(int v) const {
+    const int2 t = __ldcg(s + v);
+    return mk(t.x, t.y);
+  }
+  __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
+    int c = 0;
+    if (r.l > seen.l) {
+      asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(&s[v].x), "r"(r.l) : "memory");
+      ++c;
+    }
+    if (r.u < seen.u) {
+      asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(&s[v].y), "r"(r.u) : "memory");
+      ++c;
+    }
+    if (c) {
+      sc->note(v);
+      if (is_bot(mk(max(seen.l, r.l), min(seen.u, r.u)))) failed = 1;
+    }
+    return c;
+  }
+};
+
+// The threads' part of a dense round: every propagator outside the segments.
+__device__ __forceinline__ int run_dense(const EvFixArgs &a, const DenseSched &ds, long long first, long long stride,
+                                         unsigned long long &execs, int &failed) {
+  DenseStore st{a.store, &ds};
+  int changed = 0;
+  for (long long i = first; i < a.n && !failed; i += stride) {
+    if (in_segment(a, i)) continue;
+    const int4 b = __ldg(a.bc + i);
+    const Itv o0 = st.load(b.y), o1 = st.load(b.z), o2 = st.load(b.w);
+    changed += deduce_loaded(b.x, b.y, b.z, b.w, o0, o1, o2, st, failed);
+    ++execs;
   }
   return changed;
 }
@@ -566,6 +692,8 @@ __device__ __forceinline__ int local_insert(int *tab, int key) {
 // Listing policy of the local rounds: EvSched's, with the round's sets and
 // the list head in shared memory.
 struct LocalSched {
+  static constexpr bool kDense = false;
+  __device__ __forceinline__ void note(int) const {}
   const int *adj;
   unsigned *pstamp, *sstamp, *vstamp;
   int *next;           // global list of the next round
@@ -677,7 +805,7 @@ __device__ void run_local(const EvFixArgs &a, long long round, int *stack, int *
     }
     if (a.nseg) {
       __syncthreads();
-      changed += run_segment_phase(a, sc, false, 0, 0, sq[p], work, execs, failed);
+      changed += run_segment_phase(a, sc, sq[p], work, execs, failed);
     }
     narrowed += changed;
     const unsigned bits = __reduce_or_sync(0xFFFFFFFFu, (changed ? 1u : 0u) | (failed ? 2u : 0u));
@@ -701,9 +829,11 @@ __device__ void run_local(const EvFixArgs &a, long long round, int *stack, int *
   }
   if (tid == 0) {
     // the grid runs round `round` from the global list (or, after a fixpoint,
-    // a full certifying round); it lists into the counter of round + 1
+    // the dense certifying round); it lists into the counter of round + 1
     if (state == EV_CONTINUE) a.cnt[(round % 3) * CNT_STRIDE] = sh.cnt[round % 3];
     a.cnt[((round + 1) % 3) * CNT_STRIDE] = 0u;
+    // a dense round (the certifying one) may come next
+    for (int k = 0; k < 3; ++k) a.ccnt[k * CNT_STRIDE] = a.dsum[k * CNT_STRIDE] = a.dflag[k * CNT_STRIDE] = 0u;
     a.ctl->ev_round = round;
     a.ctl->ev_state = state;
   }
@@ -723,12 +853,17 @@ __global__ void __launch_bounds__(EV_BLOCK, 2) k_fixpoint_events(EvFixArgs a) {
   const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
   unsigned long long execs = 0, narrowed = 0, cert_execs = 0, cert_narrowed = 0;
   long long round = 0, nbar = 0;
-  // Certifying round: when a round changes nothing, one more round runs every
-  // unit once, whatever the frontier lists, stamps and chases recorded.  If
-  // it narrows nothing the store is a fixpoint of every propagator; if it
-  // narrows, it lists as any round does and the rounds go on.  full_round is
-  // the last round that ran every unit (round 0 is one).
-  long long full_round = 0;
+  // Rounds are dense (round 0, the certifying sweep, and while many
+  // variables narrow) or event rounds; an event round after a dense one first
+  // expands the dense round's noted variables into its list.  Certifying
+  // sweep: when an event round changes nothing, a dense round runs every
+  // unit once, whatever the lists, stamps, chases and segment snapshots
+  // recorded; if it narrows nothing the store is a fixpoint of every
+  // propagator, and if it narrows the rounds go on.
+  bool dense = true, expand = false, certifying = false;
+  // variables noted by the last DENSE_WINDOW dense rounds of this stretch of dense rounds
+  long long hist[DENSE_WINDOW];
+  int stretch = 0;
   int state = EV_CONTINUE;
   if (tid == 0) {
     s_bits[0] = s_bits[1] = 0u;
@@ -736,10 +871,95 @@ __global__ void __launch_bounds__(EV_BLOCK, 2) k_fixpoint_events(EvFixArgs a) {
   }
   __syncthreads();
   for (;;) {
-    const bool full = round == full_round;
-    const long long items = full ? a.n : (long long)ld_relaxed(a.cnt + (round % 3) * CNT_STRIDE);
     const int p = (int)(nbar & 1), rp = (int)(round & 1);
-    if (!full && items <= (long long)a.local_max) {
+    if (dense) {
+      // counters: this round's noted variables and flag were cleared before
+      // it; the event lists of the next two rounds (an expansion lists into
+      // round + 1's) are cleared here, nobody reads them in a dense round
+      if (blockIdx.x == 0 && tid == 0) {
+        a.cnt[((round + 1) % 3) * CNT_STRIDE] = 0u;
+        a.cnt[((round + 2) % 3) * CNT_STRIDE] = 0u;
+        a.ccnt[((round + 1) % 3) * CNT_STRIDE] = 0u;
+        a.dsum[((round + 1) % 3) * CNT_STRIDE] = 0u;
+        a.dflag[((round + 1) % 3) * CNT_STRIDE] = 0u;
+      }
+      if (tid == 0) s_sq[0].n = s_sq[0].head = s_sq[1].n = s_sq[1].head = 0;
+      const DenseSched ds = dense_sched(a, round);
+      int failed = 0;
+      const unsigned long long execs0 = execs;
+      int changed = run_dense(a, ds, gtid, gstride, execs, failed);
+      if (a.nseg) {
+        SegWork &w = work[tid >> 5];
+        failed = __any_sync(0xFFFFFFFFu, failed) ? 1 : 0;
+        for (long long sg = gwarp; sg < a.nseg && !failed; sg += nwarps)
+          changed += run_segment(a, ds, (int)sg, w, false, true, execs, failed);
+      }
+      narrowed += changed;
+      if (certifying) {
+        cert_execs += execs - execs0;
+        cert_narrowed += changed;
+      }
+      const unsigned bits = __reduce_or_sync(0xFFFFFFFFu, (changed ? 1u : 0u) | (failed ? 2u : 0u));
+      if ((tid & 31) == 0 && bits) atomicOr(&s_bits[p], bits);
+      __syncthreads();
+      if (tid == 0) {
+        const unsigned b = s_bits[p];
+        s_bits[p] = 0u;
+        s_word[p] = grid_sync_rot(a.ctl, gridDim.x, nbar, b & 1u, b & 2u, a.timeout_ns);
+      }
+      __syncthreads();
+      const unsigned w = s_word[p];
+      ++nbar;
+      const long long noted = (long long)ld_relaxed(a.ccnt + (round % 3) * CNT_STRIDE);
+      const long long degs = (long long)ld_relaxed(a.dsum + (round % 3) * CNT_STRIDE);
+      const unsigned again = ld_relaxed(a.dflag + (round % 3) * CNT_STRIDE);
+      ++round;
+      certifying = false;
+      if (w & BIT_ERROR) {
+        state = EV_ERROR;
+        break;
+      }
+      if (w & BIT_FAILED) {
+        state = EV_FAILED;
+        break;
+      }
+      if (!(w & BIT_CHANGED)) {
+        state = EV_FIXPOINT;  // every unit ran and nothing narrowed
+        break;
+      }
+      if (a.max_rounds > 0 && round >= a.max_rounds) {
+        state = EV_CAP;
+        break;
+      }
+      dense = again || (a.dense_div > 0 && degs * a.dense_div >= a.n &&
+                        (stretch < DENSE_WINDOW || noted * 8 <= hist[stretch % DENSE_WINDOW] * 7));
+      hist[stretch % DENSE_WINDOW] = noted;
+      stretch = dense ? stretch + 1 : 0;
+      expand = !dense;
+      continue;
+    }
+    if (expand) {
+      // the units of the variables dense round - 1 noted, listed for this round
+      const EvSched sc = ev_sched(a, round - 1);
+      const int *cl = ((round - 1) & 1) ? a.cvl1 : a.cvl0;
+      const long long noted = (long long)ld_relaxed(a.ccnt + ((round - 1) % 3) * CNT_STRIDE);
+      for (long long j = gtid; j < noted; j += gstride) {
+        const int v = __ldcg(cl + j);
+        sc.schedule(v, make_int2(__ldg(a.adj_ptr + v), __ldg(a.adj_ptr + v + 1)));
+      }
+      __syncthreads();
+      if (tid == 0) s_word[p] = grid_sync_rot(a.ctl, gridDim.x, nbar, 0, 0, a.timeout_ns);
+      __syncthreads();
+      ++nbar;
+      if (s_word[p] & BIT_ERROR) {
+        state = EV_ERROR;
+        break;
+      }
+      expand = false;
+      continue;
+    }
+    const long long items = (long long)ld_relaxed(a.cnt + (round % 3) * CNT_STRIDE);
+    if (items <= (long long)a.local_max) {
       // small frontier: CTA 0 runs the rounds, everyone meets at the next grid barrier
       if (blockIdx.x == 0) run_local(a, round, s_stack + tid, s_defer + tid, s_sq, work, execs, narrowed);
       __syncthreads();
@@ -761,30 +981,30 @@ __global__ void __launch_bounds__(EV_BLOCK, 2) k_fixpoint_events(EvFixArgs a) {
           state = EV_CAP;  // no round left for the certifying one
           break;
         }
-        full_round = round;
+        dense = certifying = true;
         state = EV_CONTINUE;
         continue;
       }
       if (state != EV_CONTINUE) break;
       continue;
     }
-    // the counter of round + 2 was last read in round - 1; the other
+    // the counter of round + 2 was last read in round - 1, the noted-variable
+    // counter of round + 1 in the expansion before round - 1; the other
     // segment queue was last used in round - 1
-    if (blockIdx.x == 0 && tid == 0) a.cnt[((round + 2) % 3) * CNT_STRIDE] = 0u;
+    if (blockIdx.x == 0 && tid == 0) {
+      a.cnt[((round + 2) % 3) * CNT_STRIDE] = 0u;
+      a.ccnt[((round + 1) % 3) * CNT_STRIDE] = 0u;
+      a.dsum[((round + 1) % 3) * CNT_STRIDE] = 0u;
+      a.dflag[((round + 1) % 3) * CNT_STRIDE] = 0u;
+    }
     if (tid == 0) s_sq[rp ^ 1].n = s_sq[rp ^ 1].head = 0;
     int failed = 0;
-    const unsigned long long execs0 = execs;
-    int changed =
-        run_frontier(a, round, full, items, gtid, gstride, s_stack + tid, s_defer + tid, s_sq[rp], execs, failed);
+    int changed = run_frontier(a, round, items, gtid, gstride, s_stack + tid, s_defer + tid, s_sq[rp], execs, failed);
     if (a.nseg) {
       __syncthreads();
-      changed += run_segment_phase(a, ev_sched(a, round), full, gwarp, nwarps, s_sq[rp], work, execs, failed);
+      changed += run_segment_phase(a, ev_sched(a, round), s_sq[rp], work, execs, failed);
     }
     narrowed += changed;
-    if (full && round > 0) {
-      cert_execs += execs - execs0;
-      cert_narrowed += changed;
-    }
     const unsigned bits = __reduce_or_sync(0xFFFFFFFFu, (changed ? 1u : 0u) | (failed ? 2u : 0u));
     if ((tid & 31) == 0 && bits) atomicOr(&s_bits[p], bits);
     __syncthreads();
@@ -792,7 +1012,7 @@ __global__ void __launch_bounds__(EV_BLOCK, 2) k_fixpoint_events(EvFixArgs a) {
       // read and clear: the next grid round with this parity may come after
       // a local phase, which advances nbar without a grid round of the other
       // parity (a stale changed bit would then report a change that did not
-      // happen, and certifying rounds would follow one another for ever)
+      // happen)
       const unsigned b = s_bits[p];
       s_bits[p] = 0u;
       s_word[p] = grid_sync_rot(a.ctl, gridDim.x, nbar, b & 1u, b & 2u, a.timeout_ns);
@@ -809,13 +1029,13 @@ __global__ void __launch_bounds__(EV_BLOCK, 2) k_fixpoint_events(EvFixArgs a) {
       state = EV_FAILED;
       break;
     }
-    if (a.max_rounds > 0 && round >= a.max_rounds && (w & BIT_CHANGED || (a.certify && !full))) {
+    if (a.max_rounds > 0 && round >= a.max_rounds && (w & BIT_CHANGED || a.certify)) {
       state = EV_CAP;  // still changing, or no round left for the certifying one
       break;
     }
     if (!(w & BIT_CHANGED)) {
-      if (a.certify && !full) {
-        full_round = round;
+      if (a.certify) {
+        dense = certifying = true;
         continue;
       }
       state = EV_FIXPOINT;
@@ -850,10 +1070,14 @@ int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   int r;
   if ((r = events_graph(ctx, &g, opts.segments >= 0))) return r;
   const size_t n = (size_t)ctx->n, nv = (size_t)ctx->nvars, ns = (size_t)g.nseg;
-  // scratch: pstamp | sstamp | busy | vstamp | counters (cleared each run) | list 0 | list 1
-  const size_t o_s = align256(n * 4), o_b = o_s + align256(ns * 4), o_v = o_b + align256(ns * 4),
-               o_c = o_v + align256(nv * 4), o_l0 = o_c + 3 * CNT_STRIDE * 4, o_l1 = o_l0 + align256(n * 4),
-               bytes = o_l1 + align256(n * 4);
+  // scratch: pstamp | sstamp | busy | valid | vstamp | cstamp | counters
+  // (3 x list, noted, flag, degree sum; all cleared each run) | list 0 | list 1 | noted
+  // 0 | noted 1 | segment snapshots
+  const size_t o_s = align256(n * 4), o_b = o_s + align256(ns * 4), o_sv = o_b + align256(ns * 4),
+               o_v = o_sv + align256(ns * 4), o_cs = o_v + align256(nv * 4), o_c = o_cs + align256(nv * 4),
+               o_l0 = o_c + 12 * CNT_STRIDE * 4, o_l1 = o_l0 + align256(n * 4), o_n0 = o_l1 + align256(n * 4),
+               o_n1 = o_n0 + align256(nv * 4), o_last = o_n1 + align256(nv * 4),
+               bytes = o_last + align256((size_t)g.seg_nvar * 8);
   if ((r = ensure(ctx, &ctx->d_scratch, &ctx->cap_scratch, bytes))) return r;
   char *base = (char *)ctx->d_scratch;
   PIR_CK(cudaMemsetAsync(base, 0, o_l0, ctx->stream));
@@ -866,10 +1090,20 @@ int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   a.pstamp = (unsigned *)base;
   a.sstamp = (unsigned *)(base + o_s);
   a.seg_busy = (int *)(base + o_b);
+  a.seg_valid = (int *)(base + o_sv);
+  a.seg_last = (int2 *)(base + o_last);
   a.vstamp = (unsigned *)(base + o_v);
   a.cnt = (unsigned *)(base + o_c);
+  a.ccnt = a.cnt + 3 * CNT_STRIDE;
+  a.dflag = a.cnt + 6 * CNT_STRIDE;
+  a.dsum = a.cnt + 9 * CNT_STRIDE;
+  a.cstamp = (unsigned *)(base + o_cs);
   a.list0 = (int *)(base + o_l0);
   a.list1 = (int *)(base + o_l1);
+  a.cvl0 = (int *)(base + o_n0);
+  a.cvl1 = (int *)(base + o_n1);
+  a.nvars = ctx->nvars;
+  a.dense_div = opts.dense > 0 ? opts.dense : (opts.dense < 0 ? 0 : 32);
   a.ctl = ctx->d_ctl;
   a.n = ctx->n;
   a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;

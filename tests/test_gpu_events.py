@@ -323,3 +323,22 @@ def test_kat_events(case, P):
         pass
     E.sched = P.SCHED_EVENTS
     assert run_case(case, E) == []
+
+
+@pytest.mark.parametrize("dense", [0, -1, 1, 1000])
+def test_events_dense_rounds(dense, P, oracle):
+    """Dense rounds (every unit once, AC-1 style, noting the narrowed
+    variables) while the narrowed variables' units are at least 1/dense of
+    all and getting fewer (0: 1/32; -1: only the first and the certifying
+    round; 1: hardly ever; 1000: nearly every round), then event rounds from
+    the noted variables: the oracle's fixpoint or failure every time."""
+    import workloads as W
+    insts = [W.add_chain(W.plain(30_000, 120_000, 10**6, 11), 2000, 10**6, 11), _mixed_chain(800, 3),
+             W.single_small(2, variant="spec")] + W.uneven(2, 2000, 20_000, 5)
+    for inst in insts:
+        for segments in (0, -1):
+            rc, g, st, orc, o, _ = _both(P, oracle, inst, dense=dense, segments=segments)
+            assert rc == orc
+            if orc == oracle.OK:
+                np.testing.assert_array_equal(g, o)
+                assert st["certify_narrowed"] == 0

@@ -236,3 +236,36 @@ def test_quotient_extremes_at_sign_analysis_corners():
             for n in vals:
                 assert (cdiv(a, b) > n) == ((a > n * b) if b > 0 else (a < n * b))
                 assert (fdiv(a, b) < n) == ((a < n * b) if b > 0 else (a > n * b))
+
+
+def test_idempotent_opcodes(oracle):
+    """ADD, MIN, MAX and the reified EQ / LEQ (target inside [0, 1], as install
+    leaves it) are idempotent: a second run on the intervals the first left
+    narrows nothing.  Checked on every triple of sub-intervals of [-6, 6]
+    together with unbounded ends, and on a grid of bounds at the int32
+    saturation edges.  The event kernel's segment sweeps rely on it to skip
+    re-running such a propagator after its own narrowing (and MUL and the
+    divisions are not idempotent, so they are re-run)."""
+    import itertools
+    INF, MINF = 2**31 - 1, -2**31
+    small = [(a, b) for a in range(-6, 7) for b in range(-6, 7) if a <= b]
+    small += [(MINF, 3), (-2, INF), (MINF, INF), (0, INF), (MINF, 0)]
+    edge = [MINF, MINF + 1, -2**30, -1, 0, 1, 2**30, INF - 1, INF]
+    edge = [(a, b) for a in edge for b in edge if a <= b and a != INF and b != MINF]
+    for itv in (small, edge):
+        itv = np.array(itv, np.int64)
+        idx = np.array(list(itertools.product(range(len(itv)), repeat=3)))
+        lb = itv[idx][:, :, 0].astype(np.int32)
+        ub = itv[idx][:, :, 1].astype(np.int32)
+        for op in (0, 6, 7, 8, 9):
+            L, U = lb.copy(), ub.copy()
+            if op in (8, 9):
+                L[:, 0] = np.maximum(L[:, 0], 0)
+                U[:, 0] = np.minimum(U[:, 0], 1)
+                keep = L[:, 0] <= U[:, 0]
+                L, U = L[keep], U[keep]
+            ops = np.full(len(L), op, np.int32)
+            l1, u1, _, f1, _ = oracle.deduce_batch(ops, L, U)
+            _, _, ch2, _, _ = oracle.deduce_batch(ops, l1, u1)
+            ok = ~f1 & ~(l1 > u1).any(1) & ~(l1 == INF).any(1) & ~(u1 == MINF).any(1)
+            assert not (ok & ch2).any(), op
