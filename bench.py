@@ -581,6 +581,7 @@ def run_ours(args):
     if ws == 1 and args.workload == "single_large" and not args.no_extras:
         more["out_of_l2"] = out_of_l2_record(cr, hbm)
         more["nodes"] = nodes_record(cr, args)
+        more["uneven"] = uneven_record(cr, args)
     out = {
         "metric": "propagator executions/sec", "value": value, "unit": "executions/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -808,6 +809,113 @@ def run_learned(args):
     print(json.dumps(out), flush=True)
 
 
+UNEVEN_DESC = ("uneven: 512 instances, propagators log-uniform [1e3, 2e5], vars = props/4, "
+               "5% tdiv + 5% tmod")
+
+
+def _uneven_pinned(cr, packed):
+    """The packed instances in pinned host buffers (the stores are reset from
+    lb0 / ub0 before every call)."""
+    prop_off, var_off, op, x, y, z, lb0, ub0 = packed
+    pinned = []
+    for a in (op, x, y, z, lb0, ub0):
+        b = cr.pinned(len(a))
+        b[:] = a
+        pinned.append(b)
+    return (prop_off, var_off) + tuple(pinned) + (lb0, ub0)
+
+
+def _uneven_time(cr, ctx, pk, sched, steps, warmup):
+    """pir_fixpoint_instances from pinned host buffers (install, copies in and
+    out inside each call), `steps` timed calls after `warmup`: device seconds
+    (CUDA events around the kernels), wall seconds of the calls, per-instance
+    device ms, the last call's statuses, stats and stores."""
+    prop_off, var_off, op, x, y, z, lb, ub, lb0, ub0 = pk
+    for _ in range(warmup):
+        lb[:], ub[:] = lb0, ub0
+        ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub, sched=sched)
+    cr.sync()
+    runs, walls, per = [], [], []
+    for _ in range(steps):
+        lb[:], ub[:] = lb0, ub0
+        t0 = time.perf_counter()
+        status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub, sched=sched)
+        walls.append(time.perf_counter() - t0)
+        runs.append(st)
+        per.append(ms)
+    return {"dev_s": sum(r["device_ms"] for r in runs) / 1e3, "wall_s": sum(walls), "per": np.concatenate(per),
+            "status": status, "rounds": rounds, "executions": sum(r["executions"] for r in runs),
+            "lb": lb.copy(), "ub": ub.copy()}
+
+
+def _uneven_cpu(packed):
+    """The oracle on every instance (install + Gauss-Seidel each) over the
+    host's threads: (seconds, statuses, stores)."""
+    from oracle import oracle as O
+    prop_off, var_off, op, x, y, z, lb0, ub0 = packed
+    s = np.ascontiguousarray(np.stack([lb0, ub0], 1))
+    th = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ost, _ = O.fixpoint_instances(prop_off, var_off, op, x, y, z, s, threads=th)
+    return time.perf_counter() - t0, th, ost, s
+
+
+def _uneven_equal(r, packed, ost, s):
+    """Instances whose status equals the oracle's and, when OK, whose store is
+    the oracle's bit for bit."""
+    var_off = packed[1]
+    n = 0
+    for j in range(len(ost)):
+        if r["status"][j] != ost[j]:
+            continue
+        v0, v1 = var_off[j], var_off[j + 1]
+        if ost[j] != 0 or (np.array_equal(r["lb"][v0:v1], s[v0:v1, 0]) and
+                           np.array_equal(r["ub"][v0:v1], s[v0:v1, 1])):
+            n += 1
+    return n
+
+
+def uneven_record(cr, args):
+    """The uneven-instance workload beside the single instance in the default
+    line: instances/s under the event-filtered rounds and under AC-1 (device
+    time and end to end through the C ABI), p50 / p99 per-instance time, every
+    instance checked against the oracle, which is also the CPU baseline."""
+    import pirgpu
+    import workloads as W
+    t0 = time.perf_counter()
+    insts = W.uneven(512, 1000, 200_000, 0)
+    packed = W.pack(insts)
+    gen_s = time.perf_counter() - t0
+    n = len(insts)
+    ctx = pirgpu.Context(0)
+    pk = _uneven_pinned(cr, packed)
+    steps = max(3, min(args.steps, 5))
+    res = {name: _uneven_time(cr, ctx, pk, sched, steps, 2)
+           for name, sched in (("events", pirgpu.SCHED_EVENTS), ("ac1", pirgpu.SCHED_AC1))}
+    ctx.close()
+    cpu_s, th, ost, s = _uneven_cpu(packed)
+    hbm, _ = peaks()
+    out = {"workload": UNEVEN_DESC, "propagators": int(packed[0][-1]), "generate_s": gen_s}
+    for name, r in res.items():
+        out[name] = {"value": n * steps / r["dev_s"], "unit": "instances/s", "ms_per_step": r["dev_s"] * 1e3 / steps,
+                     "instance_ms_p50": float(np.percentile(r["per"], 50)),
+                     "instance_ms_p99": float(np.percentile(r["per"], 99)),
+                     "executions_per_step": r["executions"] // steps,
+                     "max_rounds": int(r["rounds"].max()),
+                     "roofline_frac": r["executions"] * ALG_BYTES_PER_EXEC / r["dev_s"] / 1e9 / hbm,
+                     "e2e": {"value": n * steps / r["wall_s"], "unit": "instances/s",
+                             "h2d_bytes_per_step": int(packed[0][-1] * 16 + packed[1][-1] * 8),
+                             "d2h_bytes_per_step": int(packed[1][-1] * 8)},
+                     "bit_exact": {"instances_checked": n, "instances_equal": _uneven_equal(r, packed, ost, s)}}
+    out["events_over_ac1"] = res["ac1"]["dev_s"] / res["events"]["dev_s"]
+    out["cpu_baseline"] = {"value": n / cpu_s, "unit": "instances/s", "cores": th, "kind": "port",
+                           "sample": "all %d instances (install + Gauss-Seidel each), %d host threads, %.1f s"
+                                     % (n, th, cpu_s)}
+    out["schedule"] = "events: a round runs the propagators of the variables the previous round narrowed"
+    out["l2"] = "not flushed: each step copies 387 MB of instances in, more than the 129 MB L2"
+    return out
+
+
 def run_uneven(args):
     """512 independent instances, propagators log-uniform in [1e3, 2e5]."""
     import pirgpu
@@ -819,85 +927,55 @@ def run_uneven(args):
     cr.set_device(local)
     insts_all = W.uneven(512, 1000, 200_000, 0)
     n_all = len(insts_all)
-    prop_off, var_off, op, x, y, z, lb0, ub0 = W.pack(insts_all)
-    total_props = int(prop_off[-1])
-    insts = insts_all
+    packed = W.pack(insts_all)
+    total_props = int(packed[0][-1])
     if ws > 1:
         # this rank's instances (cost-balanced partition, no collective on the data path)
-        parts = shard.lpt_partition(shard.instance_costs(prop_off), ws)
-        prop_off, var_off, op, x, y, z, lb0, ub0 = shard.select_instances(prop_off, var_off, op, x, y, z,
-                                                                          lb0, ub0, parts[rank])
-        insts = [insts_all[i] for i in parts[rank]]
+        parts = shard.lpt_partition(shard.instance_costs(packed[0]), ws)
+        packed = shard.select_instances(*packed, parts[rank])
+    sched = {"events": pirgpu.SCHED_EVENTS, "ac1": pirgpu.SCHED_AC1}[args.inst_sched]
     ctx = pirgpu.Context(local)
-    # inputs in pinned host buffers (the stores are updated in place: reset before every step)
-    pinned = []
-    for a in (op, x, y, z):
-        b = cr.pinned(len(a))
-        b[:] = a
-        pinned.append(b)
-    op, x, y, z = pinned
-    lb, ub = cr.pinned(len(lb0)), cr.pinned(len(ub0))
-    for _ in range(args.warmup):
-        lb[:], ub[:] = lb0, ub0
-        ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
+    pk = _uneven_pinned(cr, packed)
     if dist:
         dist.barrier()
-    cr.sync()
     clk = ClockSampler(local)
     clk.start()
-    runs, walls, per = [], [], []
-    for _ in range(args.steps):
-        lb[:], ub[:] = lb0, ub0
-        t0 = time.perf_counter()
-        status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
-        walls.append(time.perf_counter() - t0)
-        runs.append(st)
-        per.append(ms)
+    r = _uneven_time(cr, ctx, pk, sched, args.steps, args.warmup)
     clocks = clk.stop()
-    dev_s = sum(r["device_ms"] for r in runs) / 1e3
-    t_max = dist_max(dist, dev_s)
-    wall_max = dist_max(dist, sum(walls))
-    n_failed = int(dist_sum(dist, int((status == 1).sum())))
-    per = np.concatenate(per)
-    per_all = shard.gather_to_root(dist, per)
+    t_max = dist_max(dist, r["dev_s"])
+    wall_max = dist_max(dist, r["wall_s"])
+    n_failed = int(dist_sum(dist, int((r["status"] == 1).sum())))
+    per_all = shard.gather_to_root(dist, r["per"])
     if rank != 0:
         return
     per_all = np.concatenate(per_all)
-    n = len(insts)
-    execs = sum(r["executions"] for r in runs)
     hbm, hbm_src = peaks()
-    achieved = execs * ALG_BYTES_PER_EXEC / dev_s / 1e9
+    achieved = r["executions"] * ALG_BYTES_PER_EXEC / r["dev_s"] / 1e9
     cpu = None
     if ws == 1 and not args.no_cpu:
-        from oracle import oracle as O
-        m = n
-        sub = insts
-        po, vo, o2, x2, y2, z2, l2, u2 = W.pack(sub)
-        s = np.ascontiguousarray(np.stack([l2, u2], 1))
-        th = os.cpu_count() or 1
-        t0 = time.perf_counter()
-        O.fixpoint_instances(po, vo, o2, x2, y2, z2, s, threads=th)
-        ct = time.perf_counter() - t0
-        cpu = {"value": m / ct, "unit": "instances/s", "cores": th, "kind": "port",
-               "sample": "all %d instances (install + Gauss-Seidel each), %d host threads, %.1f s" % (m, th, ct)}
+        ct, th, ost, s = _uneven_cpu(packed)
+        cpu = {"value": n_all / ct, "unit": "instances/s", "cores": th, "kind": "port",
+               "sample": "all %d instances (install + Gauss-Seidel each), %d host threads, %.1f s" % (n_all, th, ct),
+               "instances_equal": _uneven_equal(r, packed, ost, s)}
+    prof = "instances_cluster_uneven_512" if args.inst_sched == "ac1" else "instances_events_uneven_512"
     out = {
         "metric": "batched instances/sec", "value": n_all * args.steps / t_max, "unit": "instances/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic: planted-solution instances",
-        "config": {"workload": "uneven: 512 instances, propagators log-uniform [1e3, 2e5], vars = props/4, "
-                               "5% tdiv + 5% tmod", "propagators": total_props,
+        "config": {"workload": UNEVEN_DESC, "propagators": total_props, "schedule": args.inst_sched,
                    "parallelism": "instances sharded over %d ranks (cost-balanced, no collective)" % ws
                    if ws > 1 else "single",
                    "instance_ms_p50": float(np.percentile(per_all, 50)),
                    "instance_ms_p99": float(np.percentile(per_all, 99)),
+                   "executions_per_step": r["executions"] // args.steps,
                    "failed": n_failed},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": ncu_traffic("instances_cluster_uneven_512"), "peak_source": hbm_src},
+                     "traffic": ncu_traffic(prof), "peak_source": hbm_src},
         "cpu_baseline": cpu,
         "e2e": {"value": n_all * args.steps / wall_max, "unit": "instances/s",
-                "h2d_bytes_per_step": int(prop_off[-1] * 16 + var_off[-1] * 8),
-                "d2h_bytes_per_step": int(var_off[-1] * 8)},
+                "h2d_bytes_per_step": int(packed[0][-1] * 16 + packed[1][-1] * 8),
+                "d2h_bytes_per_step": int(packed[1][-1] * 8)},
         # per step: store pack, the cluster kernel, the one-CTA-per-instance kernel, store unpack
         "gpu_launches": 4 * args.steps, "clocks": clocks,
     }
@@ -1196,6 +1274,8 @@ def main():
     ap.add_argument("--cpu-instances", type=int, default=128)
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--node-sched", default="events", choices=["events", "ac1"])
+    ap.add_argument("--inst-sched", default="events", choices=["events", "ac1"],
+                    help="uneven workload: event-filtered or AC-1 rounds")
     ap.add_argument("--wake-fraction", type=float, default=1 / 32)
     ap.add_argument("--queens", type=int, default=12, help="search workload: board size")
     ap.add_argument("--cpu-search-nodes", type=int, default=2_000_000, help="search workload: CPU node cap")

@@ -32,6 +32,7 @@ struct InstOut {
   int rounds;
   unsigned long long ns;
   unsigned long long narrowed;
+  unsigned long long execs;  // executions of the event-filtered rounds
 };
 
 struct NodeOut {
@@ -170,6 +171,84 @@ __device__ __forceinline__ void cta_rounds(const Bytecode &bc, S &st, long long 
   }
 }
 
+// ------------------------------------------- event-filtered instance rounds -
+//
+// opts.sched = PIR_SCHED_EVENTS for instances: round r runs a propagator only
+// when one of its variables was narrowed in round r - 1 (round 0 runs every
+// one).  A join marks its variable in round r's bitmap right after it lands,
+// before the round's barrier, so a narrowing that a propagator did not see
+// when it read puts that propagator into the next round.  A propagator skipped
+// in round r therefore read, at its last run, the intervals it would read now,
+// and a round that narrows nothing is a fixpoint, as in AC-1.  Three bitmaps
+// of ceil(nvars / 32) words rotate: round r reads bitmap (r - 1) % 3, marks
+// r % 3 and clears (r + 1) % 3, which no thread reads or marks in round r.
+__host__ __device__ constexpr int mark_words(int nv) { return (nv + 31) >> 5; }
+__host__ __device__ constexpr int mark_bytes(int nv) { return ((3 * mark_words(nv) * 4 + 15) / 16) * 16; }
+
+__device__ __forceinline__ bool marked(const unsigned *m, int v) { return (m[v >> 5] >> (v & 31)) & 1u; }
+
+template <class S>
+struct MarkedStore {
+  S s;
+  unsigned *cur;  // round r's bitmap (shared memory)
+  __device__ __forceinline__ Itv load(int v) const { return s.load(v); }
+  __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
+    const int n = s.embed(v, seen, r, failed);
+    if (n) {
+      const unsigned bit = 1u << (v & 31);
+      if (!(*(volatile unsigned *)(cur + (v >> 5)) & bit)) atomicOr(cur + (v >> 5), bit);
+    }
+    return n;
+  }
+};
+
+// Propagator i, if round r's filter lets it run (prev: bitmap of round r - 1,
+// null in round 0); `ran` counts the executions.
+template <bool GBC, class S>
+__device__ __forceinline__ int marked_step(const Bytecode &bc, int i, S &st, const unsigned *prev, int &failed,
+                                           int &ran) {
+  const int o = bc_load<GBC>(reinterpret_cast<const int *>(bc.op) + i);
+  if (o == OP_NOP) return 0;
+  const int X = bc_load<GBC>(reinterpret_cast<const int *>(bc.x) + i);
+  const int Y = bc_load<GBC>(reinterpret_cast<const int *>(bc.y) + i);
+  const int Z = bc_load<GBC>(reinterpret_cast<const int *>(bc.z) + i);
+  if (prev && !(marked(prev, X) | marked(prev, Y) | marked(prev, Z))) return 0;
+  ++ran;
+  const Itv a = st.load(X), b = st.load(Y), d = st.load(Z);
+  return deduce_loaded(o, X, Y, Z, a, b, d, st, failed);
+}
+
+// One CTA's event-filtered rounds; marks: the three bitmaps in shared memory.
+template <bool GBC, class S>
+__device__ __forceinline__ void cta_rounds_marked(const Bytecode &bc, S &st, unsigned *marks, int nv,
+                                                  long long max_rounds, long long &rounds, int &failed, int &changed,
+                                                  unsigned long long &narrowed, unsigned long long &execs) {
+  const int words = mark_words(nv);
+  for (int w = threadIdx.x; w < words; w += blockDim.x) marks[w] = 0;
+  __syncthreads();
+  rounds = 0;
+  for (;;) {
+    const int r = (int)(rounds % 3);
+    const unsigned *prev = rounds ? marks + ((r + 2) % 3) * words : nullptr;
+    unsigned *nxt = marks + ((r + 1) % 3) * words;
+    for (int w = threadIdx.x; w < words; w += blockDim.x) nxt[w] = 0;
+    MarkedStore<S> ms{st, marks + r * words};
+    int ch = 0, f = 0, ran = 0;
+    for (int i = threadIdx.x; i < bc.nchunks * 4; i += blockDim.x) ch += marked_step<GBC>(bc, i, ms, prev, f, ran);
+    narrowed += ch;
+    execs += ran;
+    const int any_ch = __syncthreads_or(ch);
+    const int any_f = __syncthreads_or(f);
+    ++rounds;
+    if (any_f || !any_ch || (max_rounds > 0 && rounds >= max_rounds)) {
+      failed = any_f;
+      changed = any_ch;
+      return;
+    }
+  }
+}
+
+template <bool MARKS>
 __global__ void __launch_bounds__(512, 2) k_instances(InstArgs a) {
   extern __shared__ int4 sm[];
   __shared__ int s_k;
@@ -195,14 +274,18 @@ __global__ void __launch_bounds__(512, 2) k_instances(InstArgs a) {
     long long rounds = 0;
     int failed = 0, changed = 0;
     unsigned long long narrowed = 0;
+    unsigned long long execs = 0;
     const int store_bytes = ((nv * 8 + 15) / 16) * 16;
-    if (store_bytes <= a.smem_cap) {
+    // the three round bitmaps of the event-filtered rounds follow the store
+    const int mbytes = MARKS ? mark_bytes(nv) : 0;
+    if (store_bytes + mbytes <= a.smem_cap) {
       int2 *ss = reinterpret_cast<int2 *>(sm);
+      unsigned *marks = reinterpret_cast<unsigned *>(sm + store_bytes / 16);
       for (int v = threadIdx.x; v < nv; v += blockDim.x) ss[v] = gs[v];
       Bytecode sb = bc;
-      const bool bc_in_smem = store_bytes + nch * 64 <= a.smem_cap;
+      const bool bc_in_smem = store_bytes + mbytes + nch * 64 <= a.smem_cap;
       if (bc_in_smem) {
-        int4 *b4 = sm + store_bytes / 16;
+        int4 *b4 = sm + (store_bytes + mbytes) / 16;
         int4 *sop = b4, *sx = b4 + nch, *sy = b4 + 2 * nch, *sz = b4 + 3 * nch;
         for (int c = threadIdx.x; c < nch; c += blockDim.x) {
           sop[c] = bc.op[c];
@@ -219,20 +302,35 @@ __global__ void __launch_bounds__(512, 2) k_instances(InstArgs a) {
       SmemStore st{ss};
       install_chunks(sb, st);
       __syncthreads();
-      if (bc_in_smem)
-        cta_rounds<false>(sb, st, a.max_rounds, rounds, failed, changed, narrowed);
-      else
-        cta_rounds<true>(sb, st, a.max_rounds, rounds, failed, changed, narrowed);
+      if constexpr (MARKS) {
+        if (bc_in_smem)
+          cta_rounds_marked<false>(sb, st, marks, nv, a.max_rounds, rounds, failed, changed, narrowed, execs);
+        else
+          cta_rounds_marked<true>(sb, st, marks, nv, a.max_rounds, rounds, failed, changed, narrowed, execs);
+      } else {
+        if (bc_in_smem)
+          cta_rounds<false>(sb, st, a.max_rounds, rounds, failed, changed, narrowed);
+        else
+          cta_rounds<true>(sb, st, a.max_rounds, rounds, failed, changed, narrowed);
+      }
       for (int v = threadIdx.x; v < nv; v += blockDim.x) gs[v] = ss[v];
     } else {
       GlobalStore gst{gs};
       install_chunks(bc, gst);
       __syncthreads();
       RedStore st{gs};
-      cta_rounds<true>(bc, st, a.max_rounds, rounds, failed, changed, narrowed);
+      if (MARKS && mbytes <= a.smem_cap)
+        cta_rounds_marked<true>(bc, st, reinterpret_cast<unsigned *>(sm), nv, a.max_rounds, rounds, failed, changed,
+                                narrowed, execs);
+      else
+        cta_rounds<true>(bc, st, a.max_rounds, rounds, failed, changed, narrowed);
     }
     narrowed = warp_sum64(narrowed);
     if ((threadIdx.x & 31) == 0 && narrowed) atomicAdd(&a.out[j].narrowed, narrowed);
+    if constexpr (MARKS) {
+      execs = warp_sum64(execs);
+      if ((threadIdx.x & 31) == 0 && execs) atomicAdd(&a.out[j].execs, execs);
+    }
     if (threadIdx.x == 0) {
       a.out[j].status = failed ? PIR_FAILED : (changed ? PIR_TIMEOUT : PIR_OK);
       a.out[j].rounds = (int)rounds;
@@ -291,6 +389,34 @@ struct DsmStore {
   }
 };
 
+// The store of DsmStore with the round bitmaps of the event-filtered rounds:
+// every CTA holds a full copy of each bitmap (at the same shared-memory offset
+// in every CTA), so the filter reads only its own; a join marks its variable
+// in all CLU copies of round r's bitmap with cluster-scope reductions, unless
+// this CTA's copy already has it (then another join marked, or is marking,
+// every copy before the round's cluster barrier).
+struct MarkedDsm {
+  DsmStore s;
+  unsigned *cur;  // this CTA's copy of round r's bitmap (generic address)
+  __device__ __forceinline__ Itv load(int v) const { return s.load(v); }
+  __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
+    const int n = s.embed(v, seen, r, failed);
+    if (n) {
+      const unsigned bit = 1u << (v & 31);
+      unsigned *w = cur + (v >> 5);
+      if (!(*(volatile unsigned *)w & bit)) {
+#pragma unroll
+        for (int q = 0; q < CLU; ++q) {
+          unsigned long long pa;
+          asm("mapa.u64 %0, %1, %2;" : "=l"(pa) : "l"(w), "r"(q));
+          asm volatile("red.relaxed.cluster.or.b32 [%0], %1;" ::"l"(pa), "r"(bit) : "memory");
+        }
+      }
+    }
+    return n;
+  }
+};
+
 struct CluArgs {
   const int4 *op, *x, *y, *z;
   const long long *coff, *voff;
@@ -300,8 +426,10 @@ struct CluArgs {
   int *next;
   InstOut *out;
   long long max_rounds;
+  int smem_cap;  // dynamic shared memory per CTA
 };
 
+template <bool MARKS>
 __global__ void __launch_bounds__(CLU_BLOCK, 1) k_instances_cluster(CluArgs a) {
   extern __shared__ int4 sm[];
   __shared__ int s_inst;
@@ -336,6 +464,14 @@ __global__ void __launch_bounds__(CLU_BLOCK, 1) k_instances_cluster(CluArgs a) {
     if (rank == 0 && threadIdx.x == 0) s_t0 = globaltimer();
     // this CTA's slots: variables v = CLU * i + rank
     for (int i = threadIdx.x; CLU * i + rank < nv; i += blockDim.x) mine[i] = gs[CLU * i + rank];
+    // event-filtered rounds: this CTA's copies of the three round bitmaps
+    // follow its slots; round 0's starts clear
+    const int slot_bytes = (((nv + CLU - 1) / CLU) * 8 + 15) / 16 * 16;
+    const bool use_marks = MARKS && slot_bytes + mark_bytes(nv) <= a.smem_cap;
+    const int words = mark_words(nv);
+    unsigned *marks = reinterpret_cast<unsigned *>(sm + slot_bytes / 16);
+    if (MARKS && use_marks)
+      for (int w = threadIdx.x; w < words; w += blockDim.x) marks[w] = 0;
     Bytecode bc;
     bc.op = a.op + c0;
     bc.x = a.x + c0;
@@ -354,14 +490,24 @@ __global__ void __launch_bounds__(CLU_BLOCK, 1) k_instances_cluster(CluArgs a) {
     cluster.sync();
     long long round = 0;
     unsigned changed_any = 0, failed_any = 0;
-    unsigned long long narrowed = 0;
+    unsigned long long narrowed = 0, execs = 0;
     for (;;) {
       const int par = (int)(round % 3);
       if (rank == 0 && threadIdx.x == 0) s_flags[(round + 1) % 3][0] = s_flags[(round + 1) % 3][1] = 0;
       int ch = 0, f = 0;
-      // one propagator per thread and step: 1,024 threads of 64 registers keep
-      // twice the warps of 512 x 4-wide steps resident
-      for (int c = ctid; c < nch * 4; c += cstride) ch += sweep_step<1>(bc, c, st, f);
+      if (MARKS && use_marks) {
+        const unsigned *prev = round ? marks + ((par + 2) % 3) * words : nullptr;
+        unsigned *nxt = marks + ((par + 1) % 3) * words;
+        for (int w = threadIdx.x; w < words; w += blockDim.x) nxt[w] = 0;
+        MarkedDsm ms{st, marks + par * words};
+        int ran = 0;
+        for (int i = ctid; i < nch * 4; i += cstride) ch += marked_step<true>(bc, i, ms, prev, f, ran);
+        execs += ran;
+      } else {
+        // one propagator per thread and step: 1,024 threads of 64 registers
+        // keep twice the warps of 512 x 4-wide steps resident
+        for (int c = ctid; c < nch * 4; c += cstride) ch += sweep_step<1>(bc, c, st, f);
+      }
       narrowed += ch;
       const int any_ch = __syncthreads_or(ch), any_f = __syncthreads_or(f);
       if (threadIdx.x == 0) {
@@ -377,6 +523,10 @@ __global__ void __launch_bounds__(CLU_BLOCK, 1) k_instances_cluster(CluArgs a) {
     for (int i = threadIdx.x; CLU * i + rank < nv; i += blockDim.x) gs[CLU * i + rank] = mine[i];
     narrowed = warp_sum64(narrowed);
     if ((threadIdx.x & 31) == 0 && narrowed) atomicAdd(&a.out[j].narrowed, narrowed);
+    if constexpr (MARKS) {
+      execs = warp_sum64(execs);
+      if ((threadIdx.x & 31) == 0 && execs) atomicAdd(&a.out[j].execs, execs);
+    }
     if (rank == 0 && threadIdx.x == 0) {
       a.out[j].status = failed_any ? PIR_FAILED : (changed_any ? PIR_TIMEOUT : PIR_OK);
       a.out[j].rounds = (int)round;
@@ -1660,6 +1810,9 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   std::memset(&opts, 0, sizeof(opts));
   if (opts_in) opts = *opts_in;
   if (prop_off[0] != 0 || var_off[0] != 0) return set_err(ctx, PIR_EINVAL, "offsets must start at 0");
+  if (opts.sched != PIR_SCHED_AC1 && opts.sched != PIR_SCHED_EVENTS)
+    return set_err(ctx, PIR_EINVAL, "instances run AC-1 or event-filtered rounds (sched %d)", opts.sched);
+  const int marks = opts.sched == PIR_SCHED_EVENTS;
   for (int j = 0; j < ninst; ++j) {
     if (prop_off[j + 1] < prop_off[j] || var_off[j + 1] < var_off[j])
       return set_err(ctx, PIR_EINVAL, "offsets of instance %d decrease", j);
@@ -1703,10 +1856,6 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   const size_t stage_ints = (size_t)std::max<long long>(nchunks, 1) * 16;
   if (b->cap_stage < stage_ints) {
     if (b->h_stage) cudaFreeHost(b->h_stage);
-  if (b->sgx) cudaGraphExecDestroy(b->sgx);
-  if (b->sg) cudaGraphDestroy(b->sg);
-  if (b->h_sin) cudaFreeHost(b->h_sin);
-  if (b->h_sout) cudaFreeHost(b->h_sout);
     b->h_stage = nullptr;
     b->cap_stage = 0;
     if (cudaMallocHost(&b->h_stage, stage_ints * sizeof(int)) != cudaSuccess) {
@@ -1753,7 +1902,8 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
     for (int j : order) {
       const long long nv = var_off[j + 1] - var_off[j];
       const long long slot_bytes = ((nv + CLU - 1) / CLU) * 8;
-      if (nv * 8 > small_cap && slot_bytes <= clu_cap) big.push_back(j);
+      const long long mb = marks ? mark_bytes((int)nv) : 0;  // the round bitmaps beside the store
+      if (nv * 8 + mb > small_cap && slot_bytes <= clu_cap) big.push_back(j);
       else rest.push_back(j);
     }
     nbig = (int)big.size();
@@ -1784,13 +1934,15 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   // memory let that many stay resident; each gets an equal share of the SM's
   // shared memory.
   int per_sm = opts.ctas_per_sm > 0 ? opts.ctas_per_sm : 2;
+  void (*kinst)(InstArgs) = marks ? k_instances<true> : k_instances<false>;
+  void (*kclu)(CluArgs) = marks ? k_instances_cluster<true> : k_instances_cluster<false>;
   int smem = 0;
   for (;;) {
     smem = std::min(ctx->smem_optin, (int)((228 * 1024) / per_sm) - 2048);
     smem = (smem / 16) * 16;
-    PIR_CK(cudaFuncSetAttribute(k_instances, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    PIR_CK(cudaFuncSetAttribute(kinst, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int occ = 0;
-    PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_instances, block, smem));
+    PIR_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kinst, block, smem));
     if (occ >= per_sm || per_sm == 1) break;
     per_sm = std::max(1, occ);
   }
@@ -1825,7 +1977,8 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
     ca.next = d_next + 1;
     ca.out = b->d_iout;
     ca.max_rounds = a.max_rounds;
-    PIR_CK(cudaFuncSetAttribute(k_instances_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, clu_cap));
+    ca.smem_cap = clu_cap;
+    PIR_CK(cudaFuncSetAttribute(kclu, cudaFuncAttributeMaxDynamicSharedMemorySize, clu_cap));
     cudaLaunchConfig_t cfg{};
     const int nclusters = std::max(1, std::min(nbig, ctx->num_sms / CLU));
     cfg.gridDim = dim3(nclusters * CLU);
@@ -1839,14 +1992,14 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    PIR_CK(cudaLaunchKernelEx(&cfg, k_instances_cluster, ca));
+    PIR_CK(cudaLaunchKernelEx(&cfg, kclu, ca));
   }
   if (nbig < ninst) {
     // phase 2: the rest, one CTA per instance
     a.order = d_order + nbig;
     a.ninst = ninst - nbig;
     const int grid2 = std::max(1, std::min(ninst - nbig, ctx->num_sms * per_sm));
-    k_instances<<<grid2, block, smem, ctx->stream>>>(a);
+    kinst<<<grid2, block, smem, ctx->stream>>>(a);
   }
   PIR_CK(cudaGetLastError());
   PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -1867,7 +2020,7 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
     if (out_rounds) out_rounds[j] = hout[j].rounds;
     if (out_device_ms) out_device_ms[j] = (float)(hout[j].ns * 1e-6);
     st.rounds = std::max<int64_t>(st.rounds, hout[j].rounds);
-    st.executions += (int64_t)hout[j].rounds * (prop_off[j + 1] - prop_off[j]);
+    st.executions += marks ? (int64_t)hout[j].execs : (int64_t)hout[j].rounds * (prop_off[j + 1] - prop_off[j]);
     st.narrowed += (int64_t)hout[j].narrowed;
     if (hout[j].status == PIR_TIMEOUT) worst = PIR_TIMEOUT;
   }

@@ -23,14 +23,23 @@ def _uneven_set(seed, n=24, pmin=500, pmax=20_000, spec_every=0):
     return insts
 
 
+SCHEDS = ("ac1", "events")
+
+
+def _sched(P, name):
+    return {"ac1": P.SCHED_AC1, "events": P.SCHED_EVENTS}[name]
+
+
+@pytest.mark.parametrize("sched", SCHEDS)
 @pytest.mark.parametrize("seed", range(3))
-def test_instances_parity(seed, P, oracle):
+def test_instances_parity(seed, sched, P, oracle):
     import workloads as W
     insts = _uneven_set(seed, spec_every=7)
     prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
     glb, gub = lb.copy(), ub.copy()
     ctx = P.Context(0)
-    status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, glb, gub)
+    status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, glb, gub,
+                                                    sched=_sched(P, sched))
     nfail = 0
     for j, inst in enumerate(insts):
         s = inst.store()
@@ -46,18 +55,27 @@ def test_instances_parity(seed, P, oracle):
             nfail += 1
     assert nfail >= 3  # the spec-variant instances fail
     assert np.all(ms > 0)
-    assert st["executions"] == int(sum(rounds[j] * insts[j].nprops for j in range(len(insts))))
+    ac1_execs = int(sum(rounds[j] * insts[j].nprops for j in range(len(insts))))
+    if sched == "ac1":
+        assert st["executions"] == ac1_execs
+    else:  # round 0 runs every propagator, later rounds only those of narrowed variables
+        assert sum(i.nprops for i in insts) <= st["executions"] < ac1_execs
 
 
-def test_instances_smem_and_global_paths(P, oracle):
-    """Small instances run from shared memory, the largest from the global
-    store: both agree with the oracle."""
+@pytest.mark.parametrize("mode", ("auto", "one_cta"))
+@pytest.mark.parametrize("sched", SCHEDS)
+def test_instances_smem_and_global_paths(sched, mode, P, oracle):
+    """Small instances run from shared memory; the largest runs on a cluster
+    (auto) or, with the cluster kernel off (one CTA per instance), from the
+    global store: all agree with the oracle."""
     import workloads as W
     insts = [W.plain(200, 800, 1000, 1), W.plain(60_000, 240_000, 1000, 2, mix=W.MIX_UNEVEN),
              W.plain(3000, 12_000, 1000, 3, mix=W.MIX_UNEVEN)]
     prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
     ctx = P.Context(0)
-    status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
+    status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub,
+                                                    mode=P.MODE_SMEM if mode == "one_cta" else P.MODE_AUTO,
+                                                    sched=_sched(P, sched))
     for j, inst in enumerate(insts):
         s = inst.store()
         oracle.install(inst.op, inst.x, inst.y, inst.z, s)
@@ -67,13 +85,39 @@ def test_instances_smem_and_global_paths(P, oracle):
         np.testing.assert_array_equal(ub[var_off[j]:var_off[j + 1]], s[:, 1])
 
 
-def test_instances_round_cap(P):
+@pytest.mark.parametrize("sched", SCHEDS)
+def test_instances_round_cap(sched, P):
     import workloads as W
     insts = [W.add_chain(W.plain(2000, 8000, 1000, 4), 100, 1000, 4)]
     prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
     ctx = P.Context(0)
-    status, rounds, _, _ = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub, max_rounds=7)
+    status, rounds, _, _ = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub, max_rounds=7,
+                                                  sched=_sched(P, sched))
     assert status[0] == P.TIMEOUT and rounds[0] == 7
+
+
+def test_instances_events_fewer_executions(P, oracle):
+    """The event-filtered rounds reach the AC-1 rounds' stores and statuses
+    (a chain of 190 links forces a long tail of rounds that narrow a few
+    variables) with fewer executions; the learned schedule is refused."""
+    import workloads as W
+    insts = [W.add_chain(W.plain(4000, 16_000, 1000, 11), 190, 1000, 11),
+             W.add_chain(W.plain(40_000, 160_000, 1000, 12, mix=W.MIX_UNEVEN), 190, 1000, 12),
+             W.plain(900, 3600, 1000, 13, mix=W.MIX_UNEVEN)]
+    prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
+    ctx = P.Context(0)
+    res = {}
+    for name in SCHEDS:
+        glb, gub = lb.copy(), ub.copy()
+        status, rounds, _, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, glb, gub,
+                                                       sched=_sched(P, name))
+        assert np.all(status == P.OK)
+        res[name] = (glb, gub, st["executions"])
+    np.testing.assert_array_equal(res["ac1"][0], res["events"][0])
+    np.testing.assert_array_equal(res["ac1"][1], res["events"][1])
+    assert res["events"][2] * 5 < res["ac1"][2]
+    with pytest.raises(P.PirError):
+        ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb.copy(), ub.copy(), sched=P.SCHED_LEARNED)
 
 
 def _nodes_setup(P, nvars=5000, nprops=20_000, nnodes=200, kmax=48, seed=0):
@@ -232,7 +276,8 @@ def test_nodes_events_need_a_fixpoint_base(P, oracle):
     np.testing.assert_array_equal(olb[ok], ostore[ok, :, 0])
 
 
-def test_instances_cluster_path(P, oracle):
+@pytest.mark.parametrize("sched", SCHEDS)
+def test_instances_cluster_path(sched, P, oracle):
     """More large instances than clusters (work stealing across clusters of 8
     CTAs sharing the store through distributed shared memory) plus small ones
     in the same call: every store bit-exact."""
@@ -241,7 +286,7 @@ def test_instances_cluster_path(P, oracle):
     insts += [W.plain(400 + 10 * j, 1600 + 40 * j, 1000, 90 + j, mix=W.MIX_UNEVEN) for j in range(8)]
     prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
     ctx = P.Context(0)
-    status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub)
+    status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb, ub, sched=_sched(P, sched))
     for j, inst in enumerate(insts):
         s = inst.store()
         oracle.install(inst.op, inst.x, inst.y, inst.z, s)
@@ -249,7 +294,8 @@ def test_instances_cluster_path(P, oracle):
         assert status[j] == orc == oracle.OK, j
         np.testing.assert_array_equal(lb[var_off[j]:var_off[j + 1]], s[:, 0])
         np.testing.assert_array_equal(ub[var_off[j]:var_off[j + 1]], s[:, 1])
-    capped, r2, _, _ = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb.copy(), ub.copy(), max_rounds=1)
+    capped, r2, _, _ = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, lb.copy(), ub.copy(), max_rounds=1,
+                                              sched=_sched(P, sched))
     assert np.all(r2 <= 1)
 
 
@@ -300,3 +346,36 @@ def test_nodes_staged_graph_matches_watch(P):
     buf[:] = [0, 1, 1, 5000, 0, 0]  # off 0, 1, 1; var 5000 is out of range
     with pytest.raises(P.PirError):
         ctx.fixpoint_nodes_staged(2, 1, 0)
+
+
+def test_nodes_staged_after_instances(P):
+    """Staged node batches and uneven instances on one context: the instance
+    install growing its own pinned staging leaves the node staging and the
+    batch graph alone, so the batch after it still matches
+    pir_fixpoint_nodes_watch (and the context tears down cleanly)."""
+    import workloads as W
+    ctx, (blb, bub), off, var, lb, ub = _nodes_setup(P, nnodes=80, seed=3)
+    watch = np.arange(0, 5000, 11, dtype=np.int32)
+    nn, nt, nw = 80, int(off[-1]), len(watch)
+    ws, wl, wu, wr, _ = ctx.fixpoint_nodes_watch(off, var, lb, ub, watch)
+
+    def staged():
+        buf = ctx.nodes_stage(nn, nt, nw)
+        buf[:nw] = watch
+        buf[nw:nw + nn + 1] = off
+        buf[nw + nn + 1:nw + nn + 1 + nt] = var
+        buf[nw + nn + 1 + nt:nw + nn + 1 + 2 * nt] = lb
+        buf[nw + nn + 1 + 2 * nt:] = ub
+        ss, sl_, su, sr, st = ctx.fixpoint_nodes_staged(nn, nt, nw)
+        np.testing.assert_array_equal(ss, ws)
+        np.testing.assert_array_equal(sr, wr)
+        np.testing.assert_array_equal(sl_, wl)
+        np.testing.assert_array_equal(su, wu)
+
+    staged()
+    for n in (4, 12):  # the second set grows the instance staging again
+        prop_off, var_off, op, x, y, z, ilb, iub = W.pack(_uneven_set(5, n=n))
+        status, _, _, _ = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, ilb, iub)
+        assert np.all(status == P.OK)
+        staged()
+    ctx.close()

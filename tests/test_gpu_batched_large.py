@@ -8,7 +8,7 @@ tests/pir_test.cpp:60-62):
   launch of the event node kernel (with its certifying sweeps) and of the
   AC-1 node kernel;
 * 512 uneven instances, propagators log-uniform in [1e3, 2e5], 5% tdiv and
-  5% tmod, in one launch.
+  5% tmod, in one launch, under AC-1 and under the event-filtered rounds.
 """
 import numpy as np
 import pytest
@@ -83,14 +83,17 @@ def test_nodes_4096_statuses_without_stores(nodes_setup, oracle):
     assert st1["certify_narrowed"] == 0
 
 
-def test_uneven_512_bit_exact(oracle):
+@pytest.mark.parametrize("sched", ("ac1", "events"))
+def test_uneven_512_bit_exact(sched, oracle):
     import pirgpu
     import workloads as W
     insts = W.uneven(512, 1000, 200_000, 0)
     prop_off, var_off, op, x, y, z, lb, ub = W.pack(insts)
     glb, gub = lb.copy(), ub.copy()
     ctx = pirgpu.Context(0)
-    status, rounds, ms, st = ctx.fixpoint_instances(prop_off, var_off, op, x, y, z, glb, gub)
+    status, rounds, ms, st = ctx.fixpoint_instances(
+        prop_off, var_off, op, x, y, z, glb, gub,
+        sched={"ac1": pirgpu.SCHED_AC1, "events": pirgpu.SCHED_EVENTS}[sched])
     s = np.ascontiguousarray(np.stack([lb, ub], 1))
     ost, _ = oracle.fixpoint_instances(prop_off, var_off, op, x, y, z, s)
     np.testing.assert_array_equal(status, ost)
