@@ -325,9 +325,12 @@ def out_of_l2_record(cr, hbm):
         "value": best["executions"] / (best["device_ms"] / 1e3), "unit": "executions/s",
         "time_to_fixpoint_ms": best["device_ms"], "rounds": best["rounds"], "executions": best["executions"],
         "kernel_variant": list(tuned),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+        "roofline": {"bound": "l2", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "dram_bytes_per_round": prof.get("dram_bytes_per_round"),
                      "dram_gbs_ncu": prof.get("dram_gbs"),
+                     "note": "the 256 MB bytecode streams from HBM every round (dram_bytes_per_round); the "
+                             "interval gathers hit the L2-resident 32 MB store, and the round is bound by the "
+                             "L1/L2 gather path and issue (profiles/persistent_fixpoint_out_of_l2.md)",
                      "bytes_model": "40 B per execution + 4 B per narrowing join"},
         "events_schedule": {"time_to_fixpoint_ms": ev["device_ms"], "executions": ev["executions"],
                             "rounds": ev["rounds"], "certify_narrowed": ev["certify_narrowed"],
@@ -460,7 +463,9 @@ def run_ours(args):
     inst, desc = make_workload(args.workload)
     ctx = pirgpu.Context(local)
     ctx.load_store(inst.lb, inst.ub)
-    ctx.tell(inst.op, inst.x, inst.y, inst.z)
+    t0 = time.perf_counter()
+    ctx.tell(inst.op, inst.x, inst.y, inst.z)  # install: the (op, y, x, z) sort, on the device from 65,536 on
+    tell_s = time.perf_counter() - t0
     snap = ctx.snapshot()
     nprops = ctx.num_deductions()
     init_lb, init_ub = ctx.read_store()  # store after install (reified targets met with [0,1])
@@ -531,16 +536,21 @@ def run_ours(args):
     ev = None
     if args.mode in (0, 1) and args.max_rounds == 0 and not args.no_events:
         ev_runs = []
+        first_wall = None
         for _ in range(3):
             ctx.restore(snap)
             cr.flush_l2()
+            t0 = time.perf_counter()
             rc, st = ctx.fixpoint(sched=pirgpu.SCHED_EVENTS)
+            if first_wall is None:  # includes building the adjacency and the path segments
+                first_wall = time.perf_counter() - t0
             if rc != pirgpu.OK:
                 raise RuntimeError("event fixpoint status %s" % pirgpu.STATUS[rc])
             ev_runs.append(st)
         ev_store = ctx.read_store()
         st = sorted(ev_runs, key=lambda s: s["device_ms"])[1]  # median of 3
-        ev = {"time_to_fixpoint_ms": st["device_ms"], "executions": st["executions"], "rounds": st["rounds"],
+        ev = {"time_to_fixpoint_ms": st["device_ms"], "first_call_wall_ms": first_wall * 1e3,
+              "executions": st["executions"], "rounds": st["rounds"],
               "certify_executions": st["certify_executions"], "certify_narrowed": st["certify_narrowed"],
               "ac1_over_events_time": (dev_ms / args.steps) / st["device_ms"],
               "ac1_over_events_executions": (execs / args.steps) / max(st["executions"], 1),
@@ -602,6 +612,7 @@ def run_ours(args):
         "gpu_launches": args.steps * (1 if args.mode in (0, 1, 3) else rounds[0] * 2),
         "clocks": clocks,
         "time_to_fixpoint_ms": dev_ms / args.steps,
+        "tell_ms": tell_s * 1e3,
         "events_schedule": ev,
         "cpu_time_to_fixpoint": cpu_fix,
         "wall_s": wall,
@@ -774,23 +785,34 @@ def run_learned(args):
     t_train = time.perf_counter() - t0
     snap = ctx.snapshot()
 
-    def run(sched, frac=0.0):
-        ex, dev, outs = 0, 0.0, []
+    def run(sched, frac=0.0, **kw):
+        ex, cex, dev, rounds, outs = 0, 0, 0.0, 0, []
         for j in range(ntrain, ntrain + ntest):
             ctx.restore(snap)
             ctx.embed_many(var[off[j]:off[j + 1]], lb[off[j]:off[j + 1]], ub[off[j]:off[j + 1]])
-            rc, st = ctx.fixpoint(mode=1, sched=sched, wake_fraction=frac)
+            rc, st = ctx.fixpoint(mode=1, sched=sched, wake_fraction=frac, **kw)
             ex += st["executions"]
+            cex += st["certify_executions"]
             dev += st["device_ms"]
+            rounds += st["rounds"]
             outs.append((rc, ctx.read_store()))
-        return ex, dev, outs
+        return {"executions": ex, "certify_executions": cex, "device_ms": dev, "rounds": rounds}, outs
+
+    def same_as(o0, o1):
+        return sum(1 for (a, (l0, u0)), (b, (l1, u1)) in zip(o0, o1)
+                   if a == b and (a != pirgpu.OK or (np.array_equal(l0, l1) and np.array_equal(u0, u1))))
 
     run(pirgpu.SCHED_AC1)  # warm-up
-    e0, d0, o0 = run(pirgpu.SCHED_AC1)
-    e1, d1, o1 = run(pirgpu.SCHED_LEARNED, args.wake_fraction)
-    same = sum(1 for (a, (l0, u0)), (b, (l1, u1)) in zip(o0, o1)
-               if a == b and (a != pirgpu.OK or (np.array_equal(l0, l1) and np.array_equal(u0, u1))))
+    ac1, o0 = run(pirgpu.SCHED_AC1)
+    ev, oe = run(pirgpu.SCHED_EVENTS)
+    lrn, o1 = run(pirgpu.SCHED_LEARNED, args.wake_fraction)
+    quarter, oq = run(pirgpu.SCHED_LEARNED, 0.25)
+    allw, oa = run(pirgpu.SCHED_LEARNED, 1.0)
+    grid, og = run(pirgpu.SCHED_LEARNED, args.wake_fraction, local_frontier=-1)
+    for r, o in ((ev, oe), (lrn, o1), (quarter, oq), (allw, oa), (grid, og)):
+        r["bit_exact_nodes"] = same_as(o0, o)
     ctx.restore(snap)
+    e0, e1, d0, d1 = ac1["executions"], lrn["executions"], ac1["device_ms"], lrn["device_ms"]
     out = {
         "metric": "propagator executions to fixpoint (learned vs AC-1)", "value": e0 / max(e1, 1),
         "unit": "x fewer executions", "n_gpus": 1, "steps": ntest, "warmup": ntest,
@@ -800,10 +822,17 @@ def run_learned(args):
         "config": {"workload": "learned: 100,000 vars / 400,000 propagators, trained on %d nodes, tested on %d held-out nodes" % (ntrain, ntest),
                    "samples": ns, "positives": npos, "collect_s": t_collect, "train_s": t_train,
                    "epochs": args.epochs, "loss": [float(v) for v in loss], "wake_fraction": args.wake_fraction},
-        "ac1": {"executions": e0, "device_ms": d0},
-        "learned": {"executions": e1, "device_ms": d1},
+        "ac1": ac1,
+        "events": ev,
+        "learned": lrn,
+        "learned_wake_quarter": dict(quarter, note="the frontier rounds waking at least a quarter of the frontier"),
+        "learned_all_woken": dict(allw, note="the same frontier rounds with every entry woken: what the network "
+                                             "adds over the frontier alone"),
+        "learned_grid": dict(grid, note="the grid kernel: every propagator scored every round"),
         "wall_ratio_ac1_over_learned": d0 / max(d1, 1e-9),
-        "bit_exact_nodes": same, "nodes": ntest,
+        "wall_ratio_events_over_learned": ev["device_ms"] / max(d1, 1e-9),
+        "executions_all_woken_over_learned": allw["executions"] / max(e1, 1),
+        "bit_exact_nodes": lrn["bit_exact_nodes"], "nodes": ntest,
         "gpu_launches": ntest,  # one learned fixpoint launch per held-out node (the timed device time)
     }
     print(json.dumps(out), flush=True)

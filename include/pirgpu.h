@@ -64,7 +64,9 @@ enum pir_sched {
                              propagators of narrowed variables with at most 4 propagators run at
                              once by the narrowing thread (opts.chase);
                              pir_fixpoint_nodes: one CTA per node, when the base store is at its
-                             fixpoint (else AC-1 rounds) */
+                             fixpoint (else AC-1 rounds); pir_fixpoint_instances: per instance, a
+                             round runs the propagators with a variable narrowed in the previous
+                             round (per-round bitmaps of the narrowed variables beside the store) */
 };
 
 /* Number of persistent-kernel variants (propagators per thread and step x CTAs
@@ -99,7 +101,12 @@ typedef struct pir_opts {
                                  the propagators of the variables it narrowed number at least 1/dense of all
                                  (0: 1/32) and those variables keep getting fewer; < 0: dense only for the first
                                  round and the certifying sweep */
-  int32_t reserved[1];
+  int32_t lead;               /* pir_fixpoint's event schedule: AC-1 rounds of the persistent kernel run first, until
+                                 a round whose narrowed bounds have not shrunk by an eighth against the round lead
+                                 rounds before (0: 16; at most 64): a steady trickle, such as a long chain, goes to
+                                 the event kernel, which continues from that store (a lead that reaches the
+                                 fixpoint ends the run: its last round narrowed nothing); < 0, or
+                                 opts.max_rounds > 0: the event kernel from the start */
 } pir_opts;
 
 typedef struct pir_stats {
@@ -304,7 +311,11 @@ int pir_search(pirgpu_ctx *ctx, int32_t ndec, const int32_t *dec, const pir_sear
  * instance) and variables var_off[j] .. var_off[j+1]-1 of lb/ub, which are
  * updated in place.  Each instance is installed: its propagators are grouped by
  * opcode (stable, the GPU order of pir.hpp:339-341) and its reified targets
- * met with [0, 1] on the device (pir.hpp:333-335).
+ * met with [0, 1] on the device (pir.hpp:333-335).  opts->sched is
+ * PIR_SCHED_AC1 (every propagator every round) or PIR_SCHED_EVENTS (after the
+ * first round, only the propagators of variables the previous round
+ * narrowed; the same fixpoint, fewer executions); PIR_SCHED_LEARNED is
+ * rejected with PIR_EINVAL.
  * out_status[j] a pir_status, out_rounds[j] (may be NULL) its rounds,
  * out_device_ms[j] (may be NULL) the device time of that instance's own
  * fixpoint (from the moment a CTA takes it up). */
@@ -338,11 +349,20 @@ int pir_fixpoint_static(const int32_t *d_op, const int32_t *d_x, const int32_t *
 
 /* Learned propagator scheduler (used by pir_fixpoint with opts.sched =
  * PIR_SCHED_LEARNED; no counterpart in the reference, whose fixpoint loop is
- * the caller's).  An 8 -> 32 -> 32 -> 1 MLP with BF16 weights scores every
- * propagator each round (on the tensor cores); each CTA runs the top
- * opts.wake_fraction of the propagators it scored; a round of
- * woken propagators without change is followed by a full certifying sweep,
- * so the fixpoint is the plain one bit for bit.
+ * the caller's).  An 8 -> 32 -> 32 -> 1 MLP with BF16 weights scores
+ * propagators on the tensor cores.  When the store was a fixpoint before the
+ * last embeddings (a fixpoint returned PIR_OK, or a snapshot taken at one was
+ * restored, and only pir_embed / pir_embed_many changed it since), one CTA
+ * runs rounds on the frontier of the embedded variables: each round scores
+ * its frontier, runs the entries with a logit >= 0 and at least the top
+ * opts.wake_fraction of them, and defers the rest; an empty frontier is
+ * followed by a certifying round over every propagator of every variable the
+ * run embedded or narrowed.  Otherwise (or with opts.local_frontier < 0, or
+ * when the frontier outgrows 65,536 entries) every propagator is scored each
+ * round on the whole grid, each CTA runs the top opts.wake_fraction of the
+ * propagators it scored, and a round of woken propagators without change is
+ * followed by a full certifying sweep.  Either way the fixpoint is the plain
+ * one bit for bit.
  *
  * pir_sched_collect: change traces of the plain AC-1 fixpoint, node by node
  * (each node = the context's store + its tightenings, as pir_fixpoint_nodes);

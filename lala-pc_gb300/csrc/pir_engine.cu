@@ -21,19 +21,60 @@ using namespace pirgpu;
 // threads per SM bound the register budget; PIPE selects the software-pipelined
 // sweep (next step's gathers in flight while this step computes).  Thread 0 of
 // CTA 0 writes the round count.
-template <int PPI, int MINB, bool PIPE = false>
+// LEAD (the event schedule's lead; the ten AC-1 variants are built without
+// it): stop, as if the round cap were reached, after a round whose narrowed
+// bounds have not shrunk by an eighth against the round `handover` rounds
+// before -- a steady trickle, such as a long chain whose links each narrow a
+// little round after round, where a dense phase keeps shrinking -- and the
+// event schedule goes on from that store.  Each CTA adds its narrowings to
+// the round's counter before it arrives at the grid barrier and reads the
+// total after it, so every CTA takes the same decision in the same round.
+constexpr unsigned BIT_HANDOVER = 1u << 28;
+constexpr int HANDOVER_WINDOW = 64;  // the longest window
+
+// Thread 0 of each CTA, around the grid barrier of `round`: adds the CTA's
+// narrowings to the round's counter, passes the barrier, reads the total and
+// returns the barrier word, with BIT_HANDOVER when the trickle rule holds.
+// Out of line: the sweep loop keeps its registers.
+static __device__ __noinline__ unsigned barrier_handover(Control *ctl, long long round, int changed, int failed,
+                                                         long long timeout_ns, unsigned long long mine,
+                                                         unsigned window, unsigned long long *hist) {
+  const int slot3 = (int)(round % 3);
+  // before the arrival (a release): the total is complete once all CTAs arrived
+  if (mine) atomicAdd(&ctl->joins[slot3], mine);
+  unsigned w = grid_sync_rot(ctl, gridDim.x, round, changed, failed, timeout_ns);
+  if ((w & BIT_CHANGED) && !(w & (BIT_FAILED | BIT_ERROR))) {
+    const unsigned long long joins = *(volatile unsigned long long *)&ctl->joins[slot3];
+    // round + 2's counter was last read after barrier round - 1, which every CTA has left
+    if (blockIdx.x == 0) ctl->joins[(round + 2) % 3] = 0ull;
+    const int slot = (int)(round % window);
+    const bool flat = round >= window && 8ull * joins > 7ull * hist[slot];
+    hist[slot] = joins;
+    if (flat) w |= BIT_HANDOVER;
+  }
+  return w;
+}
+
+template <int PPI, int MINB, bool PIPE = false, bool LEAD = false>
 __global__ void __launch_bounds__(256, MINB) k_fixpoint_persistent(Bytecode bc, int2 *store, Control *ctl,
-                                                                   long long max_rounds, long long timeout_ns) {
+                                                                   long long max_rounds, long long timeout_ns,
+                                                                   unsigned handover) {
   // per round parity: the CTA's OR of changed (bit 0) / failed (bit 1), and the
   // barrier's decision word; two block barriers per round
   __shared__ unsigned s_bits[2], s_word[2];
+  // LEAD: this CTA's narrowings of the round, the grid's of the last rounds
+  __shared__ unsigned s_joins[LEAD ? 2 : 1];
+  __shared__ unsigned long long s_hist[LEAD ? HANDOVER_WINDOW : 1];
   RedStore st{store};
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gstride = gridDim.x * blockDim.x;
   const int nsteps = steps_of<PPI>(bc);
   unsigned long long narrowed = 0;
   long long round = 0;
-  if (threadIdx.x == 0) s_bits[0] = s_bits[1] = 0u;
+  if (threadIdx.x == 0) {
+    s_bits[0] = s_bits[1] = 0u;
+    if constexpr (LEAD) s_joins[0] = s_joins[1] = 0u;
+  }
   __syncthreads();
   for (;;) {
     const int p = (int)(round & 1);
@@ -45,16 +86,27 @@ __global__ void __launch_bounds__(256, MINB) k_fixpoint_persistent(Bytecode bc, 
     narrowed += changed;
     const unsigned bits = __reduce_or_sync(0xFFFFFFFFu, (changed ? 1u : 0u) | (failed ? 2u : 0u));
     if ((threadIdx.x & 31) == 0 && bits) atomicOr(&s_bits[p], bits);
+    if constexpr (LEAD) {
+      const unsigned wsum = __reduce_add_sync(0xFFFFFFFFu, (unsigned)changed);
+      if ((threadIdx.x & 31) == 0 && wsum) atomicAdd(&s_joins[p], wsum);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       const unsigned b = s_bits[p];
       s_bits[p ^ 1] = 0u;
-      s_word[p] = grid_sync_rot(ctl, gridDim.x, round, b & 1u, b & 2u, timeout_ns);
+      if constexpr (LEAD) {
+        const unsigned long long mine = s_joins[p];
+        s_joins[p ^ 1] = 0u;
+        s_word[p] = barrier_handover(ctl, round, b & 1u, b & 2u, timeout_ns, mine, handover, s_hist);
+      } else {
+        s_word[p] = grid_sync_rot(ctl, gridDim.x, round, b & 1u, b & 2u, timeout_ns);
+      }
     }
     __syncthreads();
     const unsigned w = s_word[p];
     ++round;
-    if ((w & BIT_ERROR) || (w & BIT_FAILED) || !(w & BIT_CHANGED) || (max_rounds > 0 && round >= max_rounds)) {
+    if ((w & BIT_ERROR) || (w & BIT_FAILED) || !(w & BIT_CHANGED) || (max_rounds > 0 && round >= max_rounds) ||
+        (LEAD && (w & BIT_HANDOVER))) {
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         ctl->rounds = round;
         if (w & BIT_FAILED) ctl->failed = 1;
@@ -81,6 +133,8 @@ static const PersistentVariant kPersistent[] = {
     {1, 3, (const void *)k_fixpoint_persistent<1, 3, true>}, {2, 2, (const void *)k_fixpoint_persistent<2, 2, true>},
 };
 static const int kNumPersistent = sizeof(kPersistent) / sizeof(kPersistent[0]);
+// The event schedule's AC-1 lead: the pipelined one-propagator variant with the handover rule.
+static const PersistentVariant kLead = {1, 3, (const void *)k_fixpoint_persistent<1, 3, true, true>};
 static_assert(sizeof(kPersistent) / sizeof(kPersistent[0]) == PIR_PERSISTENT_VARIANTS, "variant count");
 
 // One AC-1 round per launch (host-driven loop).  Change flag per round parity.
@@ -343,6 +397,53 @@ int apply_meets(pirgpu_ctx *ctx, const std::vector<int> &var, const std::vector<
   return PIR_OK;
 }
 
+// The persistent AC-1 kernel on the context's store (the autotuned variant
+// unless opts.variant names one); window > 0: the lead variant, which stops
+// after a round whose narrowings have not shrunk by an eighth against the
+// round `window` rounds before.
+static int launch_persistent(pirgpu_ctx *ctx, const pir_opts &opts, long long max_rounds, long long timeout,
+                             int window) {
+  const int block = 256;
+  Bytecode bc = bytecode_view(ctx);
+  int vi = opts.variant > 0 ? opts.variant - 1 : (ctx->tuned_variant >= 0 ? ctx->tuned_variant : 0);
+  if (vi < 0 || vi >= kNumPersistent) return set_err(ctx, PIR_EINVAL, "unknown kernel variant %d", opts.variant);
+  const PersistentVariant &pv = window > 0 ? kLead : kPersistent[vi];
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pv.fn, block, 0));
+  if (occ < 1) return set_err(ctx, PIR_ECUDA, "persistent kernel does not fit on an SM");
+  int per_sm = opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ;
+  int grid = ctx->num_sms * per_sm;
+  const int nsteps = bc.nchunks * (4 / pv.ppi);
+  grid = std::max(1, std::min(grid, (nsteps + block - 1) / block));
+  unsigned handover = window > 0 ? (unsigned)std::min(window, HANDOVER_WINDOW) : 0u;
+  void *args[] = {&bc, &ctx->d_store, &ctx->d_ctl, (void *)&max_rounds, (void *)&timeout, (void *)&handover};
+  CK(cudaLaunchCooperativeKernel(pv.fn, dim3(grid), dim3(block), args, 0, ctx->stream));
+  ctx->last_grid = grid;
+  if (window <= 0) ctx->last_variant = vi;
+  return PIR_OK;
+}
+
+int ac1_lead(pirgpu_ctx *ctx, const pir_opts &opts, int window, pir_stats *st, bool *done) {
+  int r;
+  const long long timeout = opts.barrier_timeout_ns > 0 ? opts.barrier_timeout_ns : 2000000000ll;
+  if ((r = reset_control(ctx))) return r;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  if ((r = launch_persistent(ctx, opts, 0, timeout, window))) return r;
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  Control h;
+  if ((r = read_control(ctx, &h))) return r;
+  std::memset(st, 0, sizeof(*st));
+  CK(cudaEventElapsedTime(&st->device_ms, ctx->ev0, ctx->ev1));
+  st->rounds = h.rounds;
+  st->executions = h.rounds * ctx->n;
+  st->narrowed = (int64_t)h.narrowed;
+  st->status = h.status ? h.status : (h.failed ? PIR_FAILED : (h.changed[0] ? PIR_TIMEOUT : PIR_OK));
+  // the lead's last round narrowed nothing: every propagator ran on the final store
+  if (st->status == PIR_OK) st->certify_executions = ctx->n;
+  *done = st->status != PIR_TIMEOUT;
+  return PIR_OK;
+}
+
 }  // namespace pirgpu
 
 // =============================================================== C ABI ======
@@ -558,7 +659,15 @@ int pir_get_bytecode(pirgpu_ctx *ctx, int32_t *op, int32_t *x, int32_t *y, int32
   return PIR_OK;
 }
 
+static int fixpoint_any(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats);
+
 int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
+  const int rc = fixpoint_any(ctx, opts_in, stats);
+  if (rc == PIR_OK && ctx && !ctx->failed) note_fixpoint(ctx);
+  return rc;
+}
+
+static int fixpoint_any(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
   if (!ctx) return PIR_EINVAL;
   pir_opts opts;
   std::memset(&opts, 0, sizeof(opts));
@@ -610,21 +719,7 @@ int pir_fixpoint(pirgpu_ctx *ctx, const pir_opts *opts_in, pir_stats *stats) {
     }
     CK(cudaGetLastError());
   } else if (mode == PIR_MODE_PERSISTENT) {
-    const int block = 256;
-    int vi = opts.variant > 0 ? opts.variant - 1 : (ctx->tuned_variant >= 0 ? ctx->tuned_variant : 0);
-    if (vi < 0 || vi >= kNumPersistent) return set_err(ctx, PIR_EINVAL, "unknown kernel variant %d", opts.variant);
-    const PersistentVariant &pv = kPersistent[vi];
-    int occ = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pv.fn, block, 0));
-    if (occ < 1) return set_err(ctx, PIR_ECUDA, "persistent kernel does not fit on an SM");
-    int per_sm = opts.ctas_per_sm > 0 ? std::min(opts.ctas_per_sm, occ) : occ;
-    int grid = ctx->num_sms * per_sm;
-    const int nsteps = bc.nchunks * (4 / pv.ppi);
-    grid = std::max(1, std::min(grid, (nsteps + block - 1) / block));
-    void *args[] = {&bc, &ctx->d_store, &ctx->d_ctl, (void *)&max_rounds, (void *)&timeout};
-    CK(cudaLaunchCooperativeKernel(pv.fn, dim3(grid), dim3(block), args, 0, ctx->stream));
-    ctx->last_grid = grid;
-    ctx->last_variant = vi;
+    if ((r = launch_persistent(ctx, opts, max_rounds, timeout, 0))) return r;
   } else if (mode == PIR_MODE_HOSTLOOP) {
     const int block = opts.block > 0 ? opts.block : 256;
     const int grid = std::max(1, std::min(ctx->num_sms * 8, (bc.nchunks + block - 1) / block));
@@ -888,6 +983,7 @@ int pir_restore(pirgpu_ctx *ctx, const pirgpu_snapshot *snap) {
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->failed = snap->failed;
   ctx->at_fixpoint = snap->at_fixpoint && snap->n == ctx->n;
+  if (ctx->at_fixpoint && !ctx->failed) note_fixpoint(ctx);
   return PIR_OK;
 }
 

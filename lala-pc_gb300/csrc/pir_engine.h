@@ -104,9 +104,18 @@ int device_events_graph(pirgpu_ctx *ctx, int4 *bc, int *adj_ptr, int *adj);
 
 int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);
 int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats);
+// AC-1 rounds of the persistent kernel on the context's store until a round
+// whose narrowings have not shrunk by an eighth against the round `window`
+// rounds before (at most 64); *done: the run ended (fixpoint, failure or
+// error: st->status), else the store is handed on.
+int ac1_lead(pirgpu_ctx *ctx, const pir_opts &opts, int window, pir_stats *st, bool *done);
 // Records variables embedded since the last learned fixpoint (its "just
 // changed" feature).
 void note_embedded(pirgpu_ctx *ctx, const int32_t *var, int count);
+// Records that the store is a fixpoint of the current bytecode (a fixpoint
+// returned PIR_OK, or a snapshot taken at one was restored): the learned
+// schedule then starts from the variables embedded after it.
+void note_fixpoint(pirgpu_ctx *ctx);
 
 }  // namespace pirgpu
 

@@ -357,6 +357,28 @@ struct SegStore {
   }
 };
 
+// The sweeps' store for a propagator over three distinct slots: the lane
+// owns the workspace and each slot is joined at most once per run, so the
+// interval read at the start of the run is still the current one when its
+// join comes (no reload), and the slots' propagator masks are read with the
+// intervals instead of after a narrowing.
+struct SegStore3 {
+  int2 *iv;
+  int sx, sy;
+  unsigned long long mx, my, mz;  // umask of slots sx, sy, sz
+  unsigned long long dirty;
+  __device__ __forceinline__ int embed(int i, Itv seen, Itv r, int &failed) {
+    const int nl = max(seen.l, r.l), nu = min(seen.u, r.u);
+    const int c = (nl != seen.l) + (nu != seen.u);
+    if (c) {
+      iv[i] = make_int2(nl, nu);
+      dirty |= i == sx ? mx : (i == sy ? my : mz);
+      if (is_bot(mk(nl, nu))) failed = 1;
+    }
+    return c;
+  }
+};
+
 // One propagator of the segment.  ADD, MIN, MAX and the reified EQ / LEQ
 // are idempotent (a second run on what the first left narrows nothing;
 // checked exhaustively against the oracle), so such a propagator over three
@@ -367,9 +389,56 @@ __device__ __forceinline__ void seg_run_one(const SegWork &w, SegStore &st, int 
   const int op = (int)(c & 0xFFu), sx = (int)((c >> 8) & 0xFFu), sy = (int)((c >> 16) & 0xFFu), sz = (int)(c >> 24);
   const unsigned long long bit = 1ull << k;
   st.dirty &= ~bit;
+  if (sx != sy && sx != sz && sy != sz) {
+    const int2 a = st.iv[sx], b = st.iv[sy], d = st.iv[sz];
+    SegStore3 s3{st.iv, sx, sy, st.umask[sx], st.umask[sy], st.umask[sz], 0ull};
+    deduce_loaded(op, sx, sy, sz, mk(a.x, a.y), mk(b.x, b.y), mk(d.x, d.y), s3, failed);
+    const bool idem = op == OP_ADD || op == OP_MIN || op == OP_MAX || op == OP_EQ || op == OP_LEQ;
+    st.dirty |= idem ? (s3.dirty & ~bit) : s3.dirty;
+    return;
+  }
   deduce(op, sx, sy, sz, st, failed);
-  const bool idem = op == OP_ADD || op == OP_MIN || op == OP_MAX || op == OP_EQ || op == OP_LEQ;
-  if (idem && sx != sy && sx != sz && sy != sz) st.dirty &= ~bit;
+}
+
+// seg_run_one for a segment whose propagators are all ADD over three distinct
+// slots (the links of a chain x_{i+1} = x_i + c_i): the same arithmetic,
+// with the opcode known, so none of the other opcodes' code is on the lane's
+// path.
+__device__ __forceinline__ void seg_run_add(const SegWork &w, SegStore &st, int k, int &failed) {
+  const unsigned c = (unsigned)w.code[k];
+  const int sx = (int)((c >> 8) & 0xFFu), sy = (int)((c >> 16) & 0xFFu), sz = (int)(c >> 24);
+  const unsigned long long bit = 1ull << k;
+  const int2 a = st.iv[sx], b = st.iv[sy], d = st.iv[sz];
+  SegStore3 s3{st.iv, sx, sy, st.umask[sx], st.umask[sy], st.umask[sz], 0ull};
+  deduce_loaded(OP_ADD, sx, sy, sz, mk(a.x, a.y), mk(b.x, b.y), mk(d.x, d.y), s3, failed);
+  st.dirty = (st.dirty | s3.dirty) & ~bit;  // ADD is idempotent: not marked again by its own narrowings
+}
+
+// The lane's sweeps of a segment: each pass runs the marked propagators
+// forward, then backward; a mark set during a pass ahead of the current
+// position is run in that pass.  Returns the runs.
+template <bool ALL_ADD>
+__device__ __forceinline__ unsigned long long seg_sweep(const SegWork &w, SegStore &st, int &fl) {
+  unsigned long long ex = 0;
+  for (int pass = 0; st.dirty && !fl && pass < SEG_PASSES; ++pass) {
+    for (int k = -1;;) {
+      const unsigned long long ahead = k >= 63 ? 0ull : st.dirty & (~0ull << (k + 1));
+      if (!ahead || fl) break;
+      k = __ffsll((long long)ahead) - 1;
+      if (ALL_ADD) seg_run_add(w, st, k, fl);
+      else seg_run_one(w, st, k, fl);
+      ++ex;
+    }
+    for (int k = 64;;) {
+      const unsigned long long behind = k >= 64 ? st.dirty : st.dirty & ((1ull << k) - 1ull);
+      if (!behind || fl) break;
+      k = 63 - __clzll((long long)behind);
+      if (ALL_ADD) seg_run_add(w, st, k, fl);
+      else seg_run_one(w, st, k, fl);
+      ++ex;
+    }
+  }
+  return ex;
 }
 
 // Runs segment s on the calling warp (all 32 lanes): stage, sweep, join, and
@@ -407,7 +476,14 @@ __device__ int run_segment(const EvFixArgs &a, const Sched &sc, int s, SegWork &
       if (l.x != t.x || l.y != t.y) start |= um;
     }
   }
-  for (int k = lane; k < np; k += 32) w.code[k] = __ldg(a.seg_code + p0 + k);
+  bool add_only = true;  // every propagator ADD over three distinct slots
+  for (int k = lane; k < np; k += 32) {
+    const int c = __ldg(a.seg_code + p0 + k);
+    w.code[k] = c;
+    const int sx = (c >> 8) & 0xFF, sy = (c >> 16) & 0xFF, sz = (int)((unsigned)c >> 24);
+    add_only = add_only && (c & 0xFF) == OP_ADD && sx != sy && sx != sz && sy != sz;
+  }
+  add_only = __all_sync(0xFFFFFFFFu, add_only);
   if (snap) {
     const unsigned lo = __reduce_or_sync(0xFFFFFFFFu, (unsigned)start);
     const unsigned hi = __reduce_or_sync(0xFFFFFFFFu, (unsigned)(start >> 32));
@@ -419,19 +495,7 @@ __device__ int run_segment(const EvFixArgs &a, const Sched &sc, int s, SegWork &
   int fl = 0, conv = 1;
   if (lane == 0) {
     SegStore st{w.iv, w.umask, start};
-    unsigned long long ex = 0;
-    for (int pass = 0; st.dirty && !fl && pass < SEG_PASSES; ++pass) {
-      for (int k = 0; k < np && !fl; ++k)
-        if ((st.dirty >> k) & 1ull) {
-          seg_run_one(w, st, k, fl);
-          ++ex;
-        }
-      for (int k = np - 1; k >= 0 && !fl; --k)
-        if ((st.dirty >> k) & 1ull) {
-          seg_run_one(w, st, k, fl);
-          ++ex;
-        }
-    }
+    const unsigned long long ex = add_only ? seg_sweep<true>(w, st, fl) : seg_sweep<false>(w, st, fl);
     conv = st.dirty == 0ull;
     execs += ex;
   }
@@ -914,6 +978,7 @@ __global__ void __launch_bounds__(EV_BLOCK, 2) k_fixpoint_events(EvFixArgs a) {
       const long long degs = (long long)ld_relaxed(a.dsum + (round % 3) * CNT_STRIDE);
       const unsigned again = ld_relaxed(a.dflag + (round % 3) * CNT_STRIDE);
       ++round;
+      const bool was_certifying = certifying;
       certifying = false;
       if (w & BIT_ERROR) {
         state = EV_ERROR;
@@ -924,7 +989,9 @@ __global__ void __launch_bounds__(EV_BLOCK, 2) k_fixpoint_events(EvFixArgs a) {
         break;
       }
       if (!(w & BIT_CHANGED)) {
-        state = EV_FIXPOINT;  // every unit ran and nothing narrowed
+        // every unit ran and nothing narrowed: this round certified the fixpoint
+        if (!was_certifying) cert_execs += execs - execs0;
+        state = EV_FIXPOINT;
         break;
       }
       if (a.max_rounds > 0 && round >= a.max_rounds) {
@@ -1068,6 +1135,23 @@ int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   std::memset(&st, 0, sizeof(st));
   EventsGraph g;
   int r;
+  // AC-1 rounds of the persistent kernel first, while a round still narrows
+  // something in many of its CTAs: a dense round of this kernel (every unit,
+  // noting the narrowed variables) costs several AC-1 rounds on an instance
+  // that narrows everywhere
+  pir_stats lead;
+  std::memset(&lead, 0, sizeof(lead));
+  if (opts.lead >= 0 && opts.max_rounds <= 0) {
+    bool done = false;
+    if ((r = ac1_lead(ctx, opts, opts.lead > 0 ? opts.lead : 16, &lead, &done))) return r;
+    if (done) {
+      if (lead.status == PIR_FAILED) ctx->failed = true;
+      ctx->at_fixpoint = lead.status == PIR_OK;
+      if (stats) *stats = lead;
+      if (lead.status == PIR_BARRIER_TIMEOUT) set_err(ctx, lead.status, "grid barrier wait exceeded");
+      return lead.status;
+    }
+  }
   if ((r = events_graph(ctx, &g, opts.segments >= 0))) return r;
   const size_t n = (size_t)ctx->n, nv = (size_t)ctx->nvars, ns = (size_t)g.nseg;
   // scratch: pstamp | sstamp | busy | valid | vstamp | cstamp | counters
@@ -1134,9 +1218,10 @@ int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   Control h;
   if ((r = read_control(ctx, &h))) return r;
   PIR_CK(cudaEventElapsedTime(&st.device_ms, ctx->ev0, ctx->ev1));
-  st.rounds = h.rounds;
-  st.executions = (int64_t)h.executions;
-  st.narrowed = (int64_t)h.narrowed;
+  st.device_ms += lead.device_ms;
+  st.rounds = h.rounds + lead.rounds;
+  st.executions = (int64_t)h.executions + lead.executions;
+  st.narrowed = (int64_t)h.narrowed + lead.narrowed;
   st.certify_executions = (int64_t)h.cert_execs;
   st.certify_narrowed = (int64_t)h.cert_narrowed;
   int status;

@@ -31,7 +31,10 @@ struct Control {
   int pad_i;
   // certifying sweeps: their executions and the bounds they narrowed
   unsigned long long cert_execs, cert_narrowed;
-  unsigned long long pad[5];
+  // bounds narrowed per round, three in rotation (the persistent kernel's
+  // handover to the event schedule)
+  unsigned long long joins[3];
+  unsigned long long pad[2];
 };
 
 constexpr unsigned BIT_CHANGED = 1u << 29;
@@ -73,7 +76,8 @@ static __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned
 // after the zeroing) is seen by every CTA before it can arrive at r + 2.  The
 // three words start at zero (the host clears the control block).  Every wait is
 // bounded by timeout_ns; on expiry the CTA records PIR_BARRIER_TIMEOUT in
-// ctl->status and the result carries BIT_ERROR.  With a heartbeat word `hb`
+// ctl->status and the result carries BIT_ERROR.  The result's low 20 bits
+// are the number of CTAs that reported a change (BIT_CHANGED: at least one).  With a heartbeat word `hb`
 // (a CTA working alone while the others wait), the limit runs from the last
 // change of *hb, and the waiters poll less often.
 static __device__ __noinline__ unsigned grid_sync_rot(Control *ctl, unsigned nblocks, long long round, int changed,
@@ -106,7 +110,8 @@ static __device__ __noinline__ unsigned grid_sync_rot(Control *ctl, unsigned nbl
     }
   }
   if (blockIdx.x == 0) ctl->rot[(round + 2) % 3][0] = 0ull;
-  unsigned r = 0;
+  // low 20 bits: how many CTAs reported a change in this round
+  unsigned r = (unsigned)((v >> 20) & 0xFFFFFull);
   if ((v >> 20) & 0xFFFFFull) r |= BIT_CHANGED;
   if ((v >> 40) & 0xFFFFFull) r |= BIT_FAILED;
   if (*(volatile int *)&ctl->status) r |= BIT_ERROR;

@@ -56,13 +56,26 @@ struct SchedState {
   float *d_tx = nullptr, *d_ty = nullptr;  // trace samples
   long long tcap = 0, tcount = 0;
   std::vector<int> dirty;  // variables embedded since the last learned fixpoint
+  // learned rounds on a frontier (k_learned_local): the store was a fixpoint
+  // of bytecode version base_bc at store version base_version, and `since`
+  // lists the variables embedded after it (since_ok: all of them)
+  long long base_version = -1, base_bc = -1;
+  std::vector<int> since;
+  bool since_ok = false;
+  unsigned *d_vlast = nullptr, *d_pstamp = nullptr;
+  int *d_lf = nullptr, *d_cv = nullptr, *d_since = nullptr, *d_nv = nullptr;
+  float *d_lscore = nullptr;
+  long long loc_bc_version = -1, loc_n = -1;
+  int loc_nvars = -1;
+  unsigned loc_base = 65;
 };
 
 void destroy_sched_state(pirgpu_ctx *ctx) {
   SchedState *s = ctx->sched;
   if (!s) return;
-  void *ptrs[] = {s->d_param, s->d_m, s->d_v, s->d_grad, s->d_loss, s->d_wbf, s->d_var_last, s->d_deg,
-                  s->d_pdeg, s->d_score, s->d_counts, s->d_tx, s->d_ty};
+  void *ptrs[] = {s->d_param, s->d_m,      s->d_v,  s->d_grad, s->d_loss, s->d_wbf,     s->d_var_last,
+                  s->d_deg,   s->d_pdeg,   s->d_score, s->d_counts, s->d_tx, s->d_ty, s->d_vlast,
+                  s->d_pstamp, s->d_lf,    s->d_cv, s->d_since, s->d_lscore, s->d_nv};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete s;
@@ -401,6 +414,301 @@ __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
   }
 }
 
+// ------------------------------------------- learned rounds on a frontier ----
+//
+// The learned schedule for a store that was a fixpoint before a few
+// embeddings (a search node: snapshot, embed the branching bounds, fixpoint).
+// Only the propagators of variables narrowed since can narrow anything, so a
+// round scores only its frontier -- the propagators of the variables the
+// previous round narrowed, and those deferred -- and the whole run fits one
+// CTA (rounds separated by __syncthreads, no grid barrier).  A round wakes the
+// frontier entries the network gives a logit of at least 0, and at least the
+// top `frac` of the frontier; the others are deferred to the next round (so
+// every listed propagator runs at least once after its last listing, and a
+// propagator listed in several rounds may run once).  A run that narrows a
+// variable lists the variable's propagators for the next round (once per
+// round: the first join of a round lists them all).  When the frontier is
+// empty, a certifying round runs, trusting none of the bookkeeping, every
+// propagator of every variable embedded or narrowed in this run (the others
+// read only intervals of the fixpoint the run started from); if it narrows
+// something the rounds resume, else the store is the fixpoint, the same as
+// AC-1's bit for bit (propagators are monotone).  Round ids are absolute
+// (base + round) so that the per-propagator and per-variable stamps need no
+// clearing between runs.  A frontier or a set of narrowed variables beyond
+// the lists' capacity stops the run (LOC_OVERFLOW); the host then finishes
+// with the grid kernel, whose full certifying sweep does not depend on how
+// the store was reached.
+constexpr int LOC_BLOCK = 512;
+constexpr int LOC_FCAP = 1 << 16;   // entries of one frontier list
+constexpr int LOC_CVCAP = 1 << 16;  // variables embedded or narrowed in one run
+constexpr int LOC_SINCE_CAP = 1 << 14;  // embedded variables the host hands over
+constexpr int LOC_DONE = 1, LOC_FAILED = 2, LOC_CAP = 3, LOC_OVERFLOW = 4;
+
+struct LocalArgs {
+  const int4 *bc;                 // {op, x, y, z} per propagator
+  const int *adj_ptr, *adj;       // variable -> propagator adjacency
+  int2 *store;
+  unsigned *vlast;                // per variable: id of the round of its last narrowing (base: embedded)
+  unsigned *pstamp;               // per propagator: id of the last round it is listed for
+  const unsigned char *pdeg;
+  const __nv_bfloat16 *wbf;
+  int *F0, *F1;                   // frontier lists of even / odd rounds
+  float *score;                   // per frontier slot
+  int *cv;                        // variables embedded or narrowed in this run
+  int *nv;                        // variables narrowed in the current round
+  const int *since;               // the embedded variables
+  int nsince;
+  unsigned base;                  // id of round r: base + r
+  unsigned long long *counts;     // [0] executions of scored rounds, [1] of certifying rounds,
+                                  // [2] certifying rounds, [3] end state (LOC_*)
+  Control *ctl;
+  long long max_rounds;
+  float frac;
+};
+
+// Joins into the store; the first join of a round that narrows a variable
+// appends the variable to the round's list of narrowed variables (their
+// propagators are listed for the next round by expand_vars, by the whole CTA).
+struct FrontierStore {
+  int2 *s;
+  unsigned *vlast;
+  unsigned base, rid;  // this run, this round
+  int *nv, *nnv, *cv, *ncv, *over;
+  __device__ __forceinline__ Itv load(int v) const {
+    const int2 t = __ldcg(s + v);
+    return mk(t.x, t.y);
+  }
+  __device__ __forceinline__ int embed(int v, Itv seen, Itv r, int &failed) const {
+    int n = 0;
+    if (r.l > seen.l) {
+      asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(&s[v].x), "r"(r.l) : "memory");
+      ++n;
+    }
+    if (r.u < seen.u) {
+      asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(&s[v].y), "r"(r.u) : "memory");
+      ++n;
+    }
+    if (!n) return 0;
+    if (is_bot(mk(max(seen.l, r.l), min(seen.u, r.u)))) failed = 1;
+    const unsigned old = atomicMax(vlast + v, rid);
+    if (old < base) {
+      const int k = atomicAdd(ncv, 1);
+      if (k < LOC_CVCAP) cv[k] = v;
+      else *over = 1;
+    }
+    if (old < rid) {
+      const int k = atomicAdd(nnv, 1);
+      if (k < LOC_CVCAP) nv[k] = v;
+      else *over = 1;
+    }
+    return n;
+  }
+};
+
+// Exclusive prefix sum over the CTA (blockDim.x a multiple of 32, at most
+// 1,024); *total gets the sum.  Every thread must call it.
+__device__ __forceinline__ int block_excl_scan(int x, int *s_warp, int *total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int incl = x;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < nw ? s_warp[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nw) s_warp[lane] = w;
+  }
+  __syncthreads();
+  *total = s_warp[nw - 1];
+  const int r = incl - x + (warp ? s_warp[warp - 1] : 0);
+  __syncthreads();  // s_warp is free again
+  return r;
+}
+
+// The propagators of vars[0 .. count) listed as round `id`'s frontier (each
+// once: the per-propagator stamp), by the whole CTA: the adjacency entries of
+// up to blockDim.x variables at a time are flattened (a block scan of their
+// degrees) and spread over the threads, so the stamp atomics are issued in
+// parallel instead of one variable's entries after another.
+__device__ void expand_vars(const LocalArgs &a, const int *vars, int count, unsigned id, int *f, int *nf,
+                            int *over, int *s_off, int *s_start, int *s_warp) {
+  const int tid = threadIdx.x;
+  for (int c0 = 0; c0 < count; c0 += blockDim.x) {
+    const int m = min(count - c0, (int)blockDim.x);
+    int deg = 0, start = 0;
+    if (tid < m) {
+      const int v = vars[c0 + tid];
+      start = __ldg(a.adj_ptr + v);
+      deg = __ldg(a.adj_ptr + v + 1) - start;
+    }
+    int total = 0;
+    const int off = block_excl_scan(deg, s_warp, &total);
+    s_off[tid] = off;
+    s_start[tid] = start;
+    __syncthreads();
+    for (int j = tid; j < total; j += blockDim.x) {
+      int lo = 0, hi = m - 1;  // the last variable whose entries start at or before j
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_off[mid] <= j) lo = mid;
+        else hi = mid - 1;
+      }
+      const int p = __ldg(a.adj + s_start[lo] + (j - s_off[lo]));
+      if (atomicMax(a.pstamp + p, id) < id) {
+        const int k = atomicAdd(nf, 1);
+        if (k < LOC_FCAP) f[k] = p;
+        else *over = 1;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(LOC_BLOCK, 1) k_learned_local(LocalArgs a) {
+  __shared__ float sw[NPARAM];
+  __shared__ unsigned sh[HIST_BINS];
+  __shared__ __align__(16) __nv_bfloat16 s_tile[LOC_BLOCK / 32][32 * NF];
+  __shared__ int s_off[LOC_BLOCK], s_start[LOC_BLOCK], s_warp[32];
+  __shared__ int s_nf[2], s_ncv, s_nnv, s_over;
+  stage_weights(a.wbf, sw);
+  MmaWeights W;
+  W.load(a.wbf);
+  __nv_bfloat16 *tile = s_tile[threadIdx.x >> 5];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    s_nf[0] = s_nf[1] = 0;
+    s_ncv = 0;
+    s_nnv = 0;
+    s_over = 0;
+  }
+  __syncthreads();
+  // the embedded variables start the run (round 0) and list round 1
+  for (int i = tid; i < a.nsince; i += blockDim.x) {
+    const int v = a.since[i];
+    if (atomicMax(a.vlast + v, a.base) < a.base) {
+      const int k = atomicAdd(&s_ncv, 1);
+      if (k < LOC_CVCAP) a.cv[k] = v;
+      else s_over = 1;
+    }
+  }
+  __syncthreads();
+  expand_vars(a, a.cv, min(s_ncv, LOC_CVCAP), a.base + 1u, a.F1, &s_nf[1], &s_over, s_off, s_start, s_warp);
+  unsigned long long ex = 0, cex = 0, narrowed = 0;
+  long long round = 0;
+  int state = 0, certifying = 0, ncert = 0;
+  for (;;) {
+    ++round;
+    const int cur = (int)(round & 1), nxt = cur ^ 1;
+    int *F = cur ? a.F1 : a.F0, *Fn = cur ? a.F0 : a.F1;
+    const unsigned rid = a.base + (unsigned)round, nid = rid + 1u;
+    if (s_over) {
+      state = LOC_OVERFLOW;
+      break;
+    }
+    if (s_nf[cur] == 0) {
+      // certifying round: every propagator of every variable of this run
+      __syncthreads();
+      expand_vars(a, a.cv, min(s_ncv, LOC_CVCAP), rid, F, &s_nf[cur], &s_over, s_off, s_start, s_warp);
+      certifying = 1;
+      ++ncert;
+      if (s_over) {
+        state = LOC_OVERFLOW;
+        break;
+      }
+    }
+    const int n = min(s_nf[cur], LOC_FCAP);
+    for (int i = tid; i < HIST_BINS; i += blockDim.x) sh[i] = 0;
+    if (tid == 0) {
+      s_nf[nxt] = 0;
+      s_nnv = 0;
+    }
+    __syncthreads();
+    FrontierStore st{a.store, a.vlast, a.base, rid, a.nv, &s_nnv, a.cv, &s_ncv, &s_over};
+    int changed = 0, failed = 0;
+    int bin = 0;
+    // (A) scores of the frontier, 32 entries per warp and step (warp-uniform bound)
+    if (!certifying) {
+      for (int b = warp * 32; b < n; b += blockDim.x) {
+        const int i = b + lane;
+        float f[NF] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (i < n) {
+          const int p = F[i];
+          const int4 c = __ldg(a.bc + p);
+          const Itv ia = st.load(c.y), ib = st.load(c.z), ic = st.load(c.w);
+          const unsigned last = max(__ldcg(a.vlast + c.y), max(__ldcg(a.vlast + c.z), __ldcg(a.vlast + c.w)));
+          // rounds since a variable of the propagator last narrowed ("long ago" before this run)
+          const int since = last < a.base ? 64 : (int)min(rid - last, 64u);
+          features(c.x, ia, ib, ic, (int)round - since, (int)round, a.pdeg[p], f);
+        }
+        const float s = mlp_forward_mma(f, W, sw, tile);
+        if (i < n) {
+          a.score[i] = s;
+          atomicAdd(&sh[hist_bin(s)], 1u);
+        }
+      }
+      __syncthreads();
+      // (B) at least the top frac, and every entry with a logit >= 0
+      bin = min(select_bin(sh, a.frac), hist_bin(0.f));
+    }
+    // (C) the woken entries run, the others wait for the next round
+    for (int i = tid; i < n; i += blockDim.x) {
+      const int p = F[i];
+      if (!certifying && hist_bin(a.score[i]) < bin) {
+        if (atomicMax(a.pstamp + p, nid) < nid) {
+          const int k = atomicAdd(&s_nf[nxt], 1);
+          if (k < LOC_FCAP) Fn[k] = p;
+          else s_over = 1;
+        }
+        continue;
+      }
+      const int4 c = __ldg(a.bc + p);
+      const Itv ia = st.load(c.y), ib = st.load(c.z), ic = st.load(c.w);
+      changed += deduce_loaded(c.x, c.y, c.z, c.w, ia, ib, ic, st, failed);
+      if (certifying) ++cex;
+      else ++ex;
+    }
+    narrowed += changed;
+    const int any_ch = __syncthreads_or(changed);
+    const int any_f = __syncthreads_or(failed);
+    if (any_f) {
+      state = LOC_FAILED;
+      break;
+    }
+    if (certifying && !any_ch) {
+      state = LOC_DONE;
+      break;
+    }
+    certifying = 0;
+    if (a.max_rounds > 0 && round >= a.max_rounds) {
+      state = LOC_CAP;
+      break;
+    }
+    // the propagators of the variables this round narrowed, for the next round
+    expand_vars(a, a.nv, min(s_nnv, LOC_CVCAP), nid, Fn, &s_nf[nxt], &s_over, s_off, s_start, s_warp);
+  }
+  ex = warp_sum64(ex);
+  cex = warp_sum64(cex);
+  narrowed = warp_sum64(narrowed);
+  if (lane == 0) {
+    if (ex) atomicAdd(a.counts, ex);
+    if (cex) atomicAdd(a.counts + 1, cex);
+    if (narrowed) atomicAdd(&a.ctl->narrowed, narrowed);
+  }
+  if (tid == 0) {
+    a.counts[2] = (unsigned long long)ncert;
+    a.counts[3] = (unsigned long long)state;
+    a.ctl->rounds = round;
+    if (state == LOC_FAILED) a.ctl->failed = 1;
+    if (state == LOC_CAP) a.ctl->changed[0] = 1;
+  }
+}
+
 // One traced AC-1 round: features at the time each propagator is read, then
 // the propagator; label = it narrowed a bound.  Positives are always kept,
 // negatives with probability keep_neg (a hash of round and index).
@@ -669,17 +977,145 @@ int reset_stamps(pirgpu_ctx *ctx) {
 
 void note_embedded(pirgpu_ctx *ctx, const int32_t *var, int count) {
   SchedState *s = sched(ctx);
+  // the embedding that follows bumps the store version once: the chain from
+  // the last fixpoint goes on if nothing else changed the store in between
+  if (s->since_ok && s->base_version == ctx->store_version && s->base_bc == ctx->bytecode_version &&
+      s->since.size() + (size_t)count <= (size_t)LOC_SINCE_CAP) {
+    s->since.insert(s->since.end(), var, var + count);
+    s->base_version = ctx->store_version + 1;
+  } else {
+    s->since_ok = false;
+  }
   if (s->dirty.size() > (size_t)1 << 22) return;
   s->dirty.insert(s->dirty.end(), var, var + count);
 }
 
-int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
-  int r;
-  if ((r = ensure_params(ctx)) || (r = ensure_graph(ctx)) || (r = reset_stamps(ctx))) return r;
+void note_fixpoint(pirgpu_ctx *ctx) {
   SchedState *s = sched(ctx);
+  s->base_version = ctx->store_version;
+  s->base_bc = ctx->bytecode_version;
+  s->since.clear();
+  s->since_ok = true;
+}
+
+// Buffers of the frontier rounds: stamps sized to the bytecode and the store
+// (cleared when allocated; round ids only grow between runs), frontier lists,
+// scores, the run's variables and the embedded ones.
+static int ensure_local(pirgpu_ctx *ctx) {
+  SchedState *s = sched(ctx);
+  if (s->d_vlast && s->loc_bc_version == ctx->bytecode_version && s->loc_nvars == ctx->nvars && s->loc_n == ctx->n)
+    return PIR_OK;
+  void *ptrs[] = {s->d_vlast, s->d_pstamp, s->d_lf, s->d_cv, s->d_since, s->d_lscore, s->d_nv};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  s->d_vlast = s->d_pstamp = nullptr;
+  s->d_lf = s->d_cv = s->d_since = s->d_nv = nullptr;
+  s->d_lscore = nullptr;
+  const size_t nv = (size_t)std::max(ctx->nvars, 1), n = (size_t)std::max<long long>(ctx->n, 1);
+  if (cudaMalloc(&s->d_vlast, nv * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&s->d_pstamp, n * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&s->d_lf, 2 * (size_t)LOC_FCAP * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->d_cv, (size_t)LOC_CVCAP * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->d_nv, (size_t)LOC_CVCAP * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->d_since, (size_t)LOC_SINCE_CAP * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->d_lscore, (size_t)LOC_FCAP * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, PIR_ENOMEM, "learned frontier buffers");
+  }
+  PIR_CK(cudaMemsetAsync(s->d_vlast, 0, nv * sizeof(unsigned), ctx->stream));
+  PIR_CK(cudaMemsetAsync(s->d_pstamp, 0, n * sizeof(unsigned), ctx->stream));
+  s->loc_base = 65;
+  s->loc_bc_version = ctx->bytecode_version;
+  s->loc_nvars = ctx->nvars;
+  s->loc_n = ctx->n;
+  return PIR_OK;
+}
+
+// The learned rounds on a frontier (k_learned_local), from the fixpoint the
+// store was at before the embeddings in `since`.  *handed_over: the lists
+// overflowed, the grid kernel finishes the run (stats so far in *st).
+static int fixpoint_learned_local(pirgpu_ctx *ctx, const pir_opts &opts, float frac, pir_stats *st,
+                                  bool *handed_over) {
+  SchedState *s = sched(ctx);
+  int r;
+  EventsGraph g;
+  if ((r = events_graph(ctx, &g, false)) || (r = ensure_local(ctx))) return r;
+  if (s->loc_base > 0xF0000000u) {
+    PIR_CK(cudaMemsetAsync(s->d_vlast, 0, (size_t)std::max(ctx->nvars, 1) * sizeof(unsigned), ctx->stream));
+    PIR_CK(cudaMemsetAsync(s->d_pstamp, 0, (size_t)std::max<long long>(ctx->n, 1) * sizeof(unsigned), ctx->stream));
+    s->loc_base = 65;
+  }
+  const int nsince = (int)s->since.size();
+  if (nsince)
+    PIR_CK(cudaMemcpyAsync(s->d_since, s->since.data(), nsince * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   if ((r = reset_control(ctx))) return r;
   PIR_CK(cudaMemsetAsync(s->d_counts, 0, 4 * sizeof(unsigned long long), ctx->stream));
+  LocalArgs a;
+  a.bc = g.bc;
+  a.adj_ptr = g.adj_ptr;
+  a.adj = g.adj;
+  a.store = ctx->d_store;
+  a.vlast = s->d_vlast;
+  a.pstamp = s->d_pstamp;
+  a.pdeg = s->d_pdeg;
+  a.wbf = s->d_wbf;
+  a.F0 = s->d_lf;
+  a.F1 = s->d_lf + LOC_FCAP;
+  a.score = s->d_lscore;
+  a.cv = s->d_cv;
+  a.nv = s->d_nv;
+  a.since = s->d_since;
+  a.nsince = nsince;
+  a.base = s->loc_base;
+  a.counts = s->d_counts;
+  a.ctl = ctx->d_ctl;
+  a.max_rounds = opts.max_rounds > 0 ? opts.max_rounds : 0;
+  a.frac = frac;
+  PIR_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  k_learned_local<<<1, LOC_BLOCK, 0, ctx->stream>>>(a);
+  PIR_CK(cudaGetLastError());
+  PIR_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  Control h;
+  unsigned long long cnt[4];
+  PIR_CK(cudaMemcpyAsync(cnt, s->d_counts, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+  if ((r = read_control(ctx, &h))) return r;
+  std::memset(st, 0, sizeof(*st));
+  PIR_CK(cudaEventElapsedTime(&st->device_ms, ctx->ev0, ctx->ev1));
+  s->loc_base += (unsigned)h.rounds + 2u;
+  st->rounds = h.rounds;
+  st->narrowed = (int64_t)h.narrowed;
+  st->executions = (int64_t)(cnt[0] + cnt[1]);
+  st->certify_executions = (int64_t)cnt[1];
+  *handed_over = cnt[3] == (unsigned long long)LOC_OVERFLOW;
+  st->status = cnt[3] == (unsigned long long)LOC_FAILED ? PIR_FAILED
+               : cnt[3] == (unsigned long long)LOC_CAP  ? PIR_TIMEOUT
+                                                        : PIR_OK;
+  return PIR_OK;
+}
+
+int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
+  int r;
+  if ((r = ensure_params(ctx)) || (r = ensure_graph(ctx))) return r;
+  SchedState *s = sched(ctx);
   const float frac = opts.wake_fraction > 0.f ? std::min(opts.wake_fraction, 1.f) : 1.f / 16.f;
+  // pir_fixpoint bumped the store version once since the embeddings
+  pir_stats pre;
+  std::memset(&pre, 0, sizeof(pre));
+  if (opts.local_frontier >= 0 && s->since_ok && s->base_version + 1 == ctx->store_version &&
+      s->base_bc == ctx->bytecode_version) {
+    bool handed_over = false;
+    if ((r = fixpoint_learned_local(ctx, opts, frac, &pre, &handed_over))) return r;
+    if (!handed_over) {
+      s->dirty.clear();
+      if (pre.status == PIR_FAILED) ctx->failed = true;
+      ctx->at_fixpoint = pre.status == PIR_OK;
+      if (stats) *stats = pre;
+      return pre.status;
+    }
+  }
+  if ((r = reset_stamps(ctx))) return r;
+  if ((r = reset_control(ctx))) return r;
+  PIR_CK(cudaMemsetAsync(s->d_counts, 0, 4 * sizeof(unsigned long long), ctx->stream));
   LearnedArgs a;
   a.op = ctx->d_op;
   a.x = ctx->d_x;
@@ -713,9 +1149,11 @@ int fixpoint_learned(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   std::memset(&st, 0, sizeof(st));
   PIR_CK(cudaEventElapsedTime(&st.device_ms, ctx->ev0, ctx->ev1));
   // executions: woken propagators of the learned rounds + full certifying sweeps
-  st.rounds = h.rounds;
-  st.narrowed = (int64_t)h.narrowed;
-  st.executions = (int64_t)cnt[0] + (int64_t)cnt[1] * ctx->n;
+  st.rounds = h.rounds + pre.rounds;
+  st.narrowed = (int64_t)h.narrowed + pre.narrowed;
+  st.executions = (int64_t)cnt[0] + (int64_t)cnt[1] * ctx->n + pre.executions;
+  st.certify_executions = (int64_t)cnt[1] * ctx->n + pre.certify_executions;
+  st.device_ms += pre.device_ms;
   int status = h.status ? h.status : (h.failed ? PIR_FAILED : (h.changed[0] ? PIR_TIMEOUT : PIR_OK));
   st.status = status;
   if (status == PIR_FAILED) ctx->failed = true;

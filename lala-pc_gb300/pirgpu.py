@@ -38,7 +38,7 @@ class Opts(ctypes.Structure):
                 ("wake_fraction", ctypes.c_float), ("variant", ctypes.c_int32),
                 ("local_frontier", ctypes.c_int32), ("chase", ctypes.c_int32),
                 ("certify", ctypes.c_int32), ("segments", ctypes.c_int32), ("dense", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 1)]
+                ("lead", ctypes.c_int32)]
 
 
 class SearchOpts(ctypes.Structure):
@@ -173,11 +173,13 @@ def _c32(a):
 
 
 def make_opts(mode=MODE_AUTO, max_rounds=0, barrier_timeout_ns=0, block=0, ctas_per_sm=0,
-              sched=SCHED_AC1, wake_fraction=0.0, variant=0, local_frontier=0, chase=0, certify=0, segments=0, dense=0):
+              sched=SCHED_AC1, wake_fraction=0.0, variant=0, local_frontier=0, chase=0, certify=0, segments=0, dense=0,
+              lead=0):
     o = Opts()
     o.max_rounds, o.barrier_timeout_ns, o.mode, o.block = max_rounds, barrier_timeout_ns, mode, block
     o.ctas_per_sm, o.sched, o.wake_fraction, o.variant = ctas_per_sm, sched, wake_fraction, variant
     o.local_frontier, o.chase, o.certify, o.segments, o.dense = local_frontier, chase, certify, segments, dense
+    o.lead = lead
     return o
 
 

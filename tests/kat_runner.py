@@ -103,6 +103,7 @@ class GpuEngine:
 
     mode = 0  # pirgpu.MODE_AUTO; set per test
     sched = 0  # pirgpu.SCHED_AC1; set per test
+    opts = {}  # further fixpoint options, set per test
 
     def __init__(self, lb, ub):
         import pirgpu
@@ -122,7 +123,7 @@ class GpuEngine:
         return self.ctx.num_deductions()
 
     def fixpoint(self):
-        rc, _ = self.ctx.fixpoint(mode=self.mode, sched=self.sched)
+        rc, _ = self.ctx.fixpoint(mode=self.mode, sched=self.sched, **self.opts)
         return rc == self.P.FAILED
 
     def read(self):

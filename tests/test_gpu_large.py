@@ -68,7 +68,7 @@ def test_single_large_events_bit_exact(large, chase, segments):
     import pirgpu
     inst, lb, ub = large
     ctx = _ctx(inst)
-    rc, st = ctx.fixpoint(sched=pirgpu.SCHED_EVENTS, chase=chase, segments=segments)
+    rc, st = ctx.fixpoint(sched=pirgpu.SCHED_EVENTS, chase=chase, segments=segments, lead=-1)
     assert rc == pirgpu.OK
     _check(ctx, inst, lb, ub)
     n = ctx.num_deductions()
@@ -80,12 +80,26 @@ def test_single_large_events_bit_exact(large, chase, segments):
         assert st["rounds"] < 2_000
 
 
+def test_single_large_events_default_bit_exact(large):
+    """The event schedule as the benchmark runs it: AC-1 rounds first while
+    many CTAs still narrow something, then the event kernel on the chain."""
+    import pirgpu
+    inst, lb, ub = large
+    ctx = _ctx(inst)
+    ctx.autotune(16)  # the lead runs the tuned variant; the store is put back
+    rc, st = ctx.fixpoint(sched=pirgpu.SCHED_EVENTS)
+    assert rc == pirgpu.OK
+    _check(ctx, inst, lb, ub)
+    assert st["certify_executions"] > 0 and st["certify_narrowed"] == 0
+    assert st["rounds"] < 2_000
+
+
 def test_single_large_events_uncertified_agrees(large):
     """certify < 0 skips the final sweep: the same store, n fewer executions."""
     import pirgpu
     inst, lb, ub = large
     ctx = _ctx(inst)
-    rc, st = ctx.fixpoint(sched=pirgpu.SCHED_EVENTS, certify=-1)
+    rc, st = ctx.fixpoint(sched=pirgpu.SCHED_EVENTS, certify=-1, lead=-1)
     assert rc == pirgpu.OK
     assert st["certify_executions"] == 0 and st["certify_narrowed"] == 0
     _check(ctx, inst, lb, ub)

@@ -112,24 +112,70 @@ def _run_nodes(ctx, off, var, lb, ub, sched, nodes, **kw):
     return out
 
 
+# the learned rounds on the frontier of the embedded variables (one CTA), and
+# the grid kernel that scores every propagator every round
+PATHS = {"frontier": 0, "grid": -1}
+
+
 @pytest.mark.gpu
-def test_learned_fixpoint_is_the_plain_fixpoint():
+@pytest.mark.parametrize("path", PATHS)
+def test_learned_fixpoint_is_the_plain_fixpoint(path):
     """Untrained (random) weights: the schedule is poor but the certified
     result equals the AC-1 fixpoint bit for bit, failures included."""
     import pirgpu as P
     ctx, off, var, lb, ub = _nodes(P)
     nodes = range(24)
     plain = _run_nodes(ctx, off, var, lb, ub, P.SCHED_AC1, nodes)
-    learned = _run_nodes(ctx, off, var, lb, ub, P.SCHED_LEARNED, nodes, wake_fraction=0.05)
-    for (r0, l0, u0, _), (r1, l1, u1, _) in zip(plain, learned):
+    learned = _run_nodes(ctx, off, var, lb, ub, P.SCHED_LEARNED, nodes, wake_fraction=0.05,
+                         local_frontier=PATHS[path])
+    for (r0, l0, u0, _), (r1, l1, u1, s1) in zip(plain, learned):
         assert r0 == r1
         if r0 == P.OK:
             np.testing.assert_array_equal(l0, l1)
             np.testing.assert_array_equal(u0, u1)
+            assert s1["certify_executions"] > 0
 
 
 @pytest.mark.gpu
-def test_training_reduces_executions_and_keeps_the_fixpoint():
+def test_learned_frontier_needs_a_fixpoint_before_the_embeddings():
+    """The frontier rounds start from the variables embedded since the store
+    was last a fixpoint: after a store load (no fixpoint yet) the grid kernel
+    runs instead, and the result is the AC-1 fixpoint either way; a fixpoint,
+    then embeddings, then the learned fixpoint takes the frontier path, whose
+    executions are far fewer than one sweep."""
+    import pirgpu as P
+    import workloads as W
+    base = W.plain(20_000, 80_000, 10**6, 7)
+    ctx = P.Context(0)
+    ctx.load_store(base.lb, base.ub)
+    ctx.tell(base.op, base.x, base.y, base.z)
+    rc, st = ctx.fixpoint(sched=P.SCHED_LEARNED)
+    assert rc == P.OK and st["executions"] >= 80_000  # grid kernel: a full certifying sweep at least
+    l0, u0 = ctx.read_store()
+    ref = P.Context(0)
+    ref.load_store(base.lb, base.ub)
+    ref.tell(base.op, base.x, base.y, base.z)
+    assert ref.fixpoint()[0] == P.OK
+    l1, u1 = ref.read_store()
+    np.testing.assert_array_equal(l0, l1)
+    np.testing.assert_array_equal(u0, u1)
+    # branch on a few unfixed variables, as a search node does
+    free = np.nonzero(l0 < u0)[0][:8]
+    mid = l0[free] + (u0[free] - l0[free]) // 2
+    ctx.embed_many(free, l0[free], mid)
+    ref.embed_many(free, l1[free], mid)
+    rc, st = ctx.fixpoint(sched=P.SCHED_LEARNED)
+    rr, _ = ref.fixpoint()
+    assert rc == rr
+    assert st["executions"] < 80_000
+    if rc == P.OK:
+        np.testing.assert_array_equal(ctx.read_store()[0], ref.read_store()[0])
+        np.testing.assert_array_equal(ctx.read_store()[1], ref.read_store()[1])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", PATHS)
+def test_training_reduces_executions_and_keeps_the_fixpoint(path):
     """Train on change traces of the plain fixpoint (first 64 nodes), then
     compare on 32 held-out nodes: bit-exact results, and the trained network
     needs at least 2x fewer propagator executions than plain AC-1 rounds."""
@@ -142,7 +188,8 @@ def test_training_reduces_executions_and_keeps_the_fixpoint():
     assert loss[-1] < loss[0]
     held = range(train, 96)
     plain = _run_nodes(ctx, off, var, lb, ub, P.SCHED_AC1, held)
-    learned = _run_nodes(ctx, off, var, lb, ub, P.SCHED_LEARNED, held, wake_fraction=1 / 32)
+    learned = _run_nodes(ctx, off, var, lb, ub, P.SCHED_LEARNED, held, wake_fraction=1 / 32,
+                         local_frontier=PATHS[path])
     e0 = e1 = 0
     for (r0, l0, u0, s0), (r1, l1, u1, s1) in zip(plain, learned):
         assert r0 == r1
