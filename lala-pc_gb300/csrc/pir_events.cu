@@ -414,6 +414,122 @@ __device__ __forceinline__ void seg_run_add(const SegWork &w, SegStore &st, int 
   st.dirty = (st.dirty | s3.dirty) & ~bit;  // ADD is idempotent: not marked again by its own narrowings
 }
 
+// A segment that is a path of ADD links with a constant each: link k relates
+// chain variables v_k and v_{k+1} by v_{k+1} = v_k + d_k (d_k = c_k when
+// the link reads x = v_{k+1}, y or z = v_k, the other operand the constant
+// c_k; d_k = -c_k when it runs the other way), every constant a singleton
+// used by its link alone.  The sweeps' fixpoint of such a path is the
+// difference-constraint closure along it: with P_0 = 0, P_{k+1} = P_k + d_k,
+//   lb(v_j) = P_j + max_i (lb(v_i) - P_i),  ub(v_j) = P_j + min_i (ub(v_i) - P_i),
+// and the constants narrow nothing unless the path fails (max > min: every
+// variable empty).  Bounds within +-2^28 and constants within +-2^22 keep every
+// sum the sweeps would form inside int32, so none of their saturating steps
+// saturates and the closure is their fixpoint exactly.  Called by the whole
+// warp; returns (warp-uniform) whether it solved the segment, the failure in
+// `failed`.
+constexpr long long PATH_BOUND = 1ll << 28, PATH_CONST = 1ll << 22;
+
+__device__ __noinline__ bool seg_solve_path(SegWork &w, int np, int &failed) {
+  const int lane = threadIdx.x & 31;
+  int in[2] = {0, 0}, out[2] = {0, 0};
+  long long d[2] = {0, 0};
+  bool ok = true;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = lane + 32 * h;
+    if (k >= np) continue;
+    const unsigned c = (unsigned)w.code[k];
+    const int sx = (int)((c >> 8) & 0xFFu), sy = (int)((c >> 16) & 0xFFu), sz = (int)(c >> 24);
+    auto constant = [&](int s) {
+      return !(w.var[s] & SEG_BOUNDARY) && w.umask[s] == (1ull << k) && w.iv[s].x == w.iv[s].y;
+    };
+    const bool cy = constant(sy), cz = constant(sz);
+    if (cy == cz) {
+      ok = false;
+      continue;
+    }
+    in[h] = cz ? sy : sz;
+    out[h] = sx;
+    d[h] = cz ? w.iv[sz].x : w.iv[sy].x;
+    if (d[h] <= -PATH_CONST || d[h] >= PATH_CONST) ok = false;
+  }
+  if (!__all_sync(0xFFFFFFFFu, ok)) return false;
+  // orientation: forward when link k's input is link k - 1's output, reverse
+  // when link k's output is link k - 1's input
+  const int pin0 = __shfl_up_sync(0xFFFFFFFFu, in[0], 1), pout0 = __shfl_up_sync(0xFFFFFFFFu, out[0], 1);
+  int pin1 = __shfl_up_sync(0xFFFFFFFFu, in[1], 1), pout1 = __shfl_up_sync(0xFFFFFFFFu, out[1], 1);
+  const int last_in0 = __shfl_sync(0xFFFFFFFFu, in[0], 31), last_out0 = __shfl_sync(0xFFFFFFFFu, out[0], 31);
+  if (lane == 0) {
+    pin1 = last_in0;
+    pout1 = last_out0;
+  }
+  bool fwd = true, rev = true;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = lane + 32 * h;
+    if (k == 0 || k >= np) continue;
+    const int pi = h ? pin1 : pin0, po = h ? pout1 : pout0;
+    fwd = fwd && in[h] == po;
+    rev = rev && out[h] == pi;
+  }
+  fwd = __all_sync(0xFFFFFFFFu, fwd);
+  rev = __all_sync(0xFFFFFFFFu, rev);
+  if (fwd == rev) return false;  // neither (or a degenerate one-link path)
+  // the path's variables must be used by their links alone: v_{k+1} by links
+  // k and k + 1, v_0 by link 0
+  const int v0 = __shfl_sync(0xFFFFFFFFu, fwd ? in[0] : out[0], 0);
+  int vn[2];
+  ok = true;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = lane + 32 * h;
+    vn[h] = fwd ? out[h] : in[h];
+    if (k >= np) continue;
+    if (!fwd) d[h] = -d[h];
+    const unsigned long long want = (1ull << k) | (k + 1 < np ? 1ull << (k + 1) : 0ull);
+    if (w.umask[vn[h]] != want) ok = false;
+  }
+  if (lane == 0 && w.umask[v0] != 1ull) ok = false;
+  if (!__all_sync(0xFFFFFFFFu, ok)) return false;
+  // P_{k+1}: inclusive sums of d over links 0..k (two halves of 32)
+  long long s0 = d[0], s1 = d[1];
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long t0 = __shfl_up_sync(0xFFFFFFFFu, s0, o), t1 = __shfl_up_sync(0xFFFFFFFFu, s1, o);
+    if (lane >= o) {
+      s0 += t0;
+      s1 += t1;
+    }
+  }
+  s1 += __shfl_sync(0xFFFFFFFFu, s0, 31);
+  // max of lb - P and min of ub - P over v_0 .. v_np; every bound finite and small
+  long long mx = LLONG_MIN, mn = LLONG_MAX;
+  auto take = [&](int v, long long P) {
+    const int2 t = w.iv[v];
+    if (t.x == MINF || t.y == INF || t.x <= -PATH_BOUND || t.y >= PATH_BOUND || t.x >= PATH_BOUND ||
+        t.y <= -PATH_BOUND)
+      ok = false;
+    mx = max(mx, (long long)t.x - P);
+    mn = min(mn, (long long)t.y - P);
+  };
+  if (lane == 0) take(v0, 0);
+  if (lane < np) take(vn[0], s0);
+  if (lane + 32 < np) take(vn[1], s1);
+  if (!__all_sync(0xFFFFFFFFu, ok)) return false;
+  for (int o = 16; o; o >>= 1) {
+    mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+    mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+  }
+  if (mx > mn) {
+    failed = 1;
+    return true;
+  }
+  // the closure; every value lies within the variable's own bounds
+  if (lane == 0) w.iv[v0] = make_int2((int)mx, (int)mn);
+  if (lane < np) w.iv[vn[0]] = make_int2((int)(s0 + mx), (int)(s0 + mn));
+  if (lane + 32 < np) w.iv[vn[1]] = make_int2((int)(s1 + mx), (int)(s1 + mn));
+  return true;
+}
+
 // The lane's sweeps of a segment: each pass runs the marked propagators
 // forward, then backward; a mark set during a pass ahead of the current
 // position is run in that pass.  Returns the runs.
@@ -493,11 +609,18 @@ __device__ int run_segment(const EvFixArgs &a, const Sched &sc, int s, SegWork &
   }
   __syncwarp();
   int fl = 0, conv = 1;
+  // a path of ADD links with constants is solved in closed form by the warp
+  // (each link counted as one execution); anything else is swept by a lane
+  const bool solved = add_only && seg_solve_path(w, np, fl);
   if (lane == 0) {
-    SegStore st{w.iv, w.umask, start};
-    const unsigned long long ex = add_only ? seg_sweep<true>(w, st, fl) : seg_sweep<false>(w, st, fl);
-    conv = st.dirty == 0ull;
-    execs += ex;
+    if (solved) {
+      execs += (unsigned long long)np;
+    } else {
+      SegStore st{w.iv, w.umask, start};
+      const unsigned long long ex = add_only ? seg_sweep<true>(w, st, fl) : seg_sweep<false>(w, st, fl);
+      conv = st.dirty == 0ull;
+      execs += ex;
+    }
   }
   __syncwarp();
   fl = __shfl_sync(0xFFFFFFFFu, fl, 0);

@@ -374,3 +374,62 @@ def test_events_dense_rounds(dense, P, oracle):
             if orc == oracle.OK:
                 np.testing.assert_array_equal(g, o)
                 assert st["certify_narrowed"] == 0
+
+
+def _add_path(n_links, seed, reverse=False, const_first=False, sign=1, first=(0, 10**6), last=None,
+              scale=10**6, extra=0):
+    """A path of ADD links over fresh variables v_0 .. v_n with a singleton
+    constant per link: v_{i+1} = v_i + c_i, written as x = v_{i+1}, y = v_i,
+    z = c_i (reverse: x = v_i, y = v_{i+1}, so v_i = v_{i+1} + c_i;
+    const_first: the constant as y), c_i = sign * U[1, 4]; optionally a random
+    instance of `extra` propagators beside it."""
+    import workloads as W
+    rng = np.random.default_rng(seed)
+    base = W.plain(max(extra // 4, 8), extra, 1000, seed) if extra else None
+    n0 = base.nvars if base else 0
+    v = n0 + np.arange(n_links + 1)
+    cv = n0 + n_links + 1 + np.arange(n_links)
+    c = sign * rng.integers(1, 5, n_links)
+    lb = np.full(2 * n_links + 1, -scale, np.int64)
+    ub = np.full(2 * n_links + 1, scale, np.int64)
+    lb[n_links + 1:] = ub[n_links + 1:] = c
+    lb[0], ub[0] = first
+    if last is not None:
+        lb[n_links], ub[n_links] = last
+    xo, yo = (v[:-1], v[1:]) if reverse else (v[1:], v[:-1])
+    yy, zz = (cv, yo) if const_first else (yo, cv)
+    op = np.zeros(n_links, np.int64)
+    if base:
+        return W.Instance(np.concatenate([base.lb, lb]), np.concatenate([base.ub, ub]),
+                          np.concatenate([base.op, op]), np.concatenate([base.x, xo]),
+                          np.concatenate([base.y, yy]), np.concatenate([base.z, zz]))
+    return W.Instance(lb, ub, op, xo, yy, zz)
+
+
+@pytest.mark.parametrize("case", ["forward", "reverse", "const_first", "reverse_const_first", "negative",
+                                  "infeasible", "huge_bounds", "with_random"])
+@pytest.mark.parametrize("lead", [-1, 0])
+def test_events_add_paths(case, lead, P, oracle):
+    """Paths of ADD links with constants, which the event kernel's segments
+    solve in closed form (the difference-constraint closure along the path)
+    when their bounds are small, else sweep: the oracle's store and failure
+    flag in every orientation, with the constants as either operand,
+    negative constants, an infeasible path and bounds beyond 2^28."""
+    kw = dict(reverse=case.startswith("reverse"), const_first=case.endswith("const_first"))
+    if case == "negative":
+        kw["sign"] = -1
+    if case == "infeasible":
+        kw.update(first=(0, 0), last=(0, 10))  # v_n >= n while v_n <= 10
+    if case == "huge_bounds":
+        kw.update(scale=1 << 29, first=(0, 1 << 29))
+    if case == "with_random":
+        kw["extra"] = 8000
+    inst = _add_path(3000, 31, **kw)
+    rc, store, st, orc, s, info = _both(P, oracle, inst, lead=lead)
+    assert rc == orc
+    if case == "infeasible":
+        assert rc == P.FAILED
+    else:
+        assert rc == P.OK
+        np.testing.assert_array_equal(store, s)
+        assert st["certify_narrowed"] == 0
