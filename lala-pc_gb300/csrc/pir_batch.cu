@@ -1895,7 +1895,12 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   // per SM) but fits a cluster's go to the cluster kernel, the rest to the
   // one-CTA-per-instance kernel; `order` lists the cluster ones first.
   const int small_cap = (std::min(ctx->smem_optin, (int)((228 * 1024) / 2) - 2048) / 16) * 16;
-  const int clu_cap = (ctx->smem_optin / 16) * 16 - 1024;
+  void (*kinst)(InstArgs) = marks ? k_instances<true> : k_instances<false>;
+  void (*kclu)(CluArgs) = marks ? k_instances_cluster<true> : k_instances_cluster<false>;
+  // the cluster kernel's dynamic shared memory: what its static arrays leave
+  cudaFuncAttributes clu_attr{};
+  PIR_CK(cudaFuncGetAttributes(&clu_attr, (const void *)kclu));
+  const int clu_cap = ((ctx->smem_optin - (int)clu_attr.sharedSizeBytes) / 16) * 16 - 1024;
   int nbig = 0;
   if (opts.mode != PIR_MODE_SMEM) {
     std::vector<int> big, rest;
@@ -1934,8 +1939,6 @@ extern "C" int pir_fixpoint_instances(pirgpu_ctx *ctx, int32_t ninst, const int6
   // memory let that many stay resident; each gets an equal share of the SM's
   // shared memory.
   int per_sm = opts.ctas_per_sm > 0 ? opts.ctas_per_sm : 2;
-  void (*kinst)(InstArgs) = marks ? k_instances<true> : k_instances<false>;
-  void (*kclu)(CluArgs) = marks ? k_instances_cluster<true> : k_instances_cluster<false>;
   int smem = 0;
   for (;;) {
     smem = std::min(ctx->smem_optin, (int)((228 * 1024) / per_sm) - 2048);
