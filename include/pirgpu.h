@@ -103,7 +103,7 @@ typedef struct pir_opts {
                                  round and the certifying sweep */
   int32_t lead;               /* pir_fixpoint's event schedule: AC-1 rounds of the persistent kernel run first, until
                                  a round whose narrowed bounds have not shrunk by an eighth against the round lead
-                                 rounds before (0: 16; at most 64): a steady trickle, such as a long chain, goes to
+                                 rounds before (0: 8; at most 64): a steady trickle, such as a long chain, goes to
                                  the event kernel, which continues from that store (a lead that reaches the
                                  fixpoint ends the run: its last round narrowed nothing); < 0, or
                                  opts.max_rounds > 0: the event kernel from the start */

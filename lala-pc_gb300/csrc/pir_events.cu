@@ -1266,7 +1266,7 @@ int fixpoint_events(pirgpu_ctx *ctx, const pir_opts &opts, pir_stats *stats) {
   std::memset(&lead, 0, sizeof(lead));
   if (opts.lead >= 0 && opts.max_rounds <= 0) {
     bool done = false;
-    if ((r = ac1_lead(ctx, opts, opts.lead > 0 ? opts.lead : 16, &lead, &done))) return r;
+    if ((r = ac1_lead(ctx, opts, opts.lead > 0 ? opts.lead : 8, &lead, &done))) return r;
     if (done) {
       if (lead.status == PIR_FAILED) ctx->failed = true;
       ctx->at_fixpoint = lead.status == PIR_OK;

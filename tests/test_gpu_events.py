@@ -340,7 +340,7 @@ def test_kat_events_with_lead(case, P):
 def test_events_ac1_lead(lead, P, oracle):
     """The event schedule's default start: AC-1 rounds of the persistent
     kernel until a round whose narrowed bounds have not shrunk by an eighth
-    against the round `lead` rounds before (0: 16), then the event kernel
+    against the round `lead` rounds before (0: 8), then the event kernel
     from that store.  A random instance (the lead may reach the fixpoint
     alone, its last round then being the certifying sweep), the same with a
     2,000-link chain, and a 5,000-link chain with little else (the chain's

@@ -199,3 +199,41 @@ def test_training_reduces_executions_and_keeps_the_fixpoint(path):
         e0 += s0["executions"]
         e1 += s1["executions"]
     assert e1 * 2 <= e0, (e0, e1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nembed", [10_000, 20_000])
+def test_learned_frontier_overflow_hands_over(nembed):
+    """Many embedded variables: with 10,000 the frontier outgrows the one-CTA
+    lists (65,536 entries) and the grid kernel finishes the run from the
+    store reached so far; with 20,000 the embedded variables exceed what the
+    host hands over (16,384) and the grid kernel runs from the start.  The
+    AC-1 fixpoint either way."""
+    import pirgpu as P
+    import workloads as W
+    base = W.plain(100_000, 400_000, 10**6, 9)
+    ctx = P.Context(0)
+    ctx.load_store(base.lb, base.ub)
+    ctx.tell(base.op, base.x, base.y, base.z)
+    assert ctx.fixpoint()[0] == P.OK
+    l0, u0 = ctx.read_store()
+    free = np.nonzero(l0 < u0)[0][:nembed]
+    assert len(free) == nembed
+    # bisect each toward the half holding the planted solution: the node stays feasible
+    hidden = base.meta["hidden"][free]
+    mid = l0[free] + (u0[free] - l0[free]) // 2
+    lo = np.where(hidden <= mid, l0[free], mid + 1)
+    hi = np.where(hidden <= mid, mid, u0[free])
+    snap = ctx.snapshot()
+    out = []
+    for sched, kw in ((P.SCHED_AC1, {}), (P.SCHED_LEARNED, {"wake_fraction": 0.25})):
+        ctx.restore(snap)
+        ctx.embed_many(free, lo, hi)
+        rc, st = ctx.fixpoint(sched=sched, mode=1, **kw)
+        out.append((rc, ctx.read_store(), st))
+    (r0, (a0, b0), s0), (r1, (a1, b1), s1) = out
+    assert r0 == r1 == P.OK
+    np.testing.assert_array_equal(a0, a1)
+    np.testing.assert_array_equal(b0, b1)
+    # the grid kernel's full certifying sweep ran
+    assert s1["certify_executions"] >= 400_000
