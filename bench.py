@@ -398,6 +398,15 @@ def nodes_record(cr, args):
     dev_ms = float(np.median([r["device_ms"] for r in runs]))
     value = nn / (dev_ms / 1e3)
     st = runs[0]
+    # the same batch without the per-node certifying sweeps (opts.certify < 0):
+    # the node kernel's own rounds; the statuses must be the certified ones
+    unc = []
+    for _ in range(5):
+        s_unc, _, _, _, st_unc = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=pirgpu.SCHED_EVENTS,
+                                                    certify=-1)
+        unc.append(st_unc)
+        cr.flush_l2()
+    unc_ms = float(np.median([r["device_ms"] for r in unc]))
     _, _, _, _, st_ac1 = ctx.fixpoint_nodes(off, var, lb, ub, want_stores=False, sched=pirgpu.SCHED_AC1)
     snap = ctx.snapshot()
     ctx.autotune(8)
@@ -437,6 +446,9 @@ def nodes_record(cr, args):
         "value": value, "unit": "nodes/s", "ms_per_batch": dev_ms, "schedule": "events (certified)",
         "node_kernel_variant": list(tuned), "executions_per_batch": st["executions"],
         "certify": {"executions": st["certify_executions"], "narrowed": st["certify_narrowed"]},
+        "uncertified": {"ms_per_batch": unc_ms, "nodes_per_s": nn / (unc_ms / 1e3),
+                        "executions_per_batch": unc[0]["executions"],
+                        "statuses_equal_to_certified": bool(np.array_equal(s_unc, status))},
         "max_rounds": int(rounds.max()), "nodes_failed": int((status == pirgpu.FAILED).sum()),
         "batched_ac1": {"ms_per_batch": st_ac1["device_ms"], "nodes_per_s": nn / (st_ac1["device_ms"] / 1e3),
                         "executions_per_batch": st_ac1["executions"]},
