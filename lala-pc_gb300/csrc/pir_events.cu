@@ -19,12 +19,19 @@
 // a path joined by link variables (variables with exactly two occurrences,
 // pir_segments.h).  A thread runs a propagator; a warp runs a segment: it
 // stages the segment's variables in shared memory, one lane sweeps the
-// segment's propagators forward and backward until none narrows anything,
-// and the warp joins what changed into the store and lists the units of the
-// changed variables that have occurrences outside the segment.  A segment
+// segment's propagators forward and backward until none narrows anything (a
+// path of ADD links with constants is solved by the warp in closed form
+// instead, seg_solve_path), and the warp joins what changed into the store
+// and lists the units of the changed variables that have occurrences outside
+// the segment.  A segment
 // reached through a link variable is run at once by the same warp (chasing,
 // SEG_CHASE per entry).  A long chain x_{i+1} = x_i + c_i then costs a few
 // shared-memory accesses per link instead of dependent L2 round trips.
+//
+// Before this kernel, fixpoint_events runs AC-1 rounds of the persistent
+// kernel while the bounds they narrow keep shrinking (ac1_lead, opts.lead):
+// this kernel's dense rounds cost several AC-1 rounds, and the lead hands it
+// the store once what is left is a steady trickle.
 //
 // Rounds with a large frontier run on the whole grid, separated by the grid
 // barrier.  A round whose frontier has at most `local_max` units runs on CTA

@@ -425,9 +425,10 @@ __global__ void __launch_bounds__(256) k_fixpoint_learned(LearnedArgs a) {
 // frontier entries the network gives a logit of at least 0, and at least the
 // top `frac` of the frontier; the others are deferred to the next round (so
 // every listed propagator runs at least once after its last listing, and a
-// propagator listed in several rounds may run once).  A run that narrows a
-// variable lists the variable's propagators for the next round (once per
-// round: the first join of a round lists them all).  When the frontier is
+// propagator listed in several rounds may run once).  The first join of a
+// round that narrows a variable puts the variable on the round's list, and
+// after the round the CTA lists those variables' propagators for the next
+// round (expand_vars).  When the frontier is
 // empty, a certifying round runs, trusting none of the bookkeeping, every
 // propagator of every variable embedded or narrowed in this run (the others
 // read only intervals of the fixpoint the run started from); if it narrows
